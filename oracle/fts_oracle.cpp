@@ -1,0 +1,713 @@
+// ORACLE — test infrastructure only.
+//
+// A CPU restatement (C++/OpenMP, FP64, no Eigen) of fluidtissue's per-time-step
+// P1-P1 Brezzi-Pitkaranta-stabilised Stokes solve, used as the parity checker
+// and as the timed CPU baseline.  Only tests, the smoke check and the benchmark's
+// CPU-baseline / reference arm may load it; the product path never does.
+//
+// Parity unpinned: the reference needs Eigen, CGAL, TBB and GMP, none of which
+// exists on this machine, so it cannot be built and has no tests or golden
+// vectors of its own.  This file restates its algorithm line by line (citations
+// below, paths relative to the reference project) and is pinned instead by
+// known-answer identities (mass = volume, K*const = 0, row sums of D = 0, ...)
+// and by a direct sparse solve of the same system in the tests.
+//
+// Restated reference pieces:
+//  * float-rounded P1 shape-function table at the 4-point degree-2 rule
+//      src/fem/Quadrature.hpp:24-36, :102-112; src/fem/Tetrahedron.hpp:17-18, :27-51
+//  * element geometry (detB = |det B|, invB^T)        src/fem/Assembler.hpp:430-462
+//  * node-row gather assembly, row = test, col = trial src/fem/Assembler.hpp:134-229
+//      h = (float)cbrt(detB) :193, integral = feval.dot(qw/6)*detB :143, :218
+//  * weak forms and block composition                  src/growth/Flow.cpp:54-72, :135-203
+//  * restriction to interior velocity + all pressure   src/growth/Flow.cpp:35-44, :206;
+//                                                      src/fem/MathTypes.hpp:52-94
+//  * interior dofs = nodes not on boundary triangles   src/fem/TetraMesh.cpp:266-269
+//  * source, zero mean, RHS                            src/growth/Flow.cpp:365-399
+//  * viscosity profiles                                src/growth/ViscosityProfiles.hpp:27-72
+//  * interior nodes / elements (strict phi < 0)        src/fem/LevelSet.cpp:180-211
+//  * un-preconditioned BiCGSTAB with ||r||/||b|| stop  src/growth/Flow.hpp:62, Flow.cpp:77-82, :266-285
+//      (Eigen's BiCGSTAB, external and not vendored; restated from van der Vorst 1992)
+//  * scatter to [ux(np), uy(np), uz(np), p(np)]        src/growth/Flow.cpp:290-300
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Reference element tables
+// ---------------------------------------------------------------------------
+
+// phi[a][q]: P1 basis a at quadrature point q, evaluated the way the reference
+// does: the points are double, passed through std::function<float(float,float,
+// float)>, so the arguments and the result are float while the expression
+// 1.0 - x - y - z runs in double (Tetrahedron.hpp:27-31, Quadrature.hpp:108-112).
+struct RefTables {
+    double phi[4][4];
+    double qw;  // 0.25 / 6.0 (Assembler.hpp:143)
+    RefTables() {
+        double a = (5.0 + 3.0 * std::sqrt(5.0)) / 20.0;
+        double b = (5.0 - std::sqrt(5.0)) / 20.0;
+        double qp[3][4] = {{a, b, b, b}, {b, a, b, b}, {b, b, a, b}};
+        for (int q = 0; q < 4; ++q) {
+            float x = (float)qp[0][q], y = (float)qp[1][q], z = (float)qp[2][q];
+            phi[0][q] = (double)(float)(1.0 - x - y - z);
+            phi[1][q] = (double)x;
+            phi[2][q] = (double)y;
+            phi[3][q] = (double)z;
+        }
+        qw = 0.25 / 6.0;
+    }
+};
+const RefTables& tables() {
+    static RefTables t;
+    return t;
+}
+
+// (f0 q + f1 q + f2 q + f3 q) * detB with a pairwise reduction of the
+// 4-vector dot product.
+inline double integ(const double f[4], double qw, double detB) {
+    return ((f[0] * qw + f[2] * qw) + (f[1] * qw + f[3] * qw)) * detB;
+}
+
+// Element geometry (Assembler.hpp:430-462): B = [p2-p1, p3-p1, p4-p1] from the
+// float coordinates cast to double, detB = |det B|, invB^T; g[j] = invB^T * ghat_j
+// with ghat = (-1,-1,-1), e_x, e_y, e_z (Tetrahedron.hpp:33-50).
+struct Geom {
+    double detB;
+    double g[4][3];
+    float h;
+};
+
+inline bool element_geom(const float* xyz, const int32_t* t, Geom& G) {
+    double p[4][3];
+    for (int j = 0; j < 4; ++j)
+        for (int a = 0; a < 3; ++a) p[j][a] = (double)xyz[3 * (int64_t)t[j] + a];
+    double B[3][3];
+    for (int a = 0; a < 3; ++a) {
+        B[a][0] = p[1][a] - p[0][a];
+        B[a][1] = p[2][a] - p[0][a];
+        B[a][2] = p[3][a] - p[0][a];
+    }
+    double c00 = B[1][1] * B[2][2] - B[1][2] * B[2][1];
+    double c01 = B[1][2] * B[2][0] - B[1][0] * B[2][2];
+    double c02 = B[1][0] * B[2][1] - B[1][1] * B[2][0];
+    double det = B[0][0] * c00 + B[0][1] * c01 + B[0][2] * c02;
+    G.detB = std::fabs(det);
+    if (G.detB == 0.0) return false;
+    // inverse = adj(B)/det; (invB^T)(r,c) = inv(c,r) = cof(r,c)/det
+    double cof[3][3];
+    cof[0][0] = c00;
+    cof[0][1] = c01;
+    cof[0][2] = c02;
+    cof[1][0] = B[0][2] * B[2][1] - B[0][1] * B[2][2];
+    cof[1][1] = B[0][0] * B[2][2] - B[0][2] * B[2][0];
+    cof[1][2] = B[0][1] * B[2][0] - B[0][0] * B[2][1];
+    cof[2][0] = B[0][1] * B[1][2] - B[0][2] * B[1][1];
+    cof[2][1] = B[0][2] * B[1][0] - B[0][0] * B[1][2];
+    cof[2][2] = B[0][0] * B[1][1] - B[0][1] * B[1][0];
+    double it[3][3];  // invB^T
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) it[r][c] = cof[r][c] / det;
+    for (int r = 0; r < 3; ++r) {
+        G.g[0][r] = -it[r][0] - it[r][1] - it[r][2];
+        G.g[1][r] = it[r][0];
+        G.g[2][r] = it[r][1];
+        G.g[3][r] = it[r][2];
+    }
+    G.h = (float)std::cbrt(G.detB);  // Assembler.hpp:193
+    return true;
+}
+
+// Per node pair (i,j) quantities accumulated by the row gather for row i.
+// K[al][be]: velocity block of the composed system (Flow.cpp:160-184):
+//   K[0][0]=A11(i,j) K[0][1]=A12(i,j) K[0][2]=A13(i,j)
+//   K[1][0]=A12(j,i) K[1][1]=A22(i,j) K[1][2]=A23(i,j)
+//   K[2][0]=A13(j,i) K[2][1]=A23(j,i) K[2][2]=A33(i,j)
+// Bv[al] = B_al(i,j) (velocity test i, pressure trial j), Bp[al] = B_al(j,i),
+// M = M(i,j), D = D(i,j), C[al] = C_al(i,j) (2/3 mu weighted, Flow.cpp:383-390).
+struct PairVals {
+    double K[3][3];
+    double Bv[3], Bp[3];
+    double M, D;
+    double C[3];
+};
+
+struct Topology {
+    int64_t np = 0, nt = 0;
+    std::vector<int64_t> p2t_ptr;  // np+1
+    std::vector<int32_t> p2t;      // 4 nt, ascending tet index per node
+    std::vector<int64_t> nb_ptr;   // np+1
+    std::vector<int32_t> nb;       // sorted node neighbours incl. self
+};
+
+void build_topology(int64_t np, int64_t nt, const int32_t* tets, Topology& T) {
+    T.np = np;
+    T.nt = nt;
+    T.p2t_ptr.assign(np + 1, 0);
+    for (int64_t e = 0; e < 4 * nt; ++e) T.p2t_ptr[tets[e] + 1]++;
+    for (int64_t i = 0; i < np; ++i) T.p2t_ptr[i + 1] += T.p2t_ptr[i];
+    T.p2t.resize(4 * nt);
+    std::vector<int64_t> fill(T.p2t_ptr.begin(), T.p2t_ptr.end() - 1);
+    for (int64_t k = 0; k < nt; ++k)
+        for (int j = 0; j < 4; ++j) T.p2t[fill[tets[4 * k + j]]++] = (int32_t)k;
+    std::vector<int32_t> cnt(np);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t i = 0; i < np; ++i) {
+        int32_t buf[512];
+        int n = 0;
+        for (int64_t q = T.p2t_ptr[i]; q < T.p2t_ptr[i + 1] && n < 508; ++q)
+            for (int j = 0; j < 4; ++j) buf[n++] = tets[4 * (int64_t)T.p2t[q] + j];
+        std::sort(buf, buf + n);
+        cnt[i] = (int32_t)(std::unique(buf, buf + n) - buf);
+    }
+    T.nb_ptr.assign(np + 1, 0);
+    for (int64_t i = 0; i < np; ++i) T.nb_ptr[i + 1] = T.nb_ptr[i] + cnt[i];
+    T.nb.resize(T.nb_ptr[np]);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t i = 0; i < np; ++i) {
+        int32_t buf[512];
+        int n = 0;
+        for (int64_t q = T.p2t_ptr[i]; q < T.p2t_ptr[i + 1] && n < 508; ++q)
+            for (int j = 0; j < 4; ++j) buf[n++] = tets[4 * (int64_t)T.p2t[q] + j];
+        std::sort(buf, buf + n);
+        int u = (int)(std::unique(buf, buf + n) - buf);
+        std::copy(buf, buf + u, T.nb.begin() + T.nb_ptr[i]);
+    }
+}
+
+inline int find_col(const int32_t* cols, int n, int32_t c) {
+    const int32_t* p = std::lower_bound(cols, cols + n, c);
+    return (p != cols + n && *p == c) ? (int)(p - cols) : -1;
+}
+
+// Row gather of all pair quantities of row i (Assembler.hpp:150-225).
+// mu: per element viscosity (data[k], Assembler.hpp:171-173).
+bool gather_row(int64_t i, const Topology& T, const float* xyz, const int32_t* tets,
+                const double* mu, std::vector<PairVals>& row) {
+    const RefTables& R = tables();
+    const double qw = R.qw;
+    const int32_t* cols = T.nb.data() + T.nb_ptr[i];
+    int ncol = (int)(T.nb_ptr[i + 1] - T.nb_ptr[i]);
+    row.assign(ncol, PairVals());
+    for (auto& pv : row) std::memset(&pv, 0, sizeof(PairVals));
+    bool ok = true;
+    for (int64_t q = T.p2t_ptr[i]; q < T.p2t_ptr[i + 1]; ++q) {
+        int64_t k = T.p2t[q];
+        const int32_t* t = tets + 4 * k;
+        Geom G;
+        if (!element_geom(xyz, t, G)) {
+            ok = false;
+            continue;
+        }
+        double Ve = mu ? mu[k] : 1.0;
+        double Vc = 2.0 / 3 * Ve;  // 2.0/3*mu (Flow.cpp:386)
+        float hh = G.h * G.h;       // (h*h) in float (Flow.cpp:195)
+        int a = 0;
+        if (t[1] == i) a = 1;
+        else if (t[2] == i) a = 2;
+        else if (t[3] == i) a = 3;
+        const double* ga = G.g[a];
+        const double* va = R.phi[a];
+        for (int b = 0; b < 4; ++b) {
+            int slot = find_col(cols, ncol, t[b]);
+            PairVals& P = row[slot];
+            const double* gb = G.g[b];
+            const double* ub = R.phi[b];
+            double f[4];
+            // A11..A33 and the transposed off-diagonals (Flow.cpp:136-153)
+            double kxx = ((2.0 * gb[0]) * ga[0] + gb[1] * ga[1] + gb[2] * ga[2]) * Ve;
+            double kyy = (gb[0] * ga[0] + (2.0 * gb[1]) * ga[1] + gb[2] * ga[2]) * Ve;
+            double kzz = (gb[0] * ga[0] + gb[1] * ga[1] + (2.0 * gb[2]) * ga[2]) * Ve;
+            double kxy = (gb[0] * ga[1]) * Ve;  // A12(i,j): ux.*vy
+            double kxz = (gb[0] * ga[2]) * Ve;  // A13(i,j)
+            double kyz = (gb[1] * ga[2]) * Ve;  // A23(i,j)
+            double kyx = (ga[0] * gb[1]) * Ve;  // A12(j,i)
+            double kzx = (ga[0] * gb[2]) * Ve;  // A13(j,i)
+            double kzy = (ga[1] * gb[2]) * Ve;  // A23(j,i)
+            double kv[3][3] = {{kxx, kxy, kxz}, {kyx, kyy, kyz}, {kzx, kzy, kzz}};
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) {
+                    for (int qq = 0; qq < 4; ++qq) f[qq] = kv[r][c];
+                    P.K[r][c] += integ(f, qw, G.detB);
+                }
+            for (int al = 0; al < 3; ++al) {
+                // B_al(i,j) = vx.*u : d_al phi_i * phi_j   (Flow.cpp:55-64)
+                for (int qq = 0; qq < 4; ++qq) f[qq] = ga[al] * ub[qq];
+                P.Bv[al] += integ(f, qw, G.detB);
+                // B_al(j,i): test j, trial i
+                for (int qq = 0; qq < 4; ++qq) f[qq] = gb[al] * va[qq];
+                P.Bp[al] += integ(f, qw, G.detB);
+                // C_al(i,j) = Ve * u.*v_al with Ve = 2/3 mu (Flow.cpp:385-390)
+                for (int qq = 0; qq < 4; ++qq) f[qq] = Vc * (ub[qq] * ga[al]);
+                P.C[al] += integ(f, qw, G.detB);
+            }
+            for (int qq = 0; qq < 4; ++qq) f[qq] = ub[qq] * va[qq];  // u.*v
+            P.M += integ(f, qw, G.detB);
+            double gg = gb[0] * ga[0] + gb[1] * ga[1] + gb[2] * ga[2];
+            for (int qq = 0; qq < 4; ++qq) f[qq] = (double)hh * gg;  // (h*h)*(ux.*vx+...)
+            P.D += integ(f, qw, G.detB);
+        }
+    }
+    return ok;
+}
+
+double now_ms() {
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+// ---------------------------------------------------------------------------
+// CSR helpers
+// ---------------------------------------------------------------------------
+void spmv(int64_t n, const int64_t* rp, const int32_t* ci, const double* v, const double* x,
+          double* y) {
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < n; ++r) {
+        double s = 0.0;
+        for (int64_t q = rp[r]; q < rp[r + 1]; ++q) s += v[q] * x[ci[q]];
+        y[r] = s;
+    }
+}
+
+double dot(int64_t n, const double* a, const double* b) {
+    double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+    for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+    return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Float-rounded basis table tab[a*4 + q] and the scaled weight (0.25/6).
+void ora_ref_tables(double* tab, double* qw) {
+    const RefTables& R = tables();
+    for (int a = 0; a < 4; ++a)
+        for (int q = 0; q < 4; ++q) tab[4 * a + q] = R.phi[a][q];
+    if (qw) *qw = R.qw;
+}
+
+int ora_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void ora_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+// Boundary nodes = nodes of triangles that belong to exactly one tetrahedron
+// (the exterior boundary triangles; TetraMesh.cpp:266-269).
+int ora_boundary_nodes(int64_t np, int64_t nt, const int32_t* tets, uint8_t* bnd) {
+    for (int64_t e = 0; e < 4 * nt; ++e)
+        if (tets[e] < 0 || tets[e] >= np) return 1;
+    Topology T;
+    build_topology(np, nt, tets, T);
+    std::memset(bnd, 0, (size_t)np);
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < nt; ++k) {
+        const int32_t* t = tets + 4 * k;
+        for (int f = 0; f < 4; ++f) {
+            int32_t v[3], n = 0;
+            for (int j = 0; j < 4; ++j)
+                if (j != f) v[n++] = t[j];
+            bool shared = false;
+            for (int64_t q = T.p2t_ptr[v[0]]; q < T.p2t_ptr[v[0] + 1] && !shared; ++q) {
+                int64_t k2 = T.p2t[q];
+                if (k2 == k) continue;
+                const int32_t* t2 = tets + 4 * k2;
+                int hit = 0;
+                for (int j = 0; j < 4; ++j) hit += (t2[j] == v[1]) + (t2[j] == v[2]);
+                shared = (hit == 2);
+            }
+            if (!shared)
+                for (int j = 0; j < 3; ++j) bnd[v[j]] = 1;  // benign race: all write 1
+        }
+    }
+    return 0;
+}
+
+// setViscosity (ViscosityProfiles.hpp:27-72). profile: 0 INVERSE, 1 DIRECT,
+// 2 DIRECT_RATE4X. mnmx (nullable) = {min, max} over interior elements, as the
+// reference prints (FLT_MAX, FLT_MIN when there is none).
+int ora_set_viscosity(int64_t np, int64_t nt, const int32_t* tets, const double* phi,
+                      const double* gf, double mu_int, double mu_ext, int profile,
+                      double rd_iterations, double gf_production, double* mu, double* mnmx) {
+    (void)np;
+    double mu_h = mu_int, mu_l = mu_ext;
+    double maxGF = rd_iterations > 0.0 ? gf_production : 1.0;
+    double mn = FLT_MAX, mx = FLT_MIN;
+    for (int64_t k = 0; k < nt; ++k) {
+        mu[k] = mu_l;
+        const int32_t* t = tets + 4 * k;
+        if (!(phi[t[0]] < 0.0 && phi[t[1]] < 0.0 && phi[t[2]] < 0.0 && phi[t[3]] < 0.0))
+            continue;
+        double c3 = std::max(std::max(gf[t[0]], gf[t[1]]), std::max(gf[t[2]], gf[t[3]]));
+        if (profile == 0) mu[k] = mu_l * (c3 / maxGF) + mu_h * (1.0 - c3 / maxGF);
+        if (profile == 1) mu[k] = mu_h * (c3 / maxGF) + mu_l * (1.0 - c3 / maxGF);
+        if (profile == 2) {
+            c3 *= 4.0;
+            if (c3 > maxGF) c3 = maxGF;
+            mu[k] = mu_h * (c3 / maxGF) + mu_l * (1.0 - c3 / maxGF);
+        }
+        mn = std::min(mn, mu[k]);
+        mx = std::max(mx, mu[k]);
+    }
+    if (mnmx) {
+        mnmx[0] = mn;
+        mnmx[1] = mx;
+    }
+    return 0;
+}
+
+// Nodal mass source (Flow.cpp:365-376): s_i = (c_i - sink) * growth on interior
+// nodes (phi < 0) with c_i > threshold, then s -= mean(s) over all nodes.
+int ora_source(int64_t np, const double* phi, const double* c, double gf_growth,
+               double level_sink, double growth_threshold, double* s) {
+    double sum = 0.0;
+    for (int64_t i = 0; i < np; ++i) {
+        s[i] = 0.0;
+        if (phi[i] < 0.0 && c[i] > growth_threshold) s[i] = (c[i] - level_sink) * gf_growth;
+        sum += s[i];
+    }
+    double mean = sum / (double)np;
+    for (int64_t i = 0; i < np; ++i) s[i] -= mean;
+    return 0;
+}
+
+// Block pattern of the node graph: rowptr[np+1], cols[nnzb] (sorted, incl. self).
+int ora_block_pattern_size(int64_t np, int64_t nt, const int32_t* tets, int64_t* nnzb) {
+    Topology T;
+    build_topology(np, nt, tets, T);
+    *nnzb = T.nb_ptr[np];
+    return 0;
+}
+
+// Node-pair blocks of the full (un-restricted) system in the reference's sign
+// convention (Flow.cpp:160-203), 16 doubles per block, row-major over
+// (ux, uy, uz, p) x (ux, uy, uz, p):
+//   [ K            -B_al(i,j) ]
+//   [ B_be(j,i)   alpha D(i,j) + eps M(i,j) ]
+// plus the per-node right-hand side rhs[4*i + (0..2)] = (N f)_al(i) + (C_al s)(i),
+// rhs[4*i + 3] = (M s)(i)  (Flow.cpp:392-396).  fst (nullable) = [fx, fy, fz]
+// each of length np.  Returns 2 on a degenerate element.
+int ora_assemble_blocks(int64_t np, int64_t nt, const float* xyz, const int32_t* tets,
+                        const double* mu, const double* s, const double* fst, double alpha,
+                        double eps, int64_t* rowptr, int32_t* cols, double* vals,
+                        double* rhs) {
+    Topology T;
+    build_topology(np, nt, tets, T);
+    for (int64_t i = 0; i <= np; ++i) rowptr[i] = T.nb_ptr[i];
+    std::copy(T.nb.begin(), T.nb.end(), cols);
+    int bad = 0;
+#pragma omp parallel
+    {
+        std::vector<PairVals> row;
+#pragma omp for schedule(dynamic, 256) reduction(| : bad)
+        for (int64_t i = 0; i < np; ++i) {
+            if (!gather_row(i, T, xyz, tets, mu, row)) bad |= 1;
+            double F[4] = {0, 0, 0, 0};
+            int64_t base = T.nb_ptr[i];
+            for (size_t c = 0; c < row.size(); ++c) {
+                const PairVals& P = row[c];
+                double* b = vals + 16 * (base + (int64_t)c);
+                for (int r = 0; r < 3; ++r) {
+                    for (int cc = 0; cc < 3; ++cc) b[4 * r + cc] = P.K[r][cc];
+                    b[4 * r + 3] = -P.Bv[r];
+                    b[12 + r] = P.Bp[r];
+                }
+                b[15] = alpha * P.D + eps * P.M;
+                int32_t j = T.nb[base + (int64_t)c];
+                for (int al = 0; al < 3; ++al) {
+                    double fj = fst ? fst[al * np + j] : 0.0;
+                    F[al] += P.M * fj;  // N = M for P1 (Flow.cpp:70-72)
+                }
+                for (int al = 0; al < 3; ++al) F[al] += P.C[al] * s[j];
+                F[3] += P.M * s[j];
+            }
+            for (int q = 0; q < 4; ++q) rhs[4 * i + q] = F[q];
+        }
+    }
+    return bad ? 2 : 0;
+}
+
+// Size of the reduced system (Flow.cpp:35-44, :206): N = 3 nI + np.
+int ora_reduced_size(int64_t np, const int64_t* rowptr, const int32_t* cols, const uint8_t* bnd,
+                     int64_t* N, int64_t* nnz) {
+    int64_t nI = 0;
+    for (int64_t i = 0; i < np; ++i) nI += bnd[i] ? 0 : 1;
+    int64_t z = 0;
+    for (int64_t i = 0; i < np; ++i) {
+        int64_t nint = 0, nall = rowptr[i + 1] - rowptr[i];
+        for (int64_t q = rowptr[i]; q < rowptr[i + 1]; ++q) nint += bnd[cols[q]] ? 0 : 1;
+        int64_t rowlen = 3 * nint + nall;
+        z += rowlen * (bnd[i] ? 1 : 4);
+    }
+    *N = 3 * nI + np;
+    *nnz = z;
+    return 0;
+}
+
+// Restriction subSparse(A_, sIdx_, sIdx_) / subDense(F, sIdx_) of the block
+// system to the reference's reduced ordering [ux(I), uy(I), uz(I), p(0..np-1)].
+// sidx[N] receives the full-system index 4-layout-free form of sIdx_:
+// velocity a of node i -> a*np + i, pressure of node i -> 3*np + i.
+int ora_reduce(int64_t np, const int64_t* rowptr, const int32_t* cols, const double* vals,
+               const double* rhs, const uint8_t* bnd, int64_t* rrp, int32_t* rci, double* rv,
+               double* rF, int32_t* sidx) {
+    std::vector<int64_t> red(np, -1);
+    int64_t nI = 0;
+    for (int64_t i = 0; i < np; ++i)
+        if (!bnd[i]) red[i] = nI++;
+    // row order: ux(I), uy(I), uz(I), p(all)
+    int64_t N = 3 * nI + np;
+    std::vector<int64_t> rowlen(N);
+    std::vector<int64_t> rownode(N);
+    std::vector<int> rowcomp(N);
+    for (int64_t i = 0; i < np; ++i) {
+        if (red[i] >= 0)
+            for (int a = 0; a < 3; ++a) {
+                rownode[a * nI + red[i]] = i;
+                rowcomp[a * nI + red[i]] = a;
+            }
+        rownode[3 * nI + i] = i;
+        rowcomp[3 * nI + i] = 3;
+    }
+    for (int64_t r = 0; r < N; ++r) {
+        int64_t i = rownode[r];
+        int64_t nint = 0, nall = rowptr[i + 1] - rowptr[i];
+        for (int64_t q = rowptr[i]; q < rowptr[i + 1]; ++q) nint += bnd[cols[q]] ? 0 : 1;
+        rowlen[r] = 3 * nint + nall;
+    }
+    rrp[0] = 0;
+    for (int64_t r = 0; r < N; ++r) rrp[r + 1] = rrp[r] + rowlen[r];
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < N; ++r) {
+        int64_t i = rownode[r];
+        int rc = rowcomp[r];
+        int64_t o = rrp[r];
+        for (int cc = 0; cc < 3; ++cc)
+            for (int64_t q = rowptr[i]; q < rowptr[i + 1]; ++q) {
+                int32_t j = cols[q];
+                if (red[j] < 0) continue;
+                rci[o] = (int32_t)(cc * nI + red[j]);
+                rv[o++] = vals[16 * q + 4 * rc + cc];
+            }
+        for (int64_t q = rowptr[i]; q < rowptr[i + 1]; ++q) {
+            rci[o] = (int32_t)(3 * nI + cols[q]);
+            rv[o++] = vals[16 * q + 4 * rc + 3];
+        }
+        rF[r] = rhs[4 * i + rc];
+        sidx[r] = (int32_t)(rc * np + i);
+    }
+    return 0;
+}
+
+int ora_spmv(int64_t N, const int64_t* rp, const int32_t* ci, const double* v, const double* x,
+             double* y) {
+    spmv(N, rp, ci, v, x, y);
+    return 0;
+}
+
+// Un-preconditioned BiCGSTAB (van der Vorst 1992) as the reference configures
+// Eigen's (Flow.hpp:62): stop when the updated residual satisfies
+// ||r|| <= tol ||b||, at most maxit iterations (<= 0: 2N, Eigen's default),
+// warm start from x; when rho collapses relative to ||r0||^2 the shadow
+// residual is reset to the current residual.  Returns 0 on convergence, 1 on
+// no convergence.  iters / err receive the iteration count and ||r||/||b||
+// (the solver's own error() estimate).
+int ora_bicgstab(int64_t N, const int64_t* rp, const int32_t* ci, const double* v, const double* b,
+                 double* x, double tol, int64_t maxit, int64_t* iters, double* err) {
+    std::vector<double> r(N), r0(N), p(N, 0.0), vv(N, 0.0), s(N), t(N);
+    if (maxit <= 0) maxit = 2 * N;
+    spmv(N, rp, ci, v, x, r.data());
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < N; ++q) r[q] = b[q] - r[q];
+    double bb = dot(N, b, b);
+    if (bb == 0.0) {
+        std::fill(x, x + N, 0.0);
+        if (iters) *iters = 0;
+        if (err) *err = 0.0;
+        return 0;
+    }
+    r0 = r;
+    double r0n = dot(N, r.data(), r.data());
+    double rr = r0n;
+    double tol2 = tol * tol * bb;
+    const double eps2 = DBL_EPSILON * DBL_EPSILON;
+    double rho = 1.0, alpha = 1.0, w = 1.0;
+    int64_t it = 0;
+    int restarts = 0;
+    while (rr > tol2 && it < maxit) {
+        double rho_old = rho;
+        rho = dot(N, r0.data(), r.data());
+        if (std::fabs(rho) < eps2 * r0n) {
+            // restart with the true residual as the new shadow vector
+            spmv(N, rp, ci, v, x, r.data());
+#pragma omp parallel for schedule(static)
+            for (int64_t q = 0; q < N; ++q) r[q] = b[q] - r[q];
+            r0 = r;
+            rho = r0n = dot(N, r.data(), r.data());
+            if (restarts++ == 0) it = 0;
+        }
+        double beta = (rho / rho_old) * (alpha / w);
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < N; ++q) p[q] = r[q] + beta * (p[q] - w * vv[q]);
+        spmv(N, rp, ci, v, p.data(), vv.data());
+        alpha = rho / dot(N, r0.data(), vv.data());
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < N; ++q) s[q] = r[q] - alpha * vv[q];
+        spmv(N, rp, ci, v, s.data(), t.data());
+        double tt = dot(N, t.data(), t.data());
+        w = tt > 0.0 ? dot(N, t.data(), s.data()) / tt : 0.0;
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < N; ++q) {
+            x[q] += alpha * p[q] + w * s[q];
+            r[q] = s[q] - w * t[q];
+        }
+        rr = dot(N, r.data(), r.data());
+        ++it;
+    }
+    if (iters) *iters = it;
+    double e = std::sqrt(rr / bb);
+    if (err) *err = e;
+    return e <= tol ? 0 : 1;
+}
+
+// True relative residual ||b - A x|| / ||b|| with long-double accumulation.
+double ora_true_residual(int64_t N, const int64_t* rp, const int32_t* ci, const double* v,
+                         const double* b, const double* x) {
+    long double rr = 0.0L, bb = 0.0L;
+#pragma omp parallel for reduction(+ : rr, bb) schedule(static)
+    for (int64_t r = 0; r < N; ++r) {
+        long double s = 0.0L;
+        for (int64_t q = rp[r]; q < rp[r + 1]; ++q) s += (long double)v[q] * x[ci[q]];
+        long double d = (long double)b[r] - s;
+        rr += d * d;
+        bb += (long double)b[r] * b[r];
+    }
+    return bb > 0.0L ? (double)std::sqrt(rr / bb) : 0.0;
+}
+
+// Tight solve used to produce parity targets: MINRES (Paige & Saunders 1975)
+// on the symmetric form J A x = J b of the reduced system, J = diag(+1 on the
+// 3 nI velocity rows, -1 on the np pressure rows), preconditioned by the SPD
+// diagonal minv[N] (inverse weights).  Restarted from the current iterate on the
+// true residual until ||b - A x|| / ||b|| <= tol (long-double residual) or
+// max_restarts.  Returns the true relative residual.
+double ora_minres_tight(int64_t N, int64_t nI, const int64_t* rp, const int32_t* ci,
+                        const double* v, const double* b, const double* minv, double* x,
+                        double tol, int64_t maxit, int max_restarts, int64_t* iters_out) {
+    std::vector<double> r1(N), r2(N), y(N), vv(N), w(N), w1(N), w2(N), jb(N);
+    auto apply = [&](const double* in, double* out) {
+        spmv(N, rp, ci, v, in, out);
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 3 * nI; q < N; ++q) out[q] = -out[q];
+    };
+    for (int64_t q = 0; q < N; ++q) jb[q] = q < 3 * nI ? b[q] : -b[q];
+    double bn = std::sqrt(dot(N, b, b));
+    double tr = ora_true_residual(N, rp, ci, v, b, x);
+    double inner_tol = tol;
+    int64_t total = 0;
+    for (int rs = 0; rs <= max_restarts && tr > tol && total < maxit; ++rs) {
+        apply(x, r1.data());
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < N; ++q) {
+            r1[q] = jb[q] - r1[q];
+            y[q] = minv[q] * r1[q];
+        }
+        r2 = r1;
+        double beta1 = std::sqrt(dot(N, r1.data(), y.data()));
+        if (!(beta1 > 0.0)) break;
+        double rn0 = std::sqrt(dot(N, r1.data(), r1.data()));
+        // the preconditioned target that corresponds to tol in the 2-norm,
+        // adapted from the previous sweep's observed ratio
+        double target = inner_tol * bn / rn0;
+        double oldb = 0.0, beta = beta1, dbar = 0.0, epsln = 0.0, phibar = beta1;
+        double cs = -1.0, sn = 0.0;
+        std::fill(w.begin(), w.end(), 0.0);
+        std::fill(w2.begin(), w2.end(), 0.0);
+        for (int64_t it = 1; total < maxit; ++it) {
+            ++total;
+            double s = 1.0 / beta;
+#pragma omp parallel for schedule(static)
+            for (int64_t q = 0; q < N; ++q) vv[q] = s * y[q];
+            apply(vv.data(), y.data());
+            if (it >= 2) {
+                double f = beta / oldb;
+#pragma omp parallel for schedule(static)
+                for (int64_t q = 0; q < N; ++q) y[q] -= f * r1[q];
+            }
+            double alfa = dot(N, vv.data(), y.data());
+            double f2 = alfa / beta;
+#pragma omp parallel for schedule(static)
+            for (int64_t q = 0; q < N; ++q) {
+                y[q] -= f2 * r2[q];
+                r1[q] = r2[q];
+                r2[q] = y[q];
+                y[q] = minv[q] * r2[q];
+            }
+            oldb = beta;
+            beta = std::sqrt(dot(N, r2.data(), y.data()));
+            double oldeps = epsln;
+            double delta = cs * dbar + sn * alfa;
+            double gbar = sn * dbar - cs * alfa;
+            epsln = sn * beta;
+            dbar = -cs * beta;
+            double gamma = std::sqrt(gbar * gbar + beta * beta);
+            if (gamma < DBL_MIN) gamma = DBL_MIN;
+            cs = gbar / gamma;
+            sn = beta / gamma;
+            double phi = cs * phibar;
+            phibar = sn * phibar;
+            double ig = 1.0 / gamma;
+#pragma omp parallel for schedule(static)
+            for (int64_t q = 0; q < N; ++q) {
+                double wn = (vv[q] - oldeps * w1[q] - delta * w2[q]) * ig;
+                w1[q] = w2[q];
+                w2[q] = wn;
+                x[q] += phi * wn;
+            }
+            if (phibar <= target * beta1) break;
+        }
+        double prev = tr;
+        tr = ora_true_residual(N, rp, ci, v, b, x);
+        if (tr > tol) {
+            double ratio = tr / (inner_tol > 0 ? inner_tol : tol);
+            inner_tol = tol / std::max(ratio, 1.0) * 0.5;
+            if (tr > 0.9 * prev && rs > 2) break;  // stagnation
+        }
+    }
+    if (iters_out) *iters_out = total;
+    return tr;
+}
+
+// Scatter of the reduced solution to flow = [ux(np), uy(np), uz(np), p(np)],
+// zero on boundary velocity dofs (Flow.cpp:290-300).
+int ora_scatter(int64_t np, int64_t N, const int32_t* sidx, const double* x, double* flow) {
+    std::fill(flow, flow + 4 * np, 0.0);
+    for (int64_t r = 0; r < N; ++r) flow[sidx[r]] = x[r];
+    return 0;
+}
+
+// Timing helper for the CPU baseline.
+double ora_now_ms(void) { return now_ms(); }
+
+}  // extern "C"
