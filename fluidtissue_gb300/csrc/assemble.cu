@@ -1,0 +1,497 @@
+// Element geometry, viscosity profile, mass source, right-hand side, block
+// assembly and preconditioner set-up of the P1-P1 stabilised Stokes system.
+//
+// Reference arithmetic (paths relative to the reference project):
+//   element geometry            src/fem/Assembler.hpp:430-462, h :193
+//   weak forms / composition    src/growth/Flow.cpp:54-72, :135-203
+//   viscosity profile           src/growth/ViscosityProfiles.hpp:27-72
+//   source and RHS              src/growth/Flow.cpp:365-399
+//
+// The system is stored node-blocked: block (i,j) is the 4x4 coupling of the
+// unknowns (ux,uy,uz,p) of nodes i and j, row-major.  Pressure rows are negated
+// (the symmetric form  [K -B; -B^T -(alpha D + eps M)]  of the reference's
+// [K -B; B^T alpha D + eps M], same solution), and the Dirichlet velocity rows
+// and columns of boundary nodes are identity / zero instead of being removed
+// (subSparse, Flow.cpp:206), which leaves the interior solution unchanged.
+#include <cfloat>
+
+#include "fts_device.cuh"
+#include "reduce.cuh"
+
+namespace fts {
+
+struct RefArgs {
+    double wq[4];
+    double mref[4][4];
+};
+
+static RefArgs ref_args() {
+    RefConstants R = ref_constants();
+    RefArgs a;
+    for (int i = 0; i < 4; ++i) {
+        a.wq[i] = R.wq[i];
+        for (int j = 0; j < 4; ++j) a.mref[i][j] = R.mref[i][j];
+    }
+    return a;
+}
+
+// ---------------------------------------------------------------------------
+// Geometry: detB = |det B|, invB^T, gradients, volume, h^2 (float), per element.
+// ---------------------------------------------------------------------------
+__global__ void k_geometry(int64_t nt, const float* __restrict__ xyz,
+                           const int32_t* __restrict__ tets, ElemGeom* __restrict__ geom,
+                           int* __restrict__ bad) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nt;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int4 t = reinterpret_cast<const int4*>(tets)[k];
+        int ids[4] = {t.x, t.y, t.z, t.w};
+        double p[4][3];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) p[j][a] = (double)xyz[3 * (int64_t)ids[j] + a];
+        double B[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            B[a][0] = p[1][a] - p[0][a];
+            B[a][1] = p[2][a] - p[0][a];
+            B[a][2] = p[3][a] - p[0][a];
+        }
+        double c00 = B[1][1] * B[2][2] - B[1][2] * B[2][1];
+        double c01 = B[1][2] * B[2][0] - B[1][0] * B[2][2];
+        double c02 = B[1][0] * B[2][1] - B[1][1] * B[2][0];
+        double det = B[0][0] * c00 + B[0][1] * c01 + B[0][2] * c02;
+        double adet = fabs(det);
+        ElemGeom G;
+        if (!(adet > 0.0) || !isfinite(adet)) {
+            atomicOr(bad, 1);
+            adet = 1.0;
+            det = 1.0;
+        }
+        double cof[3][3];
+        cof[0][0] = c00;
+        cof[0][1] = c01;
+        cof[0][2] = c02;
+        cof[1][0] = B[0][2] * B[2][1] - B[0][1] * B[2][2];
+        cof[1][1] = B[0][0] * B[2][2] - B[0][2] * B[2][0];
+        cof[1][2] = B[0][1] * B[2][0] - B[0][0] * B[2][1];
+        cof[2][0] = B[0][1] * B[1][2] - B[0][2] * B[1][1];
+        cof[2][1] = B[0][2] * B[1][0] - B[0][0] * B[1][2];
+        cof[2][2] = B[0][0] * B[1][1] - B[0][1] * B[1][0];
+        const double id = 1.0 / det;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            double it0 = cof[r][0] * id, it1 = cof[r][1] * id, it2 = cof[r][2] * id;
+            G.g[0][r] = -it0 - it1 - it2;
+            G.g[1][r] = it0;
+            G.g[2][r] = it1;
+            G.g[3][r] = it2;
+        }
+        G.vol = adet / 6.0;
+        float h = (float)cbrt(adet);
+        float hh = h * h;
+        G.hh = (double)hh;
+        G.pad[0] = G.pad[1] = 0.0;
+        geom[k] = G;
+    }
+}
+
+void launch_geometry(Ctx& c, int* bad) {
+    k_geometry<<<grid_for(c, c.nt), kThreads, 0, c.stream>>>(c.nt, c.xyz, c.tets, c.geom, bad);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+// ---------------------------------------------------------------------------
+// setViscosity (ViscosityProfiles.hpp:27-72): mu_ext everywhere; on interior
+// elements (all four nodes phi < 0, LevelSet.cpp:180-196) blended by the
+// largest nodal growth factor.
+// ---------------------------------------------------------------------------
+__global__ void k_viscosity_profile(int64_t nt, const int32_t* __restrict__ tets,
+                                    const double* __restrict__ phi,
+                                    const double* __restrict__ gf, double mu_h, double mu_l,
+                                    int profile, double maxGF, double* __restrict__ mu) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nt;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int4 t = reinterpret_cast<const int4*>(tets)[k];
+        double m = mu_l;
+        if (phi[t.x] < 0.0 && phi[t.y] < 0.0 && phi[t.z] < 0.0 && phi[t.w] < 0.0) {
+            double c3 = fmax(fmax(gf[t.x], gf[t.y]), fmax(gf[t.z], gf[t.w]));
+            if (profile == 0) m = mu_l * (c3 / maxGF) + mu_h * (1.0 - c3 / maxGF);
+            if (profile == 1) m = mu_h * (c3 / maxGF) + mu_l * (1.0 - c3 / maxGF);
+            if (profile == 2) {
+                c3 *= 4.0;
+                if (c3 > maxGF) c3 = maxGF;
+                m = mu_h * (c3 / maxGF) + mu_l * (1.0 - c3 / maxGF);
+            }
+        }
+        mu[k] = m;
+    }
+}
+
+void launch_viscosity_profile(Ctx& c) {
+    const fts_params& P = c.par;
+    double maxGF = P.rd_iterations > 0.0 ? P.gf_production : 1.0;
+    k_viscosity_profile<<<grid_for(c, c.nt), kThreads, 0, c.stream>>>(
+        c.nt, c.tets, c.phi, c.src, P.mu_interior, P.mu_exterior, P.mu_profile, maxGF, c.mu);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+// min / max of mu over interior elements (the values Flow.cpp:241 prints).
+__global__ void k_mu_minmax(int64_t nt, const int32_t* __restrict__ tets,
+                            const double* __restrict__ phi, const double* __restrict__ mu,
+                            Reduction red, OuterScalars* os) {
+    double mn = DBL_MAX, mx = -DBL_MAX;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nt;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int4 t = reinterpret_cast<const int4*>(tets)[k];
+        if (phi[t.x] < 0.0 && phi[t.y] < 0.0 && phi[t.z] < 0.0 && phi[t.w] < 0.0) {
+            mn = fmin(mn, mu[k]);
+            mx = fmax(mx, mu[k]);
+        }
+    }
+    // max-reduce (-mn, mx) through shuffles; partials via the ticket
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    __shared__ double smn[32], smx[32];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        smn[wid] = mn;
+        smx[wid] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            mn = fmin(mn, smn[w]);
+            mx = fmax(mx, smx[w]);
+        }
+        red.partials[blockIdx.x] = mn;
+        red.partials[kMaxPartials + blockIdx.x] = mx;
+    }
+    if (last_block(red) && threadIdx.x == 0) {
+        double a = DBL_MAX, b = -DBL_MAX;
+        for (unsigned i = 0; i < gridDim.x; ++i) {
+            a = fmin(a, __ldcg(&red.partials[i]));
+            b = fmax(b, __ldcg(&red.partials[kMaxPartials + i]));
+        }
+        os->mu_min = a;
+        os->mu_max = b;
+    }
+}
+
+void launch_mu_minmax(Ctx& c) {
+    k_mu_minmax<<<grid_for(c, c.nt), kThreads, 0, c.stream>>>(c.nt, c.tets, c.phi, c.mu, c.red,
+                                                               c.os);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+// ---------------------------------------------------------------------------
+// Mass source (Flow.cpp:365-376): s_i = (c_i - sink) * growth on interior nodes
+// with c_i > threshold; the mean over all nodes goes to os->sum (subtracted in
+// the RHS kernel).
+// ---------------------------------------------------------------------------
+__global__ void k_source(int64_t np, const double* __restrict__ phi, const double* __restrict__ c,
+                         double growth, double sink, double thr, double* __restrict__ s,
+                         Reduction red, OuterScalars* os) {
+    double acc[1] = {0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double v = 0.0;
+        if (phi[i] < 0.0 && c[i] > thr) v = (c[i] - sink) * growth;
+        s[i] = v;
+        acc[0] += v;
+    }
+    double tot[1];
+    if (grid_sum<1>(acc, red, tot) && threadIdx.x == 0) os->sum = tot[0] / (double)np;
+}
+
+void launch_source(Ctx& c) {
+    const fts_params& P = c.par;
+    k_source<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(c.np, c.phi, c.src, P.gf_growth,
+                                                           P.level_sink, P.growth_threshold,
+                                                           c.s, c.red, c.os);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+// ---------------------------------------------------------------------------
+// Right-hand side (Flow.cpp:392-396), gathered per node over its elements:
+//   F_al(i) = sum_j N(i,j) f_al(j) + sum_j C_al(i,j) s_j,
+//   C_al(i,j) = int (2/3 mu) psi_j d_al phi_i,    F_p(i) = sum_j M(i,j) s_j.
+// Stored as b = (F_x, F_y, F_z, -F_p), zero on Dirichlet velocity rows.
+// ---------------------------------------------------------------------------
+__global__ void k_rhs(int64_t np, const int32_t* __restrict__ p2t_ptr,
+                      const uint32_t* __restrict__ p2t, const int32_t* __restrict__ tets,
+                      const ElemGeom* __restrict__ geom, const double* __restrict__ mu,
+                      const double* __restrict__ s, const double* __restrict__ force,
+                      const uint8_t* __restrict__ bnd, const OuterScalars* __restrict__ os,
+                      RefArgs R, V4<double>* __restrict__ b) {
+    const double mean = os->sum;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double F[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int32_t q = p2t_ptr[i]; q < p2t_ptr[i + 1]; ++q) {
+            uint32_t e = p2t[q];
+            int64_t k = e >> 2;
+            int a = e & 3;
+            int4 t = reinterpret_cast<const int4*>(tets)[k];
+            int ids[4] = {t.x, t.y, t.z, t.w};
+            const ElemGeom& G = geom[k];
+            double vol = G.vol;
+            double sv[4], sw = 0.0, ms = 0.0;
+#pragma unroll
+            for (int bb = 0; bb < 4; ++bb) {
+                sv[bb] = s[ids[bb]] - mean;
+                sw += R.wq[bb] * sv[bb];
+                ms += R.mref[a][bb] * sv[bb];
+            }
+            double cfac = (2.0 / 3 * mu[k]) * vol * sw;
+#pragma unroll
+            for (int al = 0; al < 3; ++al) F[al] += cfac * G.g[a][al];
+            F[3] += vol * ms;
+            if (force) {
+#pragma unroll
+                for (int al = 0; al < 3; ++al) {
+                    double fm = 0.0;
+#pragma unroll
+                    for (int bb = 0; bb < 4; ++bb) fm += R.mref[a][bb] * force[al * np + ids[bb]];
+                    F[al] += vol * fm;
+                }
+            }
+        }
+        V4<double> o;
+        bool d = bnd[i] != 0;
+        o.x = d ? 0.0 : F[0];
+        o.y = d ? 0.0 : F[1];
+        o.z = d ? 0.0 : F[2];
+        o.w = -F[3];
+        b[i] = o;
+    }
+}
+
+void launch_rhs(Ctx& c, bool have_force) {
+    k_rhs<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(c.np, c.p2t_ptr, c.p2t, c.tets, c.geom,
+                                                        c.mu, c.s, have_force ? c.force : nullptr,
+                                                        c.bnd, c.os, ref_args(), c.b);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+// ---------------------------------------------------------------------------
+// Block assembly: one warp per block row i (atomic-free, as the reference's
+// node-row gather, Assembler.hpp:150-225).  The warp walks the elements around
+// node i; for each element every lane owns two of the 4 x 16 entries it adds
+// to row i (column node b = lane / 8), accumulated in a shared-memory copy of
+// the row, which is then written out coalesced with the Dirichlet masking.
+// ---------------------------------------------------------------------------
+__global__ void k_assemble(int64_t np, const int32_t* __restrict__ rowptr,
+                           const int32_t* __restrict__ cols, const int32_t* __restrict__ p2t_ptr,
+                           const uint32_t* __restrict__ p2t, const int32_t* __restrict__ tets,
+                           const ElemGeom* __restrict__ geom, const double* __restrict__ mu,
+                           const uint8_t* __restrict__ bnd, double alpha, double eps, RefArgs R,
+                           int max_row, double* __restrict__ A) {
+    extern __shared__ double smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    double* buf = smem + (size_t)wib * max_row * 16;
+    const int b = lane >> 3;        // column node (local index) handled by this lane
+    const int e0 = (lane & 7) * 2;  // first of the two entries
+    for (int64_t i = (int64_t)blockIdx.x * wpb + wib; i < np; i += (int64_t)gridDim.x * wpb) {
+        const int32_t c0 = rowptr[i];
+        const int ncol = rowptr[i + 1] - c0;
+        for (int e = lane; e < ncol * 16; e += 32) buf[e] = 0.0;
+        __syncwarp();
+        for (int32_t q = p2t_ptr[i]; q < p2t_ptr[i + 1]; ++q) {
+            const uint32_t pk = p2t[q];
+            const int64_t k = pk >> 2;
+            const int a = pk & 3;
+            const int4 t = reinterpret_cast<const int4*>(tets)[k];
+            const int tb = b == 0 ? t.x : (b == 1 ? t.y : (b == 2 ? t.z : t.w));
+            // slot of node tb in row i (sorted columns)
+            int lo = 0, hi = ncol - 1;
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (cols[c0 + mid] < tb) lo = mid + 1;
+                else hi = mid;
+            }
+            const ElemGeom* G = geom + k;
+            const double ga0 = G->g[a][0], ga1 = G->g[a][1], ga2 = G->g[a][2];
+            const double gb0 = G->g[b][0], gb1 = G->g[b][1], gb2 = G->g[b][2];
+            const double vol = G->vol;
+            const double gg = ga0 * gb0 + ga1 * gb1 + ga2 * gb2;
+            const double mv = mu[k] * vol;
+            const double ga[3] = {ga0, ga1, ga2}, gb[3] = {gb0, gb1, gb2};
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int e = e0 + u;
+                const int r = e >> 2, cc = e & 3;
+                double v;
+                if (r < 3 && cc < 3) {
+                    // K_{r,cc}(i,j) = mu vol (delta gg + d_cc phi_i d_r phi_j)
+                    v = mv * ((r == cc ? gg : 0.0) + ga[cc] * gb[r]);
+                } else if (r < 3) {
+                    v = -(ga[r] * R.wq[b] * vol);  // -B_r(i,j)
+                } else if (cc < 3) {
+                    v = -(gb[cc] * R.wq[a] * vol);  // -B_cc(j,i) (negated pressure row)
+                } else {
+                    v = -(alpha * (G->hh * vol * gg) + eps * (vol * R.mref[a][b]));
+                }
+                buf[lo * 16 + e] += v;
+            }
+            __syncwarp();
+        }
+        const bool bi = bnd[i] != 0;
+        for (int e = lane; e < ncol * 16; e += 32) {
+            const int slot = e >> 4, rc = e & 15, r = rc >> 2, cc = rc & 3;
+            const int32_t j = cols[c0 + slot];
+            double v = buf[e];
+            if (bi && r < 3) v = (j == i && r == cc) ? 1.0 : 0.0;
+            else if (cc < 3 && bnd[j]) v = 0.0;
+            A[(int64_t)(c0 + slot) * 16 + rc] = v;
+        }
+        __syncwarp();
+    }
+}
+
+void launch_assemble(Ctx& c) {
+    int max_row = c.topo.max_row;
+    size_t per_warp = (size_t)max_row * 16 * sizeof(double);
+    int wpb = 8;
+    while (wpb > 1 && per_warp * wpb > 160 * 1024) wpb >>= 1;
+    size_t shmem = per_warp * wpb;
+    FTS_CUDA(cudaFuncSetAttribute(k_assemble, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)shmem));
+    int64_t blocks = (c.np + wpb - 1) / wpb;
+    int64_t cap = (int64_t)c.num_sms * 16;
+    int grid = (int)(blocks < cap ? blocks : cap);
+    k_assemble<<<grid, wpb * 32, shmem, c.stream>>>(c.np, c.rowptr, c.cols, c.p2t_ptr, c.p2t,
+                                                    c.tets, c.geom, c.mu, c.bnd, c.par.alpha,
+                                                    c.par.eps, ref_args(), max_row, c.A64);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+// ---------------------------------------------------------------------------
+// Block-diagonal SPD preconditioner: inverse of the node's 3x3 velocity block
+// (identity on Dirichlet nodes) and, for pressure, the inverse of
+// (alpha D + eps M)_ii + sum_{e ni i} vol_e / (4 mu_e) (lumped 1/mu-weighted
+// mass, a Schur-complement estimate).  pc[8 i + 0..5] = xx xy xz yy yz zz,
+// pc[8 i + 6] = pressure weight.
+// ---------------------------------------------------------------------------
+__global__ void k_preconditioner(int64_t np, const int32_t* __restrict__ diag,
+                                 const int32_t* __restrict__ p2t_ptr,
+                                 const uint32_t* __restrict__ p2t,
+                                 const ElemGeom* __restrict__ geom, const double* __restrict__ mu,
+                                 const uint8_t* __restrict__ bnd, const double* __restrict__ A,
+                                 double* __restrict__ pc) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double* D = A + (int64_t)diag[i] * 16;
+        double o[8];
+        if (bnd[i]) {
+            o[0] = 1.0; o[1] = 0.0; o[2] = 0.0; o[3] = 1.0; o[4] = 0.0; o[5] = 1.0;
+        } else {
+            double a00 = D[0], a01 = 0.5 * (D[1] + D[4]), a02 = 0.5 * (D[2] + D[8]);
+            double a11 = D[5], a12 = 0.5 * (D[6] + D[9]), a22 = D[10];
+            double c00 = a11 * a22 - a12 * a12;
+            double c01 = a02 * a12 - a01 * a22;
+            double c02 = a01 * a12 - a02 * a11;
+            double c11 = a00 * a22 - a02 * a02;
+            double c12 = a01 * a02 - a00 * a12;
+            double c22 = a00 * a11 - a01 * a01;
+            double det = a00 * c00 + a01 * c01 + a02 * c02;
+            double id = 1.0 / det;
+            o[0] = c00 * id; o[1] = c01 * id; o[2] = c02 * id;
+            o[3] = c11 * id; o[4] = c12 * id; o[5] = c22 * id;
+        }
+        double w = 0.0;
+        for (int32_t q = p2t_ptr[i]; q < p2t_ptr[i + 1]; ++q) {
+            int64_t k = p2t[q] >> 2;
+            w += geom[k].vol / (4.0 * mu[k]);
+        }
+        o[6] = 1.0 / (-D[15] + w);
+        o[7] = 0.0;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) pc[8 * i + u] = o[u];
+    }
+}
+
+void launch_preconditioner(Ctx& c) {
+    k_preconditioner<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
+        c.np, c.diag, c.p2t_ptr, c.p2t, c.geom, c.mu, c.bnd, c.A64, c.pc64);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+// FP32 copies of the operator and preconditioner for the mixed-precision inner solve.
+__global__ void k_to_f32(int64_t n, const double* __restrict__ in, float* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n / 2;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double2 v = reinterpret_cast<const double2*>(in)[i];
+        reinterpret_cast<float2*>(out)[i] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
+void launch_to_f32(Ctx& c) {
+    k_to_f32<<<grid_for(c, c.nnzb * 8), kThreads, 0, c.stream>>>(c.nnzb * 16, c.A64, c.A32);
+    k_to_f32<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(c.np * 8, c.pc64, c.pc32);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 2;
+}
+
+// flow = [ux(np), uy(np), uz(np), p(np)], zero velocity on boundary nodes
+// (Flow.cpp:290-300).
+__global__ void k_scatter_flow(int64_t np, const V4<double>* __restrict__ x,
+                               const uint8_t* __restrict__ bnd, double* __restrict__ flow) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        V4<double> v = x[i];
+        bool d = bnd[i] != 0;
+        flow[i] = d ? 0.0 : v.x;
+        flow[np + i] = d ? 0.0 : v.y;
+        flow[2 * np + i] = d ? 0.0 : v.z;
+        flow[3 * np + i] = v.w;
+    }
+}
+
+void launch_scatter_flow(Ctx& c, double* flow_out) {
+    k_scatter_flow<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(c.np, c.x, c.bnd, flow_out);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+__global__ void k_check_finite(int64_t n, const double* __restrict__ a, int* flag) {
+    bool bad = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        bad = bad || !isfinite(a[i]);
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+__global__ void k_any_abs_above(int64_t n, const double* __restrict__ a, double thr, int* flag) {
+    bool hit = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        hit = hit || fabs(a[i]) > thr;
+    if (__any_sync(0xffffffffu, hit) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+void launch_any_abs_above(Ctx& c, const double* a, int64_t n, double thr) {
+    k_any_abs_above<<<grid_for(c, n), kThreads, 0, c.stream>>>(n, a, thr, c.err_flag);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+void launch_check_finite(Ctx& c, const double* a, int64_t n) {
+    k_check_finite<<<grid_for(c, n), kThreads, 0, c.stream>>>(n, a, c.err_flag);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+}  // namespace fts

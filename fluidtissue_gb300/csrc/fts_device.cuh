@@ -1,0 +1,200 @@
+// Device-side context and kernel interfaces of libfts (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "fts.h"
+#include "fts_internal.h"
+
+namespace fts {
+
+#define FTS_CUDA(call)                                                        \
+    do {                                                                      \
+        cudaError_t e_ = (call);                                              \
+        if (e_ != cudaSuccess) {                                              \
+            throw ::fts::CudaError(e_, #call, __FILE__, __LINE__);            \
+        }                                                                     \
+    } while (0)
+
+struct CudaError {
+    cudaError_t code;
+    std::string what;
+    CudaError(cudaError_t c, const char* call, const char* file, int line)
+        : code(c),
+          what(std::string(call) + ": " + cudaGetErrorString(c) + " (" + file + ":" +
+               std::to_string(line) + ")") {}
+};
+
+// Blocks per SM used for grid-stride kernels; grids are multiples of the SM
+// count so every SM gets the same share.
+constexpr int kThreads = 256;
+constexpr int kMaxPartials = 4096;
+
+// Node-interleaved vector element: (ux, uy, uz, p).
+template <typename T>
+struct alignas(4 * sizeof(T)) V4 {
+    T x, y, z, w;
+};
+
+// Per-element geometry, 16 doubles (128 B): gradients of the 4 P1 basis
+// functions (invB^T * ghat_j, Assembler.hpp:163-168), the element volume
+// detB/6, and (float)h^2 with h = (float)cbrt(detB) (Assembler.hpp:193,
+// Flow.cpp:195).
+struct alignas(128) ElemGeom {
+    double g[4][3];
+    double vol;
+    double hh;
+    double pad[2];
+};
+
+// Scalar state of one MINRES run (Paige & Saunders 1975), kept on the device
+// so that the iteration never waits on the host.
+struct MinresScalars {
+    double beta1, beta, oldb, alfa, dbar, epsln, oldeps, delta, gamma, phi, phibar, cs, sn;
+    double target;
+    long long iters;
+    long long maxit;
+    int stop;
+    int c_pending;
+    int status;  // 0 running/converged, 1 max iterations, 2 NaN
+    int pad;
+};
+
+// Scalars of the FP64 outer loop.
+struct OuterScalars {
+    double rr;     // ||b - S x||^2
+    double bb;     // ||b||^2
+    double scale;  // 1 / ||r|| used to normalise the FP32 inner right-hand side
+    double sum;    // scratch reduction (source mean)
+    double mu_min, mu_max;
+    int nonfinite;
+    int pad;
+};
+
+struct Reduction {
+    double* partials;   // [kMaxPartials * 4]
+    unsigned* ticket;   // [1]
+};
+
+// Krylov work vectors of one precision (node-interleaved V4<T>, np each).
+template <typename T>
+struct KrylovWork {
+    V4<T>* q = nullptr;
+    V4<T>* R[2] = {nullptr, nullptr};
+    V4<T>* Y[2] = {nullptr, nullptr};
+    V4<T>* W[2] = {nullptr, nullptr};
+    V4<T>* X = nullptr;  // correction accumulated by the inner solve
+    V4<T>* r0 = nullptr; // right-hand side of the inner solve
+};
+
+struct Ctx {
+    fts_params par{};
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    HostTopology topo;
+    int64_t np = 0, nt = 0, nnzb = 0;
+    int num_sms = 148;
+    std::string last_error;
+
+    // mesh
+    float* xyz = nullptr;
+    int32_t* tets = nullptr;
+    uint8_t* bnd = nullptr;
+    int32_t* rowptr = nullptr;
+    int32_t* cols = nullptr;
+    int32_t* diag = nullptr;
+    int32_t* p2t_ptr = nullptr;
+    uint32_t* p2t = nullptr;
+    ElemGeom* geom = nullptr;
+
+    // per-solve inputs (device staging)
+    double* phi = nullptr;
+    double* src = nullptr;
+    double* force = nullptr;
+    double* mu = nullptr;
+    double* s = nullptr;
+    double* flow = nullptr;
+
+    // system
+    double* A64 = nullptr;
+    float* A32 = nullptr;
+    double* pc64 = nullptr;   // 8 per node: inverse of the 3x3 velocity block (xx,xy,xz,yy,yz,zz),
+    float* pc32 = nullptr;    // inverse pressure weight, pad
+    V4<double>* b = nullptr;
+    V4<double>* x = nullptr;
+    V4<double>* r = nullptr;
+    KrylovWork<double> w64;
+    KrylovWork<float> w32;
+    bool have32 = false;
+
+    // scalars / reductions
+    MinresScalars* ms = nullptr;
+    MinresScalars* ms_host = nullptr;   // pinned
+    OuterScalars* os = nullptr;
+    OuterScalars* os_host = nullptr;    // pinned
+    Reduction red{};
+    int* err_flag = nullptr;
+
+    // learned ratio between true and preconditioned residual reductions
+    double pc_ratio64 = 10.0;
+    double pc_ratio32 = 10.0;
+    bool matrix_valid = false;
+
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    int64_t device_bytes = 0;
+
+    // launch accounting and optional per-application event timing of the
+    // Krylov loop's operator kernel
+    int64_t launches = 0;
+    int64_t spmv_runs = 0;
+    double ms_spmv = 0.0;
+    static constexpr int kTimedPairs = 32;
+    cudaEvent_t tev[2 * kTimedPairs] = {};
+    bool tev_ready = false;
+};
+
+// ---- assembly (assemble.cu) -----------------------------------------------
+void launch_geometry(Ctx& c, int* bad);
+void launch_viscosity_profile(Ctx& c);
+void launch_mu_minmax(Ctx& c);
+void launch_source(Ctx& c);
+void launch_rhs(Ctx& c, bool have_force);
+void launch_assemble(Ctx& c);
+void launch_preconditioner(Ctx& c);
+void launch_to_f32(Ctx& c);
+void launch_scatter_flow(Ctx& c, double* flow_out);
+void launch_check_finite(Ctx& c, const double* a, int64_t n);
+void launch_any_abs_above(Ctx& c, const double* a, int64_t n, double thr);
+
+// ---- Krylov (krylov.cu) ------------------------------------------------------
+// r = b - S x (FP64) and ||r||^2, ||b||^2 into c.os
+void launch_residual64(Ctx& c);
+// inner MINRES on S d = r0 in precision T; returns the number of iterations
+template <typename T>
+long long minres_inner(Ctx& c, double rtol, long long maxit, double* achieved, int* status);
+void launch_prepare_inner32(Ctx& c);       // r0_32 = r * scale
+void launch_update_x64(Ctx& c);            // x += d (FP64 inner)
+void launch_update_x_from32(Ctx& c);       // x += d32 / scale
+void launch_apply(Ctx& c, int precision, const V4<double>* in, V4<double>* out);
+
+template <typename T>
+inline T* dev_alloc(Ctx& c, size_t n) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(T) + 16);
+    if (e != cudaSuccess) throw CudaError(e, "cudaMalloc", __FILE__, __LINE__);
+    c.device_bytes += (int64_t)(n * sizeof(T));
+    return static_cast<T*>(p);
+}
+
+inline int grid_for(const Ctx& c, int64_t work, int threads = kThreads, int per_sm = 8) {
+    int64_t need = (work + threads - 1) / threads;
+    int64_t cap = (int64_t)c.num_sms * per_sm;
+    if (need < 1) need = 1;
+    return (int)(need < cap ? need : cap);
+}
+
+}  // namespace fts

@@ -1,0 +1,49 @@
+// Internal declarations shared by the host setup code (setup.cpp) and the
+// CUDA translation units.  Not part of the public ABI.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "fts.h"
+
+namespace fts {
+
+// Host-side mesh topology built once per context (Flow::init's share of
+// Mesh3D: p2t, the node graph and the interior-dof flags).
+struct HostTopology {
+    int64_t np = 0, nt = 0;
+    std::vector<int32_t> rowptr;   // [np+1] block rows of the node graph
+    std::vector<int32_t> cols;     // [nnzb] sorted neighbour nodes incl. self
+    std::vector<int32_t> diag;     // [np] position of (i,i) in cols
+    std::vector<int32_t> p2t_ptr;  // [np+1]
+    std::vector<uint32_t> p2t;     // [4 nt] (tet << 2 | local index), ascending tet per node
+    std::vector<uint8_t> bnd;      // [np] 1 = Dirichlet velocity node
+    int32_t max_row = 0;           // longest block row
+    int32_t max_p2t = 0;           // most tetrahedra around one node
+    int32_t lattice_n = 0;         // n if the mesh is the Kuhn lattice of n^3 nodes (index
+                                   // i + n j + n^2 k, Kuhn node graph), else 0
+    int64_t n_interior = 0;        // nI
+};
+
+// Validates the mesh and builds the topology (OpenMP).  Returns an fts_status.
+int build_topology(const fts_mesh& m, HostTopology& T, std::string& err);
+
+// Exterior-boundary nodes: nodes of the triangles that belong to exactly one
+// tetrahedron (TetraMesh.cpp:266-269).
+void boundary_from_faces(const fts_mesh& m, const HostTopology& T, std::vector<uint8_t>& bnd);
+
+// Reference-element constants (float-rounded basis table at the 4-point rule,
+// Quadrature.hpp:24-36, :102-112; Tetrahedron.hpp:17-18, :27-51):
+//   wq[b]     = sum_q 0.25 phi_b(q)             (so that int psi_b = vol * wq[b])
+//   mref[a][b] = sum_q 0.25 phi_a(q) phi_b(q)    (so that M_ab = vol * mref[a][b])
+struct RefConstants {
+    double wq[4];
+    double mref[4][4];
+};
+RefConstants ref_constants();
+
+double wall_ms();
+
+}  // namespace fts

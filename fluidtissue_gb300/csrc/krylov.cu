@@ -1,0 +1,427 @@
+// Block-sparse operator application and preconditioned MINRES (Paige &
+// Saunders 1975) on the symmetric form of the stabilised Stokes system, in FP64
+// or FP32.  One MINRES iteration is three kernels:
+//   A: q = S v (v = y / beta) fused with the dot products v.q and v.r1
+//   B: Lanczos update r_new = q - (beta/oldb) r1 - (alpha/beta) r2, the
+//      block-diagonal preconditioner y = P^-1 r_new and the dot r_new.y
+//   C: w_new = (v - oldeps w_prev - delta w_cur) / gamma, x += phi w_new
+// The scalar recurrences run in the last block of A and B (a grid ticket), so
+// the iteration never waits on the host; the host polls the stop flag every few
+// iterations.  Dot products accumulate in FP64 in both precisions.
+//
+// The reference solves the same system with Eigen's un-preconditioned BiCGSTAB
+// (src/growth/Flow.hpp:62, Flow.cpp:266); the stopping quantity is the same
+// relative residual ||b - A x|| / ||b||, checked in FP64 by the outer loop.
+#include <cfloat>
+#include <cmath>
+
+#include "fts_device.cuh"
+#include "reduce.cuh"
+
+namespace fts {
+
+template <typename T>
+__device__ __forceinline__ V4<T> ld4(const V4<T>* p) {
+    return *p;
+}
+
+template <typename T>
+__device__ __forceinline__ T bsr_row_dot(const T* __restrict__ A, const int32_t* __restrict__ cols,
+                                         int32_t k0, int32_t k1, int r,
+                                         const V4<T>* __restrict__ x) {
+    T acc = T(0);
+    for (int32_t k = k0; k < k1; ++k) {
+        const int32_t j = __ldg(cols + k);
+        const V4<T> a = *reinterpret_cast<const V4<T>*>(A + (int64_t)k * 16 + r * 4);
+        const V4<T> xj = x[j];
+        acc = fma(a.x, xj.x, acc);
+        acc = fma(a.y, xj.y, acc);
+        acc = fma(a.z, xj.z, acc);
+        acc = fma(a.w, xj.w, acc);
+    }
+    return acc;
+}
+
+template <typename T>
+__device__ __forceinline__ T comp(const V4<T>& v, int r) {
+    return r == 0 ? v.x : (r == 1 ? v.y : (r == 2 ? v.z : v.w));
+}
+
+// ---------------------------------------------------------------------------
+// Plain operator application (tests / inspection): out = S in.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_apply(int64_t np, const int32_t* __restrict__ rowptr,
+                        const int32_t* __restrict__ cols, const T* __restrict__ A,
+                        const V4<T>* __restrict__ in, T* __restrict__ out) {
+    const int r = threadIdx.x & 3;
+    for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 2; row < np;
+         row += ((int64_t)gridDim.x * blockDim.x) >> 2) {
+        out[row * 4 + r] = bsr_row_dot<T>(A, cols, rowptr[row], rowptr[row + 1], r, in);
+    }
+}
+
+__global__ void k_cast_d2f(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+__global__ void k_cast_f2d(int64_t n, const float* __restrict__ a, double* __restrict__ b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (double)a[i];
+}
+
+void launch_apply(Ctx& c, int precision, const V4<double>* in, V4<double>* out) {
+    int grid = grid_for(c, c.np * 4);
+    if (precision == FTS_PREC_MIXED) {
+        k_cast_d2f<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(
+            c.np * 4, reinterpret_cast<const double*>(in), reinterpret_cast<float*>(c.w32.q));
+        k_apply<float><<<grid, kThreads, 0, c.stream>>>(c.np, c.rowptr, c.cols, c.A32, c.w32.q,
+                                                        reinterpret_cast<float*>(c.w32.r0));
+        k_cast_f2d<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(
+            c.np * 4, reinterpret_cast<const float*>(c.w32.r0), reinterpret_cast<double*>(out));
+    } else {
+        k_apply<double><<<grid, kThreads, 0, c.stream>>>(c.np, c.rowptr, c.cols, c.A64, in,
+                                                         reinterpret_cast<double*>(out));
+    }
+    FTS_CUDA(cudaGetLastError());
+    c.launches += precision == FTS_PREC_MIXED ? 3 : 1;
+}
+
+// ---------------------------------------------------------------------------
+// Outer residual (FP64): r = b - S x, ||r||^2, ||b||^2.
+// ---------------------------------------------------------------------------
+__global__ void k_residual64(int64_t np, const int32_t* __restrict__ rowptr,
+                             const int32_t* __restrict__ cols, const double* __restrict__ A,
+                             const V4<double>* __restrict__ x, const V4<double>* __restrict__ b,
+                             double* __restrict__ r, Reduction red, OuterScalars* os) {
+    const int rr = threadIdx.x & 3;
+    double acc[2] = {0.0, 0.0};
+    for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 2; row < np;
+         row += ((int64_t)gridDim.x * blockDim.x) >> 2) {
+        double ax = bsr_row_dot<double>(A, cols, rowptr[row], rowptr[row + 1], rr, x);
+        double bv = reinterpret_cast<const double*>(b)[row * 4 + rr];
+        double v = bv - ax;
+        r[row * 4 + rr] = v;
+        acc[0] += v * v;
+        acc[1] += bv * bv;
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
+        os->rr = tot[0];
+        os->bb = tot[1];
+        os->scale = tot[0] > 0.0 ? 1.0 / sqrt(tot[0]) : 0.0;
+        os->nonfinite = isfinite(tot[0]) ? 0 : 1;
+    }
+}
+
+void launch_residual64(Ctx& c) {
+    k_residual64<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(
+        c.np, c.rowptr, c.cols, c.A64, c.x, c.b, reinterpret_cast<double*>(c.r), c.red, c.os);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+// ---------------------------------------------------------------------------
+// MINRES kernels
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ V4<T> apply_pc(const T* __restrict__ pc, int64_t i, const V4<T>& v) {
+    const V4<T> p0 = *reinterpret_cast<const V4<T>*>(pc + 8 * i);
+    const V4<T> p1 = *reinterpret_cast<const V4<T>*>(pc + 8 * i + 4);
+    V4<T> z;
+    z.x = p0.x * v.x + p0.y * v.y + p0.z * v.z;
+    z.y = p0.y * v.x + p0.w * v.y + p1.x * v.z;
+    z.z = p0.z * v.x + p1.x * v.y + p1.y * v.z;
+    z.w = p1.z * v.w;
+    return z;
+}
+
+// r0 -> R2 (= R[0]), y = P^-1 r0 -> Y[0], beta1 = sqrt(r0 . y).
+template <typename T>
+__global__ void k_minres_init(int64_t np, const V4<T>* __restrict__ r0, const T* __restrict__ pc,
+                              V4<T>* __restrict__ R2, V4<T>* __restrict__ Y, double rtol,
+                              long long maxit, Reduction red, MinresScalars* s) {
+    double acc[1] = {0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        V4<T> v = r0[i];
+        R2[i] = v;
+        V4<T> z = apply_pc<T>(pc, i, v);
+        Y[i] = z;
+        acc[0] += (double)(v.x * z.x) + (double)(v.y * z.y) + (double)(v.z * z.z) +
+                  (double)(v.w * z.w);
+    }
+    double tot[1];
+    if (grid_sum<1>(acc, red, tot) && threadIdx.x == 0) {
+        double b1 = tot[0] > 0.0 ? sqrt(tot[0]) : 0.0;
+        s->beta1 = b1;
+        s->beta = b1;
+        s->oldb = 0.0;
+        s->alfa = 0.0;
+        s->dbar = 0.0;
+        s->epsln = 0.0;
+        s->oldeps = 0.0;
+        s->delta = 0.0;
+        s->gamma = 1.0;
+        s->phi = 0.0;
+        s->phibar = b1;
+        s->cs = -1.0;
+        s->sn = 0.0;
+        s->target = rtol * b1;
+        s->iters = 0;
+        s->maxit = maxit;
+        s->c_pending = 0;
+        s->status = isfinite(tot[0]) ? 0 : 2;
+        s->stop = (!(b1 > 0.0) || !isfinite(tot[0])) ? 1 : 0;
+    }
+}
+
+// A: q = S (y / beta); partial dots v.q and v.r1.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_minres_A(int64_t np, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ cols,
+           const T* __restrict__ A, const V4<T>* __restrict__ Y, const V4<T>* __restrict__ R1,
+           T* __restrict__ q, Reduction red, MinresScalars* s) {
+    if (s->stop) return;
+    const double invb = 1.0 / s->beta;
+    const T tinv = (T)invb;
+    const int r = threadIdx.x & 3;
+    double acc[2] = {0.0, 0.0};
+    const T* y = reinterpret_cast<const T*>(Y);
+    const T* r1 = reinterpret_cast<const T*>(R1);
+    for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 2; row < np;
+         row += ((int64_t)gridDim.x * blockDim.x) >> 2) {
+        T ax = bsr_row_dot<T>(A, cols, rowptr[row], rowptr[row + 1], r, Y);
+        T qv = ax * tinv;
+        const int64_t e = row * 4 + r;
+        q[e] = qv;
+        T ve = y[e] * tinv;
+        acc[0] += (double)(ve * qv);
+        acc[1] += (double)(ve * r1[e]);
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
+        double c1 = s->iters >= 1 ? s->beta / s->oldb : 0.0;
+        s->alfa = tot[0] - c1 * tot[1];
+    }
+}
+
+// B: r_new = q - c1 r1 - c2 r2 (into R1's buffer), y_new = P^-1 r_new, beta.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_minres_B(int64_t np, const V4<T>* __restrict__ q, V4<T>* R1, const V4<T>* __restrict__ R2,
+           const T* __restrict__ pc, V4<T>* __restrict__ Ynew, Reduction red, MinresScalars* s) {
+    if (s->stop) return;
+    const T c1 = (T)(s->iters >= 1 ? s->beta / s->oldb : 0.0);
+    const T c2 = (T)(s->alfa / s->beta);
+    double acc[1] = {0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const V4<T> qv = q[i], a = R1[i], b2 = R2[i];
+        V4<T> n;
+        n.x = qv.x - c1 * a.x - c2 * b2.x;
+        n.y = qv.y - c1 * a.y - c2 * b2.y;
+        n.z = qv.z - c1 * a.z - c2 * b2.z;
+        n.w = qv.w - c1 * a.w - c2 * b2.w;
+        R1[i] = n;
+        const V4<T> z = apply_pc<T>(pc, i, n);
+        Ynew[i] = z;
+        acc[0] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z) +
+                  (double)(n.w * z.w);
+    }
+    double tot[1];
+    if (grid_sum<1>(acc, red, tot) && threadIdx.x == 0) {
+        const double alfa = s->alfa;
+        s->oldb = s->beta;
+        const double beta = tot[0] > 0.0 ? sqrt(tot[0]) : 0.0;
+        s->beta = beta;
+        s->oldeps = s->epsln;
+        const double delta = s->cs * s->dbar + s->sn * alfa;
+        const double gbar = s->sn * s->dbar - s->cs * alfa;
+        s->epsln = s->sn * beta;
+        s->dbar = -s->cs * beta;
+        double gamma = sqrt(gbar * gbar + beta * beta);
+        if (gamma < DBL_MIN) gamma = DBL_MIN;
+        s->delta = delta;
+        s->gamma = gamma;
+        s->cs = gbar / gamma;
+        s->sn = beta / gamma;
+        s->phi = s->cs * s->phibar;
+        s->phibar = s->sn * s->phibar;
+        s->iters += 1;
+        s->c_pending = 1;
+        if (!isfinite(tot[0]) || !isfinite(s->phibar)) {
+            s->status = 2;
+            s->stop = 1;
+        } else if (s->phibar <= s->target || !(beta > 0.0)) {
+            s->stop = 1;
+        } else if (s->iters >= s->maxit) {
+            s->status = 1;
+            s->stop = 1;
+        }
+    }
+}
+
+// C: w_new = (v - oldeps w_prev - delta w_cur) / gamma (into w_prev), x += phi w_new.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_minres_C(int64_t np, const V4<T>* __restrict__ Yk, V4<T>* Wprev, const V4<T>* __restrict__ Wcur,
+           V4<T>* __restrict__ X, Reduction red, MinresScalars* s) {
+    if (!s->c_pending) return;
+    const T inv = (T)(1.0 / s->oldb);
+    const T oe = (T)s->oldeps, de = (T)s->delta, ig = (T)(1.0 / s->gamma), ph = (T)s->phi;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const V4<T> y = Yk[i], wp = Wprev[i], wc = Wcur[i];
+        V4<T> w, xv = X[i];
+        w.x = (y.x * inv - oe * wp.x - de * wc.x) * ig;
+        w.y = (y.y * inv - oe * wp.y - de * wc.y) * ig;
+        w.z = (y.z * inv - oe * wp.z - de * wc.z) * ig;
+        w.w = (y.w * inv - oe * wp.w - de * wc.w) * ig;
+        Wprev[i] = w;
+        xv.x += ph * w.x;
+        xv.y += ph * w.y;
+        xv.z += ph * w.z;
+        xv.w += ph * w.w;
+        X[i] = xv;
+    }
+    if (last_block(red) && threadIdx.x == 0) s->c_pending = 0;
+}
+
+template <typename T>
+static const T* op_of(const Ctx& c);
+template <>
+const double* op_of<double>(const Ctx& c) { return c.A64; }
+template <>
+const float* op_of<float>(const Ctx& c) { return c.A32; }
+template <typename T>
+static const T* pc_of(const Ctx& c);
+template <>
+const double* pc_of<double>(const Ctx& c) { return c.pc64; }
+template <>
+const float* pc_of<float>(const Ctx& c) { return c.pc32; }
+template <typename T>
+static KrylovWork<T>& work_of(Ctx& c);
+template <>
+KrylovWork<double>& work_of<double>(Ctx& c) { return c.w64; }
+template <>
+KrylovWork<float>& work_of<float>(Ctx& c) { return c.w32; }
+
+// Runs MINRES on S d = r0 (work.r0; for FP64 the outer residual c.r) from
+// d = 0 until the preconditioned residual norm drops by rtol.  Returns the
+// iteration count; *achieved = phibar / beta1, *status = scalar status.
+template <typename T>
+long long minres_inner(Ctx& c, double rtol, long long maxit, double* achieved, int* status) {
+    KrylovWork<T>& w = work_of<T>(c);
+    const T* A = op_of<T>(c);
+    const T* pc = pc_of<T>(c);
+    const int64_t np = c.np;
+    const V4<T>* r0 = w.r0;
+    FTS_CUDA(cudaMemsetAsync(w.W[0], 0, np * sizeof(V4<T>), c.stream));
+    FTS_CUDA(cudaMemsetAsync(w.W[1], 0, np * sizeof(V4<T>), c.stream));
+    FTS_CUDA(cudaMemsetAsync(w.X, 0, np * sizeof(V4<T>), c.stream));
+    FTS_CUDA(cudaMemsetAsync(w.R[1], 0, np * sizeof(V4<T>), c.stream));
+    const int gn = grid_for(c, np);
+    const int ge = grid_for(c, np * 4);
+    k_minres_init<T><<<gn, kThreads, 0, c.stream>>>(np, r0, pc, w.R[0], w.Y[0], rtol, maxit,
+                                                    c.red, c.ms);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+    const bool timed = c.par.time_kernels != 0;
+    if (timed && !c.tev_ready) {
+        for (auto& e : c.tev) FTS_CUDA(cudaEventCreate(&e));
+        c.tev_ready = true;
+    }
+    const int poll = np > 200000 ? 8 : 32;  // <= Ctx::kTimedPairs
+    long long k = 0, done_before = 0;
+    for (;;) {
+        for (int u = 0; u < poll; ++u) {
+            ++k;
+            const int p = (int)(k & 1);       // r1 = R[p], r2 = R[1-p], new -> R[p]
+            V4<T>* R1 = w.R[p];
+            V4<T>* R2 = w.R[1 - p];
+            V4<T>* Yk = w.Y[(k - 1) & 1];
+            V4<T>* Yn = w.Y[k & 1];
+            V4<T>* Wprev = w.W[p];
+            V4<T>* Wcur = w.W[1 - p];
+            if (timed) FTS_CUDA(cudaEventRecord(c.tev[2 * u], c.stream));
+            k_minres_A<T><<<ge, kThreads, 0, c.stream>>>(np, c.rowptr, c.cols, A, Yk, R1,
+                                                         reinterpret_cast<T*>(w.q), c.red, c.ms);
+            if (timed) FTS_CUDA(cudaEventRecord(c.tev[2 * u + 1], c.stream));
+            k_minres_B<T><<<gn, kThreads, 0, c.stream>>>(np, w.q, R1, R2, pc, Yn, c.red, c.ms);
+            k_minres_C<T><<<gn, kThreads, 0, c.stream>>>(np, Yk, Wprev, Wcur, w.X, c.red, c.ms);
+        }
+        c.launches += 3 * poll;
+        FTS_CUDA(cudaGetLastError());
+        FTS_CUDA(cudaMemcpyAsync(c.ms_host, c.ms, sizeof(MinresScalars), cudaMemcpyDeviceToHost,
+                                 c.stream));
+        FTS_CUDA(cudaStreamSynchronize(c.stream));
+        // operator applications that did work in this chunk = completed iterations
+        const long long ran = c.ms_host->iters - done_before;
+        done_before = c.ms_host->iters;
+        if (timed) {
+            for (long long u = 0; u < ran && u < poll; ++u) {
+                float ms = 0.f;
+                FTS_CUDA(cudaEventElapsedTime(&ms, c.tev[2 * u], c.tev[2 * u + 1]));
+                c.ms_spmv += ms;
+            }
+        }
+        c.spmv_runs += ran;
+        if (c.ms_host->stop) break;
+    }
+    const MinresScalars& S = *c.ms_host;
+    *achieved = S.beta1 > 0.0 ? S.phibar / S.beta1 : 0.0;
+    *status = S.status;
+    return S.iters;
+}
+
+template long long minres_inner<double>(Ctx&, double, long long, double*, int*);
+template long long minres_inner<float>(Ctx&, double, long long, double*, int*);
+
+// r0_32 = r * (1/||r||) (FP32 right-hand side of the inner solve).
+__global__ void k_prepare_inner32(int64_t n, const double* __restrict__ r,
+                                  const OuterScalars* __restrict__ os, float* __restrict__ r32) {
+    const double sc = os->scale;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        r32[i] = (float)(r[i] * sc);
+}
+
+void launch_prepare_inner32(Ctx& c) {
+    k_prepare_inner32<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(
+        c.np * 4, reinterpret_cast<const double*>(c.r), c.os, reinterpret_cast<float*>(c.w32.r0));
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+__global__ void k_update_x64(int64_t n, const double* __restrict__ d, double* __restrict__ x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        x[i] += d[i];
+}
+
+void launch_update_x64(Ctx& c) {
+    k_update_x64<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(
+        c.np * 4, reinterpret_cast<const double*>(c.w64.X), reinterpret_cast<double*>(c.x));
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+__global__ void k_update_x_from32(int64_t n, const float* __restrict__ d,
+                                  const OuterScalars* __restrict__ os, double* __restrict__ x) {
+    const double rn = os->scale > 0.0 ? 1.0 / os->scale : 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        x[i] += rn * (double)d[i];
+}
+
+void launch_update_x_from32(Ctx& c) {
+    k_update_x_from32<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(
+        c.np * 4, reinterpret_cast<const float*>(c.w32.X), c.os, reinterpret_cast<double*>(c.x));
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+}  // namespace fts

@@ -1,0 +1,209 @@
+/*
+ * fts.h — C ABI of libfts.so, the GB300-native variable-viscosity P1-P1
+ * Stokes solve of fluidtissue (one Stokes step of the growth loop).
+ *
+ * It replaces the C++ class Flow (src/growth/Flow.hpp:15-63):
+ *   Flow::init(const LevelSet&, const Parameters&)   -> fts_create
+ *   Flow::solve(const LevelSet&, const VecXd&, VecXd&) -> fts_solve
+ *   Flow::~Flow                                       -> fts_destroy
+ * The same inputs go in — the tetrahedral mesh (Mesh3D::p float xyz, Mesh3D::t),
+ * the nodal level set phi (LevelSet::getPhi), the nodal growth factor "source"
+ * (growth.cpp:73-76) — and the same output comes out: flow[4*np] =
+ * [ux(np), uy(np), uz(np), p(np)] with zero velocity on the exterior boundary
+ * (Flow.cpp:290-300).
+ *
+ * Plain pointers and sizes only; no exceptions cross the boundary; every call
+ * returns an fts_status.  A context is not re-entrant; distinct contexts may be
+ * used from distinct host threads.  All work of a context runs on one GPU
+ * (fts_params.device) and on one CUDA stream (fts_set_stream).
+ */
+#ifndef FTS_H
+#define FTS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference returns 0 / -1 (Flow.cpp:84, :281-285); the
+ * non-zero codes here refine its -1. */
+typedef enum fts_status {
+    FTS_OK = 0,
+    FTS_ERR_BAD_INPUT = 1,          /* null pointer, size or index out of range, unsupported option */
+    FTS_ERR_DEGENERATE_ELEMENT = 2, /* a tetrahedron with det B == 0 (Assembler.hpp:446-457) */
+    FTS_ERR_NOT_CONVERGED = 3,      /* the solver stopped above the tolerance (Flow.cpp:281-285) */
+    FTS_ERR_CUDA = 4,               /* a CUDA runtime call failed */
+    FTS_ERR_OOM = 5,                /* device allocation failed */
+    FTS_ERR_UNSUPPORTED = 6,        /* a reference option outside this path (surface tension, P2) */
+    FTS_ERR_NAN = 7                 /* NaN or Inf in the inputs or in the iteration */
+} fts_status;
+
+/* Arithmetic of the solve. */
+enum {
+    FTS_PREC_FP64 = 0,  /* FP64 assembly, SpMV, Krylov (parity path) */
+    FTS_PREC_MIXED = 1  /* FP32 inner Krylov (SpMV, preconditioner, vector updates) with an
+                           FP64 outer refinement loop (residual, solution update, dot products) */
+};
+
+/* Krylov method. */
+enum {
+    FTS_SOLVER_MINRES = 0,   /* preconditioned MINRES on the symmetric form (default) */
+    FTS_SOLVER_BICGSTAB = 1  /* un-preconditioned BiCGSTAB on the reference's form, as Flow.hpp:62 */
+};
+
+/* Velocity-block preconditioner of MINRES. */
+enum {
+    FTS_PC_AUTO = 0,      /* multigrid when the mesh is a Kuhn lattice with odd n, else Jacobi */
+    FTS_PC_JACOBI = 1,    /* node 3x3 block Jacobi (any mesh) */
+    FTS_PC_MULTIGRID = 2  /* geometric multigrid V-cycle (Kuhn lattices only) */
+};
+
+/* Operator representation. */
+enum {
+    FTS_OP_AUTO = 0,       /* assembled BSR */
+    FTS_OP_ASSEMBLED = 1,  /* node-blocked 4x4 BSR, assembled every solve */
+    FTS_OP_MATFREE = 2     /* element-by-element operator for the FP32 inner solve */
+};
+
+/* Mesh3D (src/fem/TetraMesh.hpp:49-62).  The library copies what it needs
+ * during fts_create and keeps no pointer. */
+typedef struct fts_mesh {
+    int64_t np;               /* nodes */
+    int64_t nt;               /* tetrahedra */
+    const float* xyz;         /* [3*np] node coordinates x,y,z per node (Mesh3D::p, Vec3f) */
+    const int32_t* tets;      /* [4*nt] node indices per tetrahedron (Mesh3D::t) */
+    const uint8_t* boundary;  /* [np] nullable: 1 = node on an exterior boundary triangle.
+                                 NULL: derived from the triangles that belong to exactly one
+                                 tetrahedron (TetraMesh.cpp:266-269). */
+} fts_mesh;
+
+/* The Parameters keys the Stokes step reads (Flow.cpp:23, :77-82, :105,
+ * :199, :223-228, :359-372; ViscosityProfiles.hpp:32-59), plus GB300 options.
+ * Start from fts_params_default(). */
+typedef struct fts_params {
+    int32_t velocity_degree;    /* "Stokes velocity degree": 1 (P1-P1 stabilised) */
+    double alpha;               /* "alpha": Brezzi-Pitkaranta weight of h^2 (grad p, grad q) */
+    double eps;                 /* "eps": pressure mass regularisation */
+    double tol;                 /* "Stokes tolerance": stop at ||b - A x|| <= tol ||b|| */
+    int32_t max_iter;           /* "Max. CG iterations" (<= 0: 2 N as Eigen's default) */
+    double mu_interior;         /* "Viscosity interior" */
+    double mu_exterior;         /* "Viscosity exterior" */
+    int32_t mu_profile;         /* "Viscosity profile": 0 INVERSE, 1 DIRECT, 2 DIRECT_RATE4X */
+    double gf_growth;           /* "GF growth" */
+    double level_sink;          /* "Level sink" */
+    double growth_threshold;    /* "Growth threshold" */
+    double rd_iterations;       /* "RD iterations" (selects maxGF and the early exit) */
+    double gf_production;       /* "GF production" */
+    double advection_dt;        /* "Advection dt" (< FLT_MIN: nothing to solve) */
+    double surface_tension;     /* "Surface tension": must be 0 on this path */
+    /* GB300 options */
+    int32_t precision;          /* FTS_PREC_* */
+    int32_t solver;             /* FTS_SOLVER_* */
+    int32_t preconditioner;     /* FTS_PC_* */
+    int32_t operator_kind;      /* FTS_OP_* */
+    int32_t warm_start;         /* 1: start from the previous solution (USE_INITIAL_GUESS,
+                                   Flow.cpp:15); 0: start from zero */
+    int32_t device;             /* CUDA device ordinal */
+    double inner_tol;           /* mixed precision: relative reduction asked of each FP32
+                                   inner solve (<= 0: default 1e-4) */
+    int32_t verbose;            /* 1: print the reference's progress lines to stdout */
+    int32_t time_kernels;       /* 1: bracket every operator application of the Krylov
+                                   loop with CUDA events (fills fts_stats.ms_spmv) */
+} fts_params;
+
+/* Per-solve statistics (the quantities Flow.cpp prints, plus timings). */
+typedef struct fts_stats {
+    int32_t status;            /* fts_status of the call */
+    int32_t solved;            /* 0 when an early exit left flow untouched (Flow.cpp:223-251) */
+    int64_t iterations;        /* Krylov iterations, all precisions (Flow.cpp:270) */
+    int64_t iterations_fp32;   /* of which in the FP32 inner solver */
+    int32_t outer_iterations;  /* FP64 residual recomputations */
+    double rel_residual;       /* true ||b - A x|| / ||b|| in FP64 at return */
+    double error_estimate;     /* the solver's own estimate (Flow.cpp:271) */
+    double mu_min, mu_max;     /* over interior elements (Flow.cpp:241) */
+    double f_norm;             /* ||F|| (Flow.cpp:248) */
+    double ms_assembly;        /* device time of viscosity, source, RHS and matrix assembly */
+    double ms_solve;           /* device time of the Krylov solve */
+    double ms_total;           /* wall time of the call */
+    int64_t device_bytes;      /* device memory held by the context */
+    int64_t kernel_launches;   /* kernels this library launched during the call */
+    int64_t spmv_launches;     /* operator applications inside the Krylov loop */
+    double ms_spmv;            /* their summed CUDA-event time (time_kernels = 1) */
+    double spmv_bytes;         /* algorithmic bytes of one such application */
+    double spmv_bytes_fp64;    /* the same for the FP64 operator */
+} fts_stats;
+
+typedef struct fts_ctx fts_ctx;
+
+/* Defaults: P1, alpha 0.032, eps 1e-3, tol 1e-4 (parameters/summary.txt),
+ * profile INVERSE with equal viscosities, FP64, MINRES, AUTO preconditioner and
+ * operator, warm start on, device 0. */
+void fts_params_default(fts_params* p);
+
+/* Flow::init (src/growth/Flow.cpp:20-85): validates and uploads the mesh,
+ * builds the dof map, the block sparsity pattern and the per-element geometry.
+ * Returns FTS_ERR_DEGENERATE_ELEMENT if any tetrahedron is flat. */
+int fts_create(const fts_mesh* mesh, const fts_params* params, fts_ctx** out);
+
+/* Flow::solve (src/growth/Flow.cpp:89-94, :218-302) with host arrays:
+ *   phi[np]    level set (interior = phi < 0, LevelSet.cpp:180-211)
+ *   source[np] growth factor (or activator)
+ *   mu[nt]     nullable: per-element viscosity; NULL = setViscosity's profile
+ *              (ViscosityProfiles.hpp:27-72)
+ *   force[3*np] nullable: nodal body force [fx(np), fy(np), fz(np)] (the
+ *              surface-tension load slot of Flow.cpp:352-363)
+ *   flow[4*np] output [ux, uy, uz, p]; left untouched by the early exits
+ *   stats      nullable
+ * The inputs are copied to the device, the system is assembled and solved on
+ * the GPU and the result copied back; the call returns when flow is filled. */
+int fts_solve(fts_ctx* ctx, const double* phi, const double* source, const double* mu,
+              const double* force, double* flow, fts_stats* stats);
+
+/* The same with device pointers (no host copies); flow may be device memory. */
+int fts_solve_device(fts_ctx* ctx, const double* phi, const double* source, const double* mu,
+                     const double* force, double* flow, fts_stats* stats);
+
+/* Stream for all subsequent work of ctx (a cudaStream_t; NULL = the context's
+ * own stream). */
+int fts_set_stream(fts_ctx* ctx, void* stream);
+
+/* Replace the solver options of an existing context (precision, solver,
+ * preconditioner, tolerances, warm start); the mesh stays. */
+int fts_update_params(fts_ctx* ctx, const fts_params* params);
+
+/* Reset the warm-start vector (Flow::up_, Flow.cpp:47-48) to zero. */
+int fts_reset_guess(fts_ctx* ctx);
+
+/* Frees all device and host memory of ctx. */
+void fts_destroy(fts_ctx* ctx);
+
+/* Human-readable text of a status code. */
+const char* fts_status_string(int status);
+
+/* Last error message recorded on ctx (empty if none). */
+const char* fts_last_error(const fts_ctx* ctx);
+
+/* ---- inspection (tests and profiling) ---------------------------------- */
+
+/* Sizes of the assembled node-block system: np, block nonzeros, and the
+ * reference's reduced dimension N = 3 nI + np (Flow.cpp:35-44). */
+int fts_get_sizes(const fts_ctx* ctx, int64_t* np, int64_t* nnzb, int64_t* n_reduced);
+
+/* Copies the last assembled FP64 block matrix to host arrays: rowptr[np+1],
+ * cols[nnzb], vals[16*nnzb] (row-major 4x4 per block over ux,uy,uz,p, in the
+ * symmetric sign convention: pressure rows negated; boundary velocity rows and
+ * columns replaced by identity / zero), rhs[4*np] (same convention). */
+int fts_get_system(const fts_ctx* ctx, int32_t* rowptr, int32_t* cols, double* vals, double* rhs);
+
+/* Applies the assembled operator: y = S x on host vectors of length 4*np,
+ * node-interleaved (ux,uy,uz,p per node); precision FTS_PREC_FP64 or
+ * FTS_PREC_MIXED (the FP32 copy). */
+int fts_apply(fts_ctx* ctx, int32_t precision, const double* x, double* y);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FTS_H */
