@@ -1,0 +1,362 @@
+"""Benchmark: variable-viscosity P1-P1 Stokes solves/s on one GB300.
+
+Workload (default): ``ellipsoid129`` — 129^3 Kuhn lattice (12.6M tets),
+jitter +-0.1h, ellipsoid level set, 16 Gaussian centres, mu = clip(1/(0.01+c),
+0.01, 100), relative residual 1e-8.  One step = one complete Stokes solve
+(viscosity, source, RHS and matrix assembly, Krylov solve, scatter to flow)
+from a zero initial guess, inputs resident in HBM.
+
+Reported:
+  value     mixed-precision solves/s (device-resident inputs)
+  e2e       the same through fts_solve with pinned host buffers (H2D of
+            phi/source/mu and D2H of flow inside the timed region)
+  fp64      the plain FP64 GPU path on the same workload
+  roofline  the Krylov loop's operator kernel (BSR SpMV fused with the MINRES
+            dots), algorithmic bytes / CUDA-event time, vs measured HBM peak
+  cpu_baseline  the CPU oracle (restated reference algorithm) on the box's
+            host cores, bounded sample
+
+``--impl reference`` times the reference's algorithm on the host CPU (the
+oracle port): assembly + un-preconditioned BiCGSTAB, bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Stokes solves/s at 129^3 to 1e-8 resid: mixed-prec vs FP64 GPU; SpMV HBM GB/s"
+UNIT = "solves/s"
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic(kernel: str):
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get(kernel)
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, idx: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(idx), f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _setup_dist(ws, local, backend="nccl"):
+    import torch
+    import torch.distributed as dist
+    if ws > 1 and not dist.is_initialized():
+        torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return dist if ws > 1 else None
+
+
+def _max_over_ranks(v: float, dist) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def run_ours(args):
+    import torch
+    from fluidtissue_gb300 import workloads as W
+    from fluidtissue_gb300.flow import Flow, Mesh
+
+    ws, rank, local = _dist()
+    dist = _setup_dist(ws, local)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    inst = W.WORKLOADS[args.workload]()
+    par = dict(inst.params)
+    npn, nt = inst.np, inst.nt
+
+    stream = torch.cuda.Stream(device=dev)
+    phi_d = torch.from_numpy(inst.phi).to(dev)
+    src_d = torch.from_numpy(inst.source).to(dev)
+    mu_d = torch.from_numpy(inst.mu).to(dev)
+    flow_d = torch.zeros(4 * npn, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+
+    def make(precision):
+        f = Flow()
+        rc = f.init(Mesh(inst.xyz, inst.tets), par, precision=precision, warm_start=False,
+                    device=local, preconditioner=args.preconditioner, time_kernels=True,
+                    inner_tol=args.inner_tol)
+        if rc != 0:
+            raise RuntimeError(f"fts_create failed ({rc}): {f.last_error()}")
+        f.set_stream(stream.cuda_stream)
+        return f
+
+    def device_steps(f, k):
+        stats = []
+        for _ in range(k):
+            rc = f.solve_device(phi_d.data_ptr(), src_d.data_ptr(), mu_d.data_ptr(),
+                                flow_d.data_ptr())
+            if rc != 0:
+                raise RuntimeError(f"fts_solve_device failed ({rc}): {f.last_error()}")
+            stats.append(dict(f.last_stats))
+        return stats
+
+    def timed(fn, k, clocks_idx=None):
+        _barrier(dist)
+        torch.cuda.synchronize()
+        clk = Clocks(clocks_idx) if clocks_idx is not None else None
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        t0 = time.perf_counter()
+        out = fn(k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        ms = e0.elapsed_time(e1)
+        _barrier(dist)
+        clocks = clk.stop() if clk else None
+        return out, _max_over_ranks(ms, dist), wall, clocks
+
+    # ---- mixed precision, device-resident inputs (value) --------------------
+    fm = make("mixed")
+    device_steps(fm, args.warmup)
+    stats_m, ms_m, wall_m, clocks = timed(lambda k: device_steps(fm, k), args.steps, local)
+    value = ws * args.steps / (ms_m / 1e3)
+
+    # ---- e2e through fts_solve with pinned host buffers ----------------------
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    phi_h, src_h, mu_h = pin(inst.phi), pin(inst.source), pin(inst.mu)
+    flow_h = torch.zeros(4 * npn, dtype=torch.float64).pin_memory().numpy()
+
+    def host_steps(k):
+        for _ in range(k):
+            rc = fm.solve(phi_h, src_h, flow_h, mu=mu_h)
+            if rc != 0:
+                raise RuntimeError(f"fts_solve failed ({rc}): {fm.last_error()}")
+        return None
+
+    host_steps(1)
+    _, ms_e, wall_e, _ = timed(host_steps, args.steps)
+    e2e = ws * args.steps / (ms_e / 1e3)
+    rel_mixed = float(fm.last_stats["rel_residual"])
+    flow_mixed = flow_h.copy()
+
+    # ---- plain FP64 on the same workload -------------------------------------
+    f64 = make("fp64")
+    device_steps(f64, 1)
+    k64 = max(1, args.steps_fp64)
+    stats_d, ms_d, _, _ = timed(lambda k: device_steps(f64, k), k64)
+    value_fp64 = ws * k64 / (ms_d / 1e3)
+    flow64 = flow_d.cpu().numpy()
+    vel_err = float(np.linalg.norm(flow_mixed[:3 * npn] - flow64[:3 * npn]) /
+                    np.linalg.norm(flow64[:3 * npn]))
+    p_err = float(np.linalg.norm(flow_mixed[3 * npn:] - flow64[3 * npn:]) /
+                  np.linalg.norm(flow64[3 * npn:]))
+
+    # ---- roofline of the dominant kernel (live CUDA-event timing) -----------
+    spmv_ms = sum(s["ms_spmv"] for s in stats_m)
+    spmv_n = sum(s["spmv_launches"] for s in stats_m)
+    per = spmv_ms / max(spmv_n, 1)
+    bytes_per = stats_m[0]["spmv_bytes"]
+    achieved = bytes_per / (per / 1e3) / 1e9 if spmv_n else None
+    peak, peak_kind = _peaks()
+    spmv64_ms = sum(s["ms_spmv"] for s in stats_d)
+    spmv64_n = sum(s["spmv_launches"] for s in stats_d)
+    ach64 = (stats_d[0]["spmv_bytes"] / (spmv64_ms / spmv64_n / 1e3) / 1e9) if spmv64_n else None
+
+    launches = int(sum(s["kernel_launches"] for s in stats_m))
+    it_m = statistics.mean(s["iterations"] for s in stats_m)
+    it_d = statistics.mean(s["iterations"] for s in stats_d)
+    dofs = 4 * npn
+
+    res = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_m / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
+        "data": "synthetic (seeded Kuhn lattice, analytic level set, Gaussian growth factor)",
+        "config": {"workload": f"{args.workload}: {npn} nodes, {nt} tets, "
+                               f"{dofs} block DOF, tol {par['Stokes tolerance']}",
+                   "precision": "mixed", "preconditioner": args.preconditioner,
+                   "l2": "inputs larger than L2 (operator > 1 GB streamed every iteration)",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "e2e": {"value": round(e2e, 4), "unit": UNIT,
+                "h2d_bytes_per_step": int(phi_h.nbytes + src_h.nbytes + mu_h.nbytes),
+                "d2h_bytes_per_step": int(flow_h.nbytes)},
+        "fp64": {"value": round(value_fp64, 4), "unit": UNIT,
+                 "ms_per_step": round(ms_d / k64, 3), "iterations": it_d,
+                 "spmv_gbs": round(ach64, 1) if ach64 else None},
+        "mixed_vs_fp64": round(value / value_fp64, 3),
+        "mixed": {"iterations": it_m, "iterations_fp32": statistics.mean(
+            s["iterations_fp32"] for s in stats_m),
+                  "outer": statistics.mean(s["outer_iterations"] for s in stats_m),
+                  "rel_residual": rel_mixed, "vel_err_vs_fp64": vel_err,
+                  "p_err_vs_fp64": p_err},
+        "dof_iterations_per_s": round(value * it_m * dofs, 1),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
+                     "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4) if achieved else None,
+                     "traffic": _traffic("k_minres_A<float>"),
+                     "kernel": "k_minres_A<float> (FP32 BSR SpMV + MINRES dots)",
+                     "bytes_per_launch": bytes_per, "ms_per_launch": round(per, 5),
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "ms_assembly": round(statistics.mean(s["ms_assembly"] for s in stats_m), 3),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_baseline(inst, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(res), flush=True)
+    fm.close()
+    f64.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(inst, seconds: float) -> dict:
+    """The oracle (restated reference: row-gather assembly + un-preconditioned
+    BiCGSTAB, OpenMP) on this host's cores, bounded to ~``seconds``: full
+    assembly plus as many BiCGSTAB iterations as fit; solves/s extrapolated
+    with the reference algorithm's iteration count to 1e-8 on this workload."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    threads = O.num_threads()
+    t0 = time.perf_counter()
+    R, _, _, _ = O.system(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source, inst.mu,
+                          inst.params)
+    t_asm = time.perf_counter() - t0
+    it = 8
+    t_it = None
+    while True:
+        t1 = time.perf_counter()
+        O.bicgstab(R, None, tol=1e-30, maxit=it)
+        t_run = time.perf_counter() - t1
+        t_it = t_run / it
+        if t_asm + t_run > seconds * 0.5 or it >= 4096:
+            break
+        it *= 2
+    n_ref = REFERENCE_ITERATIONS.get(inst.name)
+    value = 1.0 / (t_asm + n_ref * t_it) if n_ref else None
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"oracle on {inst.name}: full assembly ({t_asm:.2f} s) + {it} BiCGSTAB "
+                       f"iterations ({t_it * 1e3:.1f} ms each); solves/s = 1/(t_asm + "
+                       f"N_ref t_iter) with N_ref = {n_ref} (reference BiCGSTAB iterations "
+                       f"to the tolerance, profiles/reference_iterations.md)"),
+            "t_assembly_s": t_asm, "t_iteration_s": t_it}
+
+
+# Iterations the reference's un-preconditioned BiCGSTAB needs to reach the
+# workload tolerance (measured with the GPU implementation of that algorithm;
+# see profiles/reference_iterations.md).  None = not yet measured.
+REFERENCE_ITERATIONS: dict = {}
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    from fluidtissue_gb300 import workloads as W
+    inst = W.WORKLOADS[args.workload]()
+    vals = []
+    cb = None
+    for _ in range(args.warmup + args.steps):
+        cb = cpu_baseline(inst, args.cpu_seconds / max(1, args.steps + args.warmup))
+        vals.append(cb["value"])
+    v = vals[-1]
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+           "config": {"workload": inst.name}, "cpu_baseline": cb,
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps-fp64", type=int, default=2)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ellipsoid129")
+    ap.add_argument("--preconditioner", default="auto", choices=["auto", "jacobi", "multigrid"])
+    ap.add_argument("--inner-tol", type=float, default=0.0)
+    ap.add_argument("--cpu-seconds", type=float, default=30.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

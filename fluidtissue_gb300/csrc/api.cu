@@ -22,9 +22,11 @@ static void free_all(Ctx& c) {
                     c.b, c.x, c.r, c.w64.q, c.w64.R[0], c.w64.R[1], c.w64.Y[0], c.w64.Y[1],
                     c.w64.W[0], c.w64.W[1], c.w64.X, c.w32.q, c.w32.R[0], c.w32.R[1],
                     c.w32.Y[0], c.w32.Y[1], c.w32.W[0], c.w32.W[1], c.w32.X, c.w32.r0, c.ms,
-                    c.os, c.red.partials, c.red.ticket, c.err_flag};
+                    c.os, c.red.partials, c.red.ticket, c.err_flag, c.bicg};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    mg_free(c.mg64);
+    mg_free(c.mg32);
     if (c.ms_host) cudaFreeHost(c.ms_host);
     if (c.os_host) cudaFreeHost(c.os_host);
     for (auto& e : c.ev)
@@ -65,8 +67,12 @@ static int validate_params(const fts_params& p, std::string& err) {
         err = "unknown precision";
         return FTS_ERR_BAD_INPUT;
     }
-    if (p.solver != FTS_SOLVER_MINRES) {
-        err = "only the MINRES solver is built";
+    if (p.solver != FTS_SOLVER_MINRES && p.solver != FTS_SOLVER_BICGSTAB) {
+        err = "unknown solver";
+        return FTS_ERR_BAD_INPUT;
+    }
+    if (p.solver == FTS_SOLVER_BICGSTAB && p.precision != FTS_PREC_FP64) {
+        err = "the reference's BiCGSTAB runs in FP64 only";
         return FTS_ERR_UNSUPPORTED;
     }
     if (!(p.alpha >= 0.0) || !(p.eps >= 0.0)) {
@@ -74,6 +80,28 @@ static int validate_params(const fts_params& p, std::string& err) {
         return FTS_ERR_BAD_INPUT;
     }
     return FTS_OK;
+}
+
+// Multigrid needs the Kuhn lattice structure and at least three levels
+// (odd n >= 9); otherwise node 3x3 block Jacobi.
+static int mg_levels(int n) {
+    int l = 1;
+    while (n % 2 == 1 && n >= 5) {
+        n = (n + 1) / 2;
+        ++l;
+    }
+    return l;
+}
+
+static void configure_preconditioner(Ctx& c) {
+    const int n = c.topo.lattice_n;
+    const bool mg_ok = n > 0 && n % 2 == 1 && mg_levels(n) >= 3;
+    if (c.par.preconditioner == FTS_PC_MULTIGRID && !mg_ok) {
+        c.last_error = "multigrid needs a Kuhn lattice mesh with odd n >= 9";
+        throw (int)FTS_ERR_UNSUPPORTED;
+    }
+    c.use_mg = mg_ok && c.par.preconditioner != FTS_PC_JACOBI;
+    c.crank = (c.par.eps > 0.0 && c.volume > 0.0) ? 1.0 / (c.par.eps * c.volume) : 0.0;
 }
 
 static void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
@@ -138,6 +166,26 @@ static void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
     FTS_CUDA(cudaMemcpyAsync(c.p2t, T.p2t.data(), 4 * c.nt * sizeof(uint32_t),
                              cudaMemcpyHostToDevice, c.stream));
     if (p.precision == FTS_PREC_MIXED) ensure_fp32(c);
+    // total volume (for the rank-one constant-pressure term of the preconditioner)
+    double vol = 0.0;
+#pragma omp parallel for reduction(+ : vol) schedule(static)
+    for (int64_t k = 0; k < c.nt; ++k) {
+        const int32_t* t = m.tets + 4 * k;
+        double q[4][3];
+        for (int j = 0; j < 4; ++j)
+            for (int a = 0; a < 3; ++a) q[j][a] = (double)m.xyz[3 * (int64_t)t[j] + a];
+        double u[3], v[3], w[3];
+        for (int a = 0; a < 3; ++a) {
+            u[a] = q[1][a] - q[0][a];
+            v[a] = q[2][a] - q[0][a];
+            w[a] = q[3][a] - q[0][a];
+        }
+        double det = u[0] * (v[1] * w[2] - v[2] * w[1]) - u[1] * (v[0] * w[2] - v[2] * w[0]) +
+                     u[2] * (v[0] * w[1] - v[1] * w[0]);
+        vol += std::fabs(det) / 6.0;
+    }
+    c.volume = vol;
+    configure_preconditioner(c);
     launch_geometry(c, c.err_flag);
     int bad = 0;
     FTS_CUDA(cudaMemcpyAsync(&bad, c.err_flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
@@ -195,6 +243,9 @@ static int solve_device(Ctx& c, bool have_mu, bool have_force, double* flow_out,
     if (P.precision == FTS_PREC_MIXED) {
         ensure_fp32(c);
         launch_to_f32(c);
+        setup_preconditioner<float>(c);
+    } else {
+        setup_preconditioner<double>(c);
     }
     FTS_CUDA(cudaEventRecord(c.ev[1], c.stream));
     int bad = 0;
@@ -221,6 +272,32 @@ static int solve_device(Ctx& c, bool have_mu, bool have_force, double* flow_out,
     const long long N = 3 * c.topo.n_interior + c.np;
     const long long maxit = P.max_iter > 0 ? P.max_iter : 2 * N;
     FTS_CUDA(cudaEventRecord(c.ev[2], c.stream));
+    if (P.solver == FTS_SOLVER_BICGSTAB) {
+        // the reference's algorithm: stop on the updated residual (Flow.cpp:266-285)
+        double err = 0.0;
+        int bst = 0;
+        long long it = bicgstab_solve(c, tol, maxit, &err, &bst);
+        launch_residual64(c);
+        read_outer(c);
+        FTS_CUDA(cudaEventRecord(c.ev[3], c.stream));
+        FTS_CUDA(cudaEventSynchronize(c.ev[3]));
+        st.ms_solve = elapsed(c.ev[2], c.ev[3]);
+        st.iterations = it;
+        st.outer_iterations = 1;
+        st.rel_residual = std::sqrt(c.os_host->rr) / bnorm;
+        st.error_estimate = err;
+        if (bst == 2 || c.os_host->nonfinite) {
+            c.last_error = "non-finite value in BiCGSTAB";
+            return FTS_ERR_NAN;
+        }
+        if (!(err <= tol)) {
+            c.last_error = "BiCGSTAB stopped above the tolerance";
+            return FTS_ERR_NOT_CONVERGED;
+        }
+        launch_scatter_flow(c, flow_out);
+        st.solved = 1;
+        return FTS_OK;
+    }
     double rel = std::sqrt(c.os_host->rr) / bnorm;
     long long iters = 0, iters32 = 0;
     int outer = 0;
@@ -471,7 +548,15 @@ int fts_update_params(fts_ctx* ctx, const fts_params* params) {
         ctx->c.last_error = "the device of a context cannot change";
         return FTS_ERR_BAD_INPUT;
     }
+    const fts_params old = ctx->c.par;
     ctx->c.par = *params;
+    try {
+        configure_preconditioner(ctx->c);
+    } catch (int code) {
+        ctx->c.par = old;
+        configure_preconditioner(ctx->c);
+        return code;
+    }
     return FTS_OK;
 }
 

@@ -8,6 +8,7 @@
 
 #include "fts.h"
 #include "fts_internal.h"
+#include "mg.cuh"
 
 namespace fts {
 
@@ -55,6 +56,11 @@ struct alignas(128) ElemGeom {
 struct MinresScalars {
     double beta1, beta, oldb, alfa, dbar, epsln, oldeps, delta, gamma, phi, phibar, cs, sn;
     double target;
+    double rtol;      // requested reduction of the preconditioned residual norm
+    double crank;    // rank-one constant-pressure weight 1/(eps * volume)
+    double ycorr[2]; // pressure shift of Y[0] / Y[1] (rank-one part of P^-1)
+    double psum;     // sum of the pressure components of the Lanczos vector
+    double pdot;     // its pressure part of n . P^-1 n (diagonal term)
     long long iters;
     long long maxit;
     int stop;
@@ -138,6 +144,15 @@ struct Ctx {
     OuterScalars* os_host = nullptr;    // pinned
     Reduction red{};
     int* err_flag = nullptr;
+    double* bicg = nullptr;              // scalars of the reference-algorithm BiCGSTAB
+    int bicg_restarts = 0;
+
+    // preconditioner
+    bool use_mg = false;
+    MG<double> mg64;
+    MG<float> mg32;
+    double volume = 0.0;  // sum of element volumes
+    double crank = 0.0;   // 1 / (eps * volume), 0 when eps = 0
 
     // learned ratio between true and preconditioned residual reductions
     double pc_ratio64 = 10.0;
@@ -180,6 +195,10 @@ void launch_prepare_inner32(Ctx& c);       // r0_32 = r * scale
 void launch_update_x64(Ctx& c);            // x += d (FP64 inner)
 void launch_update_x_from32(Ctx& c);       // x += d32 / scale
 void launch_apply(Ctx& c, int precision, const V4<double>* in, V4<double>* out);
+// the reference's un-preconditioned BiCGSTAB on c.x (bicgstab.cu)
+long long bicgstab_solve(Ctx& c, double tol, long long maxit, double* err, int* status);
+template <typename T>
+void setup_preconditioner(Ctx& c);   // multigrid hierarchy when c.use_mg
 
 template <typename T>
 inline T* dev_alloc(Ctx& c, size_t n) {

@@ -16,14 +16,10 @@
 #include <cmath>
 
 #include "fts_device.cuh"
+#include "mg.cuh"
 #include "reduce.cuh"
 
 namespace fts {
-
-template <typename T>
-__device__ __forceinline__ V4<T> ld4(const V4<T>* p) {
-    return *p;
-}
 
 template <typename T>
 __device__ __forceinline__ T bsr_row_dot(const T* __restrict__ A, const int32_t* __restrict__ cols,
@@ -40,11 +36,6 @@ __device__ __forceinline__ T bsr_row_dot(const T* __restrict__ A, const int32_t*
         acc = fma(a.w, xj.w, acc);
     }
     return acc;
-}
-
-template <typename T>
-__device__ __forceinline__ T comp(const V4<T>& v, int r) {
-    return r == 0 ? v.x : (r == 1 ? v.y : (r == 2 ? v.z : v.w));
 }
 
 // ---------------------------------------------------------------------------
@@ -125,39 +116,45 @@ void launch_residual64(Ctx& c) {
 
 // ---------------------------------------------------------------------------
 // MINRES kernels
+//
+// Preconditioner P (SPD, block diagonal): velocity block = node 3x3 block
+// Jacobi or one multigrid V-cycle (mg.cu); pressure block = diag(alpha D +
+// eps M + lumped mass/mu)^-1 plus the rank-one term crank * 1 1^T with
+// crank = 1/(eps * volume), which lifts the constant pressure mode (eigenvalue
+// ~eps of the Schur complement) to ~1.  The rank-one part of y = P^-1 r is kept
+// as a scalar ycorr[buffer] added to the pressure component wherever y is
+// read, so applying P needs no extra pass over memory.
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ __forceinline__ V4<T> apply_pc(const T* __restrict__ pc, int64_t i, const V4<T>& v) {
+__device__ __forceinline__ void pc_jacobi(const T* __restrict__ pc, int64_t i, const V4<T>& v,
+                                          V4<T>& z) {
     const V4<T> p0 = *reinterpret_cast<const V4<T>*>(pc + 8 * i);
     const V4<T> p1 = *reinterpret_cast<const V4<T>*>(pc + 8 * i + 4);
-    V4<T> z;
     z.x = p0.x * v.x + p0.y * v.y + p0.z * v.z;
     z.y = p0.y * v.x + p0.w * v.y + p1.x * v.z;
     z.z = p0.z * v.x + p1.x * v.y + p1.y * v.z;
     z.w = p1.z * v.w;
-    return z;
 }
 
-// r0 -> R2 (= R[0]), y = P^-1 r0 -> Y[0], beta1 = sqrt(r0 . y).
-template <typename T>
-__global__ void k_minres_init(int64_t np, const V4<T>* __restrict__ r0, const T* __restrict__ pc,
-                              V4<T>* __restrict__ R2, V4<T>* __restrict__ Y, double rtol,
-                              long long maxit, Reduction red, MinresScalars* s) {
-    double acc[1] = {0.0};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        V4<T> v = r0[i];
-        R2[i] = v;
-        V4<T> z = apply_pc<T>(pc, i, v);
-        Y[i] = z;
-        acc[0] += (double)(v.x * z.x) + (double)(v.y * z.y) + (double)(v.z * z.z) +
-                  (double)(v.w * z.w);
-    }
-    double tot[1];
-    if (grid_sum<1>(acc, red, tot) && threadIdx.x == 0) {
-        double b1 = tot[0] > 0.0 ? sqrt(tot[0]) : 0.0;
-        s->beta1 = b1;
-        s->beta = b1;
+__global__ void k_minres_reset(MinresScalars* s, double rtol, long long maxit, double crank) {
+    s->rtol = rtol;
+    s->maxit = maxit;
+    s->crank = crank;
+    s->iters = 0;
+    s->stop = 0;
+    s->c_pending = 0;
+    s->status = 0;
+    s->ycorr[0] = s->ycorr[1] = 0.0;
+}
+
+// beta^2 of a new Lanczos vector is known: initialise (init) or run the
+// Givens step of the QR factorisation and the convergence test.
+__device__ void finalize_beta(MinresScalars* s, double beta2, bool init) {
+    const bool finite = isfinite(beta2);
+    const double beta = beta2 > 0.0 ? sqrt(beta2) : 0.0;
+    if (init) {
+        s->beta1 = beta;
+        s->beta = beta;
         s->oldb = 0.0;
         s->alfa = 0.0;
         s->dbar = 0.0;
@@ -166,111 +163,176 @@ __global__ void k_minres_init(int64_t np, const V4<T>* __restrict__ r0, const T*
         s->delta = 0.0;
         s->gamma = 1.0;
         s->phi = 0.0;
-        s->phibar = b1;
+        s->phibar = beta;
         s->cs = -1.0;
         s->sn = 0.0;
-        s->target = rtol * b1;
-        s->iters = 0;
-        s->maxit = maxit;
-        s->c_pending = 0;
-        s->status = isfinite(tot[0]) ? 0 : 2;
-        s->stop = (!(b1 > 0.0) || !isfinite(tot[0])) ? 1 : 0;
+        s->target = s->rtol * beta;
+        s->status = finite ? 0 : 2;
+        s->stop = (!(beta > 0.0) || !finite) ? 1 : 0;
+        return;
+    }
+    const double alfa = s->alfa;
+    s->oldb = s->beta;
+    s->beta = beta;
+    s->oldeps = s->epsln;
+    const double delta = s->cs * s->dbar + s->sn * alfa;
+    const double gbar = s->sn * s->dbar - s->cs * alfa;
+    s->epsln = s->sn * beta;
+    s->dbar = -s->cs * beta;
+    double gamma = sqrt(gbar * gbar + beta * beta);
+    if (gamma < DBL_MIN) gamma = DBL_MIN;
+    s->delta = delta;
+    s->gamma = gamma;
+    s->cs = gbar / gamma;
+    s->sn = beta / gamma;
+    s->phi = s->cs * s->phibar;
+    s->phibar = s->sn * s->phibar;
+    s->iters += 1;
+    s->c_pending = 1;
+    if (!finite || !isfinite(s->phibar)) {
+        s->status = 2;
+        s->stop = 1;
+    } else if (s->phibar <= s->target || !(beta > 0.0)) {
+        s->stop = 1;
+    } else if (s->iters >= s->maxit) {
+        s->status = 1;
+        s->stop = 1;
     }
 }
 
-// A: q = S (y / beta); partial dots v.q and v.r1.
+// A: q = S v with v = (y + ycorr e_p) / beta; partial dots v.q and v.r1.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 k_minres_A(int64_t np, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ cols,
-           const T* __restrict__ A, const V4<T>* __restrict__ Y, const V4<T>* __restrict__ R1,
-           T* __restrict__ q, Reduction red, MinresScalars* s) {
+           const T* __restrict__ A, const V4<T>* __restrict__ Y, int ybuf,
+           const V4<T>* __restrict__ R1, T* __restrict__ q, Reduction red, MinresScalars* s) {
     if (s->stop) return;
     const double invb = 1.0 / s->beta;
     const T tinv = (T)invb;
+    const T wadd = (T)s->ycorr[ybuf];
     const int r = threadIdx.x & 3;
     double acc[2] = {0.0, 0.0};
     const T* y = reinterpret_cast<const T*>(Y);
     const T* r1 = reinterpret_cast<const T*>(R1);
     for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 2; row < np;
          row += ((int64_t)gridDim.x * blockDim.x) >> 2) {
-        T ax = bsr_row_dot<T>(A, cols, rowptr[row], rowptr[row + 1], r, Y);
-        T qv = ax * tinv;
+        T ax = T(0);
+        const int32_t k1 = rowptr[row + 1];
+        for (int32_t k = rowptr[row]; k < k1; ++k) {
+            const int32_t j = __ldg(cols + k);
+            const V4<T> a = *reinterpret_cast<const V4<T>*>(A + (int64_t)k * 16 + r * 4);
+            const V4<T> xj = Y[j];
+            ax = fma(a.x, xj.x, ax);
+            ax = fma(a.y, xj.y, ax);
+            ax = fma(a.z, xj.z, ax);
+            ax = fma(a.w, xj.w + wadd, ax);
+        }
+        const T qv = ax * tinv;
         const int64_t e = row * 4 + r;
         q[e] = qv;
-        T ve = y[e] * tinv;
+        const T ve = (y[e] + (r == 3 ? wadd : T(0))) * tinv;
         acc[0] += (double)(ve * qv);
         acc[1] += (double)(ve * r1[e]);
     }
     double tot[2];
     if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
-        double c1 = s->iters >= 1 ? s->beta / s->oldb : 0.0;
+        const double c1 = s->iters >= 1 ? s->beta / s->oldb : 0.0;
         s->alfa = tot[0] - c1 * tot[1];
     }
 }
 
-// B: r_new = q - c1 r1 - c2 r2 (into R1's buffer), y_new = P^-1 r_new, beta.
+// Preconditioner stage 1.
+//   init: n = r0 (written to Rn)      else: n = q - c1 R1 - c2 R2 (written to Rn = R1)
+//   y.w = ip * n.w;  Jacobi: y.xyz = D3^-1 n.xyz;  multigrid: b0 = n.xyz (SoA)
+// Jacobi finishes beta here; multigrid leaves sum(n.w) and n.w y.w for stage 2.
+template <typename T, bool MGV>
+__global__ void __launch_bounds__(kThreads)
+k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
+             const V4<T>* __restrict__ R2, V4<T>* Rn, const T* __restrict__ pc,
+             V4<T>* __restrict__ Ynew, int ybuf, T* __restrict__ b0, Reduction red,
+             MinresScalars* s) {
+    if (s->stop) return;
+    T c1 = T(0), c2 = T(0);
+    if (!init) {
+        c1 = (T)(s->iters >= 1 ? s->beta / s->oldb : 0.0);
+        c2 = (T)(s->alfa / s->beta);
+    }
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        V4<T> n;
+        if (init) {
+            n = R1[i];  // r0
+        } else {
+            const V4<T> qv = q[i], a = R1[i], b2 = R2[i];
+            n.x = qv.x - c1 * a.x - c2 * b2.x;
+            n.y = qv.y - c1 * a.y - c2 * b2.y;
+            n.z = qv.z - c1 * a.z - c2 * b2.z;
+            n.w = qv.w - c1 * a.w - c2 * b2.w;
+        }
+        Rn[i] = n;
+        V4<T> z;
+        if (MGV) {
+            z.x = z.y = z.z = T(0);
+            z.w = pc[8 * i + 6] * n.w;
+            b0[i] = n.x;
+            b0[np + i] = n.y;
+            b0[2 * np + i] = n.z;
+        } else {
+            pc_jacobi<T>(pc, i, n, z);
+            acc[2] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z);
+        }
+        Ynew[i] = z;
+        acc[0] += (double)n.w;
+        acc[1] += (double)(n.w * z.w);
+    }
+    double tot[3];
+    if (grid_sum<3>(acc, red, tot) && threadIdx.x == 0) {
+        if (MGV) {
+            s->psum = tot[0];
+            s->pdot = tot[1];
+        } else {
+            const double cr = s->crank;
+            s->ycorr[ybuf] = cr * tot[0];
+            finalize_beta(s, tot[2] + tot[1] + cr * tot[0] * tot[0], init != 0);
+        }
+    }
+}
+
+// Multigrid stage 2: y.xyz = V-cycle output x0 (SoA); beta.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_minres_B(int64_t np, const V4<T>* __restrict__ q, V4<T>* R1, const V4<T>* __restrict__ R2,
-           const T* __restrict__ pc, V4<T>* __restrict__ Ynew, Reduction red, MinresScalars* s) {
+k_minres_pc2(int64_t np, int init, const V4<T>* __restrict__ Rn, const T* __restrict__ x0,
+             V4<T>* __restrict__ Ynew, int ybuf, Reduction red, MinresScalars* s) {
     if (s->stop) return;
-    const T c1 = (T)(s->iters >= 1 ? s->beta / s->oldb : 0.0);
-    const T c2 = (T)(s->alfa / s->beta);
     double acc[1] = {0.0};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
          i += (int64_t)gridDim.x * blockDim.x) {
-        const V4<T> qv = q[i], a = R1[i], b2 = R2[i];
-        V4<T> n;
-        n.x = qv.x - c1 * a.x - c2 * b2.x;
-        n.y = qv.y - c1 * a.y - c2 * b2.y;
-        n.z = qv.z - c1 * a.z - c2 * b2.z;
-        n.w = qv.w - c1 * a.w - c2 * b2.w;
-        R1[i] = n;
-        const V4<T> z = apply_pc<T>(pc, i, n);
+        const V4<T> n = Rn[i];
+        V4<T> z = Ynew[i];
+        z.x = x0[i];
+        z.y = x0[np + i];
+        z.z = x0[2 * np + i];
         Ynew[i] = z;
-        acc[0] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z) +
-                  (double)(n.w * z.w);
+        acc[0] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z);
     }
     double tot[1];
     if (grid_sum<1>(acc, red, tot) && threadIdx.x == 0) {
-        const double alfa = s->alfa;
-        s->oldb = s->beta;
-        const double beta = tot[0] > 0.0 ? sqrt(tot[0]) : 0.0;
-        s->beta = beta;
-        s->oldeps = s->epsln;
-        const double delta = s->cs * s->dbar + s->sn * alfa;
-        const double gbar = s->sn * s->dbar - s->cs * alfa;
-        s->epsln = s->sn * beta;
-        s->dbar = -s->cs * beta;
-        double gamma = sqrt(gbar * gbar + beta * beta);
-        if (gamma < DBL_MIN) gamma = DBL_MIN;
-        s->delta = delta;
-        s->gamma = gamma;
-        s->cs = gbar / gamma;
-        s->sn = beta / gamma;
-        s->phi = s->cs * s->phibar;
-        s->phibar = s->sn * s->phibar;
-        s->iters += 1;
-        s->c_pending = 1;
-        if (!isfinite(tot[0]) || !isfinite(s->phibar)) {
-            s->status = 2;
-            s->stop = 1;
-        } else if (s->phibar <= s->target || !(beta > 0.0)) {
-            s->stop = 1;
-        } else if (s->iters >= s->maxit) {
-            s->status = 1;
-            s->stop = 1;
-        }
+        const double cr = s->crank;
+        s->ycorr[ybuf] = cr * s->psum;
+        finalize_beta(s, tot[0] + s->pdot + cr * s->psum * s->psum, init != 0);
     }
 }
 
 // C: w_new = (v - oldeps w_prev - delta w_cur) / gamma (into w_prev), x += phi w_new.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_minres_C(int64_t np, const V4<T>* __restrict__ Yk, V4<T>* Wprev, const V4<T>* __restrict__ Wcur,
-           V4<T>* __restrict__ X, Reduction red, MinresScalars* s) {
+k_minres_C(int64_t np, const V4<T>* __restrict__ Yk, int ybuf, V4<T>* Wprev,
+           const V4<T>* __restrict__ Wcur, V4<T>* __restrict__ X, Reduction red,
+           MinresScalars* s) {
     if (!s->c_pending) return;
     const T inv = (T)(1.0 / s->oldb);
+    const T wadd = (T)s->ycorr[ybuf];
     const T oe = (T)s->oldeps, de = (T)s->delta, ig = (T)(1.0 / s->gamma), ph = (T)s->phi;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -279,7 +341,7 @@ k_minres_C(int64_t np, const V4<T>* __restrict__ Yk, V4<T>* Wprev, const V4<T>* 
         w.x = (y.x * inv - oe * wp.x - de * wc.x) * ig;
         w.y = (y.y * inv - oe * wp.y - de * wc.y) * ig;
         w.z = (y.z * inv - oe * wp.z - de * wc.z) * ig;
-        w.w = (y.w * inv - oe * wp.w - de * wc.w) * ig;
+        w.w = ((y.w + wadd) * inv - oe * wp.w - de * wc.w) * ig;
         Wprev[i] = w;
         xv.x += ph * w.x;
         xv.y += ph * w.y;
@@ -308,6 +370,35 @@ template <>
 KrylovWork<double>& work_of<double>(Ctx& c) { return c.w64; }
 template <>
 KrylovWork<float>& work_of<float>(Ctx& c) { return c.w32; }
+template <typename T>
+static MG<T>& mg_of(Ctx& c);
+template <>
+MG<double>& mg_of<double>(Ctx& c) { return c.mg64; }
+template <>
+MG<float>& mg_of<float>(Ctx& c) { return c.mg32; }
+
+// y = P^-1 n for the Lanczos vector in Rn (stage 1, V-cycle, stage 2).
+template <typename T>
+static void launch_pc(Ctx& c, bool use_mg, int init, const V4<T>* q, V4<T>* R1, const V4<T>* R2,
+                      V4<T>* Rn, V4<T>* Ynew, int ybuf) {
+    KrylovWork<T>& w = work_of<T>(c);
+    const int gn = grid_for(c, c.np);
+    const T* pc = pc_of<T>(c);
+    if (use_mg) {
+        MG<T>& mg = mg_of<T>(c);
+        k_minres_pc1<T, true><<<gn, kThreads, 0, c.stream>>>(c.np, init, q, R1, R2, Rn, pc, Ynew,
+                                                             ybuf, mg.L[0].b, c.red, c.ms);
+        mg_vcycle<T>(c, mg, &c.ms->stop);
+        k_minres_pc2<T><<<gn, kThreads, 0, c.stream>>>(c.np, init, Rn, mg.L[0].x, Ynew, ybuf,
+                                                       c.red, c.ms);
+        c.launches += 2;
+    } else {
+        k_minres_pc1<T, false><<<gn, kThreads, 0, c.stream>>>(c.np, init, q, R1, R2, Rn, pc, Ynew,
+                                                              ybuf, nullptr, c.red, c.ms);
+        c.launches += 1;
+    }
+    (void)w;
+}
 
 // Runs MINRES on S d = r0 (work.r0; for FP64 the outer residual c.r) from
 // d = 0 until the preconditioned residual norm drops by rtol.  Returns the
@@ -316,25 +407,25 @@ template <typename T>
 long long minres_inner(Ctx& c, double rtol, long long maxit, double* achieved, int* status) {
     KrylovWork<T>& w = work_of<T>(c);
     const T* A = op_of<T>(c);
-    const T* pc = pc_of<T>(c);
     const int64_t np = c.np;
-    const V4<T>* r0 = w.r0;
+    const bool use_mg = c.use_mg;
     FTS_CUDA(cudaMemsetAsync(w.W[0], 0, np * sizeof(V4<T>), c.stream));
     FTS_CUDA(cudaMemsetAsync(w.W[1], 0, np * sizeof(V4<T>), c.stream));
     FTS_CUDA(cudaMemsetAsync(w.X, 0, np * sizeof(V4<T>), c.stream));
     FTS_CUDA(cudaMemsetAsync(w.R[1], 0, np * sizeof(V4<T>), c.stream));
-    const int gn = grid_for(c, np);
     const int ge = grid_for(c, np * 4);
-    k_minres_init<T><<<gn, kThreads, 0, c.stream>>>(np, r0, pc, w.R[0], w.Y[0], rtol, maxit,
-                                                    c.red, c.ms);
-    FTS_CUDA(cudaGetLastError());
+    const int gn = grid_for(c, np);
+    k_minres_reset<<<1, 1, 0, c.stream>>>(c.ms, rtol, maxit, c.crank);
     c.launches += 1;
+    // initial Lanczos vector r0 -> R[0], y = P^-1 r0 -> Y[0]
+    launch_pc<T>(c, use_mg, 1, nullptr, const_cast<V4<T>*>(w.r0), nullptr, w.R[0], w.Y[0], 0);
+    FTS_CUDA(cudaGetLastError());
     const bool timed = c.par.time_kernels != 0;
     if (timed && !c.tev_ready) {
         for (auto& e : c.tev) FTS_CUDA(cudaEventCreate(&e));
         c.tev_ready = true;
     }
-    const int poll = np > 200000 ? 8 : 32;  // <= Ctx::kTimedPairs
+    const int poll = use_mg ? (np > 200000 ? 4 : 16) : (np > 200000 ? 8 : 32);
     long long k = 0, done_before = 0;
     for (;;) {
         for (int u = 0; u < poll; ++u) {
@@ -342,18 +433,18 @@ long long minres_inner(Ctx& c, double rtol, long long maxit, double* achieved, i
             const int p = (int)(k & 1);       // r1 = R[p], r2 = R[1-p], new -> R[p]
             V4<T>* R1 = w.R[p];
             V4<T>* R2 = w.R[1 - p];
-            V4<T>* Yk = w.Y[(k - 1) & 1];
-            V4<T>* Yn = w.Y[k & 1];
+            const int yk = (int)((k - 1) & 1), yn = (int)(k & 1);
             V4<T>* Wprev = w.W[p];
             V4<T>* Wcur = w.W[1 - p];
             if (timed) FTS_CUDA(cudaEventRecord(c.tev[2 * u], c.stream));
-            k_minres_A<T><<<ge, kThreads, 0, c.stream>>>(np, c.rowptr, c.cols, A, Yk, R1,
+            k_minres_A<T><<<ge, kThreads, 0, c.stream>>>(np, c.rowptr, c.cols, A, w.Y[yk], yk, R1,
                                                          reinterpret_cast<T*>(w.q), c.red, c.ms);
             if (timed) FTS_CUDA(cudaEventRecord(c.tev[2 * u + 1], c.stream));
-            k_minres_B<T><<<gn, kThreads, 0, c.stream>>>(np, w.q, R1, R2, pc, Yn, c.red, c.ms);
-            k_minres_C<T><<<gn, kThreads, 0, c.stream>>>(np, Yk, Wprev, Wcur, w.X, c.red, c.ms);
+            launch_pc<T>(c, use_mg, 0, w.q, R1, R2, R1, w.Y[yn], yn);
+            k_minres_C<T><<<gn, kThreads, 0, c.stream>>>(np, w.Y[yk], yk, Wprev, Wcur, w.X, c.red,
+                                                         c.ms);
+            c.launches += 2;
         }
-        c.launches += 3 * poll;
         FTS_CUDA(cudaGetLastError());
         FTS_CUDA(cudaMemcpyAsync(c.ms_host, c.ms, sizeof(MinresScalars), cudaMemcpyDeviceToHost,
                                  c.stream));
@@ -379,6 +470,13 @@ long long minres_inner(Ctx& c, double rtol, long long maxit, double* achieved, i
 
 template long long minres_inner<double>(Ctx&, double, long long, double*, int*);
 template long long minres_inner<float>(Ctx&, double, long long, double*, int*);
+
+template <typename T>
+void setup_preconditioner(Ctx& c) {
+    if (c.use_mg) mg_setup<T>(c, mg_of<T>(c));
+}
+template void setup_preconditioner<double>(Ctx&);
+template void setup_preconditioner<float>(Ctx&);
 
 // r0_32 = r * (1/||r||) (FP32 right-hand side of the inner solve).
 __global__ void k_prepare_inner32(int64_t n, const double* __restrict__ r,

@@ -23,6 +23,7 @@ from . import _native as N
 
 PREC = {"fp64": A.PREC_FP64, "mixed": A.PREC_MIXED}
 PC = {"auto": A.PC_AUTO, "jacobi": A.PC_JACOBI, "multigrid": A.PC_MULTIGRID}
+SOLVER = {"minres": A.SOLVER_MINRES, "bicgstab": A.SOLVER_BICGSTAB}
 OP = {"auto": A.OP_AUTO, "assembled": A.OP_ASSEMBLED, "matfree": A.OP_MATFREE}
 
 
@@ -56,7 +57,8 @@ def _par(par: dict, key: str) -> float:
 
 
 def make_params(par: dict, precision="fp64", preconditioner="auto", operator="auto",
-                warm_start=True, device=0, inner_tol=0.0, verbose=False) -> A.FtsParams:
+                warm_start=True, device=0, inner_tol=0.0, verbose=False,
+                time_kernels=False, solver="minres") -> A.FtsParams:
     """fts_params from reference parameter keys plus GB300 options."""
     lib = N.load()
     p = A.FtsParams()
@@ -78,12 +80,14 @@ def make_params(par: dict, precision="fp64", preconditioner="auto", operator="au
     p.advection_dt = _par(par, "Advection dt")
     p.surface_tension = _par(par, "Surface tension")
     p.precision = PREC[precision]
+    p.solver = SOLVER[solver]
     p.preconditioner = PC[preconditioner]
     p.operator_kind = OP[operator]
     p.warm_start = 1 if warm_start else 0
     p.device = int(device)
     p.inner_tol = float(inner_tol)
     p.verbose = 1 if verbose else 0
+    p.time_kernels = 1 if time_kernels else 0
     return p
 
 

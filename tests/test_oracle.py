@@ -1,0 +1,196 @@
+"""CPU tests of the oracle (the checker) — no GPU.
+
+The reference has no tests or golden vectors and cannot be built here, so the
+oracle is pinned by known-answer identities of the P1 forms, by a direct
+sparse solve of the same system, and by the committed fixtures in
+tests/golden (regression pins).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, workload
+
+import oracle as O  # noqa: E402
+
+
+def _blocks(inst, alpha=None, eps=None, mu=None, s=None):
+    par = inst.params
+    s = O.source(inst.phi, inst.source, par["GF growth"]) if s is None else s
+    return O.assemble_blocks(inst.xyz, inst.tets, inst.mu if mu is None else mu, s,
+                             par["alpha"] if alpha is None else alpha,
+                             par["eps"] if eps is None else eps)
+
+
+def _volumes(inst):
+    P = inst.xyz.astype(np.float64)[inst.tets]
+    B = np.stack([P[:, 1] - P[:, 0], P[:, 2] - P[:, 0], P[:, 3] - P[:, 0]], axis=2)
+    return np.abs(np.linalg.det(B)) / 6.0
+
+
+def test_reference_tables():
+    tab, qw = O.ref_tables()
+    a = (5 + 3 * np.sqrt(5)) / 20
+    b = (5 - np.sqrt(5)) / 20
+    # float-rounded P1 values at the 4-point rule (Quadrature.hpp:24-36)
+    assert tab[1, 0] == float(np.float32(a)) and tab[1, 1] == float(np.float32(b))
+    assert tab[0, 3] == float(np.float32(1.0 - 3 * float(np.float32(b))))
+    assert qw == 0.25 / 6.0
+    assert np.allclose(tab.sum(axis=0), 1.0, atol=1e-7)
+
+
+@pytest.mark.parametrize("name,n", [("sphere17", 9), ("sphere65", 9)])
+def test_mass_matrix_sums_to_volume(name, n):
+    inst = workload(name, n)
+    B = _blocks(inst, alpha=0.0, eps=1.0)
+    M = B.vals[:, 3, 3]
+    # The basis table is float-rounded (Tetrahedron.hpp:17-18), so the mass
+    # matrix sums to volume * sum_q w_q (sum_a phi_a(q))^2, not exactly to 1.
+    tab, _ = O.ref_tables()
+    table_factor = float(np.sum(0.25 * tab.sum(axis=0) ** 2))
+    assert abs(table_factor - 1.0) < 1e-7
+    assert abs(M.sum() - _volumes(inst).sum() * table_factor) <= 1e-12
+    assert abs(_volumes(inst).sum() - 1.0) <= 1e-6
+
+
+@pytest.mark.parametrize("name,n", [("sphere17", 9), ("sphere65", 9)])
+def test_rigid_and_constant_identities(name, n):
+    inst = workload(name, n)
+    B = _blocks(inst, alpha=1.0, eps=0.0)
+    npn = inst.np
+    rows = np.repeat(np.arange(npn), np.diff(B.rowptr))
+    V = B.vals
+    # K applied to a constant velocity field vanishes on every row
+    for comp in range(3):
+        rs = np.zeros((npn, 3))
+        np.add.at(rs, rows, V[:, :3, comp])
+        assert np.abs(rs).max() <= 1e-12 * np.abs(V[:, :3, :3]).max()
+    # D applied to a constant pressure vanishes (sum_j D_ij = 0)
+    ds = np.zeros(npn)
+    np.add.at(ds, rows, V[:, 3, 3])
+    assert np.abs(ds).max() <= 1e-12 * np.abs(V[:, 3, 3]).max()
+    # sum_i B_al(i, k) = int d_al(sum_i phi_i) psi_k = 0 for every pressure column k
+    cs = np.zeros((npn, 3))
+    np.add.at(cs, B.cols, -V[:, :3, 3])
+    assert np.abs(cs).max() <= 1e-12 * np.abs(V[:, :3, 3]).max()
+
+
+def test_block_symmetry():
+    inst = workload("sphere65", 9)
+    B = _blocks(inst)
+    npn = inst.np
+    pos = {}
+    rows = np.repeat(np.arange(npn), np.diff(B.rowptr))
+    for q, (i, j) in enumerate(zip(rows, B.cols)):
+        pos[(i, j)] = q
+    for q, (i, j) in enumerate(zip(rows, B.cols)):
+        t = B.vals[pos[(j, i)]]
+        b = B.vals[q]
+        assert np.allclose(b[:3, :3], t[:3, :3].T, rtol=0, atol=1e-15)
+        assert np.allclose(b[3, :3], -t[:3, 3], rtol=0, atol=1e-15)  # B^T vs -B
+        assert abs(b[3, 3] - t[3, 3]) <= 1e-15
+
+
+def test_zero_source_gives_zero_rhs():
+    inst = workload("sphere17", 9)
+    s = np.zeros(inst.np)
+    B = _blocks(inst, s=s)
+    assert np.abs(B.rhs).max() == 0.0
+
+
+def test_source_zero_mean_and_interior():
+    inst = workload("sphere17", 9)
+    s = O.source(inst.phi, inst.source, 0.5, 0.1, 0.2)
+    assert abs(s.sum()) <= 1e-12 * max(1.0, np.abs(s).sum())
+    raw = np.where((inst.phi < 0) & (inst.source > 0.2), (inst.source - 0.1) * 0.5, 0.0)
+    assert np.allclose(s, raw - raw.mean(), atol=1e-15)
+
+
+def test_boundary_nodes_are_cube_faces():
+    inst = workload("sphere65", 9)
+    bnd = O.boundary_nodes(inst.np, inst.tets)
+    assert np.array_equal(bnd, inst.boundary)
+
+
+@pytest.mark.parametrize("profile", [0, 1, 2])
+def test_viscosity_profile_restatement(profile):
+    inst = workload("sphere17", 9)
+    mu, mm = O.set_viscosity(inst.tets, inst.phi, inst.source, 30.0, 2.0, profile, 1.0, 1.5)
+    inside = np.all(inst.phi[inst.tets] < 0, axis=1)
+    c3 = inst.source[inst.tets].max(axis=1)
+    if profile == 2:
+        c3 = np.minimum(4 * c3, 1.5)
+    f = c3 / 1.5
+    want = 2.0 * f + 30.0 * (1 - f) if profile == 0 else 30.0 * f + 2.0 * (1 - f)
+    ref = np.where(inside, want, 2.0)
+    assert np.allclose(mu, ref, rtol=1e-15, atol=0)
+    assert mm[0] == ref[inside].min() and mm[1] == ref[inside].max()
+
+
+def test_tight_solve_matches_direct_solve():
+    inst = workload("sphere17", 9)
+    R, _, _, mu = O.system(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source, inst.mu,
+                           inst.params)
+    x, tr, _ = O.solve_tight(R, inst.xyz, inst.tets, mu, tol=1e-13)
+    xd = O.direct_solve(R)
+    assert tr <= 1e-12
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) <= 1e-10
+
+
+def test_bicgstab_reference_algorithm():
+    """Un-preconditioned BiCGSTAB (the reference's solver) reaches its stopping
+    rule and agrees with the direct solve to the accuracy its tolerance allows."""
+    inst = workload("sphere17", 9)
+    R, _, _, _ = O.system(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source, inst.mu,
+                          inst.params)
+    # Eigen's default cap is 2N iterations; near it the outcome depends on
+    # rounding (OpenMP reduction order), so only the cap itself is checked.
+    x, info, it, err = O.bicgstab(R, None, tol=1e-10)
+    assert it <= 2 * R.N and (info == 0) == (err <= 1e-10)
+    x, info, it, err = O.bicgstab(R, None, tol=1e-8)
+    assert info == 0 and err <= 1e-8
+    assert O.true_residual(R, x) <= 2e-8
+    xd = O.direct_solve(R)
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) <= 1e-4
+    # warm start from the solution: converged at iteration 0
+    x2, info2, it2, _ = O.bicgstab(R, x, tol=1e-8)
+    assert info2 == 0 and it2 == 0
+
+
+def test_flow_solve_early_exits():
+    inst = workload("sphere17", 9)
+    par = dict(inst.params)
+    par["Advection dt"] = 0.0
+    flow = np.full(4 * inst.np, 7.0)
+    st, out, _, info = O.flow_solve(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source,
+                                    inst.mu, par, flow=flow)
+    assert st == 0 and np.all(out == 7.0) and info["exit"] == "advection dt zero"
+    par = dict(inst.params)
+    st, out, _, info = O.flow_solve(inst.xyz, inst.tets, inst.boundary, inst.phi,
+                                    np.zeros(inst.np), inst.mu, par, flow=flow)
+    assert st == 0 and np.all(out == 7.0) and info["exit"] == "load zero"
+
+
+@pytest.mark.parametrize("fixture", ["sphere17.npz", "sphere65_n9.npz"])
+def test_golden_fixture(fixture):
+    """The oracle reproduces the committed fixture from the stored inputs."""
+    import importlib.util
+    from fluidtissue_gb300 import workloads as W
+    spec = importlib.util.spec_from_file_location("mk", ROOT / "tests/golden/make_golden.py")
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    g = np.load(ROOT / "tests" / "golden" / fixture)
+    n = int(g["n"])
+    inst = W.WORKLOADS[str(g["name"])](n)
+    assert mk.mesh_hash(inst.xyz, inst.tets) == str(g["mesh_sha256"])
+    R, _, _, mu = O.system(inst.xyz, inst.tets, g["boundary"], g["phi"], g["source"], g["mu"],
+                           inst.params)
+    assert np.allclose(R.F, g["F"], rtol=0, atol=1e-13 * np.abs(g["F"]).max())
+    x, tr, _ = O.solve_tight(R, inst.xyz, inst.tets, mu, tol=1e-13)
+    flow = O.scatter(R, x)
+    ref = g["flow"]
+    npn = inst.np
+    ev = np.linalg.norm(flow[:3 * npn] - ref[:3 * npn]) / np.linalg.norm(ref[:3 * npn])
+    ep = np.linalg.norm(flow[3 * npn:] - ref[3 * npn:]) / np.linalg.norm(ref[3 * npn:])
+    assert ev <= 1e-10 and ep <= 1e-10
