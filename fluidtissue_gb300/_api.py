@@ -99,7 +99,10 @@ SIGNATURES = {
     "fts_get_sizes": (C.c_int, [_vp, _P(C.c_int64), _P(C.c_int64), _P(C.c_int64)]),
     "fts_get_system": (C.c_int, [_vp, _P(C.c_int32), _P(C.c_int32), _dp, _dp]),
     "fts_apply": (C.c_int, [_vp, C.c_int32, _dp, _dp]),
+    "fts_bsr_residual_noalloc": (C.c_int, [C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
+
+NOALLOC_MAX_NODES = 1048576
 
 
 def declare(lib: C.CDLL) -> None:

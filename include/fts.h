@@ -202,6 +202,31 @@ int fts_get_system(const fts_ctx* ctx, int32_t* rowptr, int32_t* cols, double* v
  * FTS_PREC_MIXED (the FP32 copy). */
 int fts_apply(fts_ctx* ctx, int32_t precision, const double* x, double* y);
 
+/* ---- allocation-free residual ------------------------------------------- */
+
+/* Largest system (block rows = nodes) fts_bsr_residual_noalloc accepts: its
+ * reduction scratch is a fixed static device array of 256 KB. */
+#define FTS_NOALLOC_MAX_NODES 1048576
+
+/* No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory — applications that own all of the GPU's memory
+ * through their own arena, or loops that must not stall on the device
+ * synchronisation cudaMalloc / cudaFree can cause.  It computes the FP64
+ * residual of a node-blocked system in the layout fts_get_system returns,
+ * r = b - S x, with norms[0] = ||r||^2 and norms[1] = ||b||^2, and allocates
+ * nothing: rowptr[np+1], cols[nnzb], vals[16*nnzb], x[4*np], b[4*np] (inputs)
+ * and r[4*np], norms[2] (outputs) are device memory owned by the caller; the
+ * reduction scratch is a static device array (every GPU that loads the library
+ * holds it until exit).  np must be <= FTS_NOALLOC_MAX_NODES, else
+ * FTS_ERR_BAD_INPUT.  Runs on `stream` (a cudaStream_t; NULL = the legacy
+ * default stream) of the current device and returns without waiting for it.
+ * The first call on a device looks up the scratch array's device address and
+ * should come before any stream capture.  Calls share the array: calls whose
+ * kernels overlap on the GPU race and their norms are wrong. */
+int fts_bsr_residual_noalloc(int64_t np, const int32_t* rowptr, const int32_t* cols,
+                             const double* vals, const double* x, const double* b, double* r,
+                             double* norms, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
