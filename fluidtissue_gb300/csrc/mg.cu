@@ -6,9 +6,12 @@
 // node; each fine node is either a coarse node or the midpoint of a coarse
 // Kuhn edge, so the prolongation P is linear interpolation with weights 1 or
 // 1/2 along the 14 Kuhn directions.  The Galerkin operator P^T K P keeps the
-// 15-point Kuhn stencil, so every level stores K as 15 direction blocks of 3x3
-// per node, in tiles of 32 nodes: K[((node/32)*135 + 9d + 3r + c)*32 + node%32] — every load of a
-// warp is one coalesced segment and no column indices are read.
+// 15-point Kuhn stencil.  K is symmetric, so every level stores only the self
+// block and the 7 positive-direction 3x3 blocks per node (72 values) in tiles
+// of 32 nodes: K[((node/32)*72 + 9d + 3r + c)*32 + node%32]; the block in the
+// negative direction -e of node v is the transpose of node (v - e)'s block in
+// direction +e.  Every load of a warp is one coalesced segment and no column
+// indices are read.
 //
 // Smoother: Chebyshev polynomial of degree kSmooth in D^-1 K (D = 3x3 node
 // blocks) on [lambda/10, lambda], lambda from power iteration; the same
@@ -71,11 +74,21 @@ static void init_tables(int device) {
     if (device < 64) done[device] = true;
 }
 
-// Tiled stencil layout: 32 consecutive nodes share one tile of 135 x 32
-// values (entry q = 9 d + 3 r + c), so the 135 loads of a warp stay inside one
-// contiguous 17 KB (FP32) region.
+// Tiled stencil layout: 32 consecutive nodes share one tile of kStored x 32
+// values (entry q = 9 d + 3 r + c, d = 0..7), so the loads of a warp stay
+// inside one contiguous 9 KB (FP32) region.
+constexpr int kStored = 72;
 __device__ __forceinline__ int64_t kidx(int q, int64_t v) {
-    return ((v >> 5) * 135 + q) * 32 + (v & 31);
+    return ((v >> 5) * kStored + q) * 32 + (v & 31);
+}
+
+// Entry x = 3r + c of the block K(f, f + off[e]) for any of the 15 directions.
+template <typename T>
+__device__ __forceinline__ T kblock(const T* __restrict__ K, int e, int x, int64_t f, int n) {
+    if (e < 8) return K[kidx(9 * e + x, f)];
+    const int ep = e - 7;  // positive direction; the block is stored at f - off[ep]
+    const int64_t w = f - (c_off[ep][0] + (int64_t)n * (c_off[ep][1] + (int64_t)n * c_off[ep][2]));
+    return K[kidx(9 * ep + 3 * (x % 3) + x / 3, w)];
 }
 
 __device__ __forceinline__ int nbr(int i, int j, int k, int d, int n) {
@@ -94,7 +107,7 @@ __global__ void k_mg_extract(int n, const int32_t* __restrict__ rowptr,
                              const int32_t* __restrict__ cols, const double* __restrict__ A,
                              T* __restrict__ K) {
     const int64_t N = (int64_t)n * n * n;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * 15;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * 8;
          t += (int64_t)gridDim.x * blockDim.x) {
         const int d = (int)(t / N);
         const int64_t v = t - d * N;
@@ -137,7 +150,7 @@ template <typename T>
 __global__ void k_mg_galerkin(int nf, const T* __restrict__ Kf, const uint8_t* __restrict__ mf,
                               int nc, T* __restrict__ Kc, const uint8_t* __restrict__ mc) {
     const int64_t Nf = (int64_t)nf * nf * nf, Nc = (int64_t)nc * nc * nc;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Nc * 15;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Nc * 8;
          t += (int64_t)gridDim.x * blockDim.x) {
         const int dJ = (int)(t / Nc);
         const int64_t I = t - dJ * Nc;
@@ -160,8 +173,15 @@ __global__ void k_mg_galerkin(int nf, const T* __restrict__ Kf, const uint8_t* _
                 if (g < 0 || mf[g]) continue;
                 const T w = (T)c_gal_w[q];
 #pragma unroll
-                for (int x = 0; x < 9; ++x) acc[x] += w * Kf[kidx(e * 9 + x, f)];
+                for (int x = 0; x < 9; ++x) acc[x] += w * kblock<T>(Kf, e, x, f, nf);
             }
+        }
+        if (dJ == 0) {  // the self block of a symmetric operator: symmetrise rounding
+            T s01 = T(0.5) * (acc[1] + acc[3]), s02 = T(0.5) * (acc[2] + acc[6]),
+              s12 = T(0.5) * (acc[5] + acc[7]);
+            acc[1] = acc[3] = s01;
+            acc[2] = acc[6] = s02;
+            acc[5] = acc[7] = s12;
         }
 #pragma unroll
         for (int x = 0; x < 9; ++x) Kc[kidx(dJ * 9 + x, I)] = acc[x];
@@ -206,7 +226,7 @@ __device__ __forceinline__ void stencil_apply(int n, int64_t N, int64_t v64,
     const bool inner = i > 0 && j > 0 && k > 0 && i < n - 1 && j < n - 1 && k < n - 1;
     T a0 = T(0), a1 = T(0), a2 = T(0);
 #pragma unroll
-    for (int d = 0; d < 15; ++d) {
+    for (int d = 0; d < 8; ++d) {  // self and positive directions: own blocks
         const int w = inner ? v + c_off[d][0] + n * c_off[d][1] + nn * c_off[d][2]
                             : nbr(i, j, k, d, n);
         if (w < 0) continue;
@@ -215,6 +235,17 @@ __device__ __forceinline__ void stencil_apply(int n, int64_t N, int64_t v64,
         a0 = fma(kb[0], x0, fma(kb[32], x1, fma(kb[64], x2, a0)));
         a1 = fma(kb[96], x0, fma(kb[128], x1, fma(kb[160], x2, a1)));
         a2 = fma(kb[192], x0, fma(kb[224], x1, fma(kb[256], x2, a2)));
+    }
+#pragma unroll
+    for (int d = 1; d < 8; ++d) {  // negative directions: neighbour's block, transposed
+        const int w = inner ? v - c_off[d][0] - n * c_off[d][1] - nn * c_off[d][2]
+                            : nbr(i, j, k, d + 7, n);
+        if (w < 0) continue;
+        const T x0 = x[w], x1 = x[N + w], x2 = x[2 * N + w];
+        const T* kb = K + kidx(d * 9, (int64_t)w);
+        a0 = fma(kb[0], x0, fma(kb[96], x1, fma(kb[192], x2, a0)));
+        a1 = fma(kb[32], x0, fma(kb[128], x1, fma(kb[224], x2, a1)));
+        a2 = fma(kb[64], x0, fma(kb[160], x1, fma(kb[256], x2, a2)));
     }
     y[0] = a0;
     y[1] = a1;
@@ -276,7 +307,8 @@ __global__ void k_mg_power_init(int64_t N, const uint8_t* __restrict__ mask, T* 
 //   d_0 = D^-1 r / theta;  d_i = rho_i rho_{i-1} d_{i-1} + (2 rho_i/delta) D^-1 r_i.
 // ---------------------------------------------------------------------------
 constexpr double kLowFrac = 0.1;
-constexpr int kCoefStride = 64;  // per level: 1/theta, then (ca_s, cb_s) for s >= 1
+constexpr int kCoefStride = 64;      // per level: 1/theta, then (ca_s, cb_s) for s >= 1
+constexpr int kCoarseThreads = 256;  // one CTA for the coarsest level (<= 9^3 nodes)
 
 // Chebyshev coefficients of one level, computed once per solve on the host.
 static void cheb_table(double lam, double* out) {
@@ -436,7 +468,7 @@ __global__ void k_mg_prolong(int nf, T* __restrict__ xf, const uint8_t* __restri
 
 // Coarsest level: kCoarse Chebyshev steps from zero in a single CTA.
 template <typename T>
-__global__ void k_mg_coarse_solve(int n, const T* __restrict__ K, const T* __restrict__ Di,
+__global__ void __launch_bounds__(kCoarseThreads) k_mg_coarse_solve(int n, const T* __restrict__ K, const T* __restrict__ Di,
                                   const T* __restrict__ b, T* __restrict__ x, T* __restrict__ r,
                                   T* __restrict__ d0, T* __restrict__ d1,
                                   const double* __restrict__ coef, int steps,
@@ -488,7 +520,7 @@ void mg_build(Ctx& c, MG<T>& mg) {
         MGLevel<T> L;
         L.n = n;
         L.N = (int64_t)n * n * n;
-        L.K = dev_alloc<T>(c, (size_t)((L.N + 31) / 32) * 32 * 135);
+        L.K = dev_alloc<T>(c, (size_t)((L.N + 31) / 32) * 32 * kStored);
         L.Di = dev_alloc<T>(c, (size_t)L.N * 6);
         for (auto** p : {&L.b, &L.x, &L.r, &L.d0, &L.d1}) *p = dev_alloc<T>(c, (size_t)L.N * 3);
         L.mask = dev_alloc<uint8_t>(c, (size_t)L.N);
@@ -515,14 +547,14 @@ template <typename T>
 void mg_setup(Ctx& c, MG<T>& mg) {
     mg_build<T>(c, mg);
     MGLevel<T>& F = mg.L[0];
-    k_mg_extract<T><<<grid_for(c, F.N * 15), kThreads, 0, c.stream>>>(F.n, c.rowptr, c.cols,
+    k_mg_extract<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(F.n, c.rowptr, c.cols,
                                                                        c.A64, F.K);
     c.launches += 1;
     for (size_t l = 0; l < mg.L.size(); ++l) {
         MGLevel<T>& L = mg.L[l];
         if (l > 0) {
             MGLevel<T>& P = mg.L[l - 1];
-            k_mg_galerkin<T><<<grid_for(c, L.N * 15), kThreads, 0, c.stream>>>(P.n, P.K, P.mask,
+            k_mg_galerkin<T><<<grid_for(c, L.N * 8), kThreads, 0, c.stream>>>(P.n, P.K, P.mask,
                                                                                L.n, L.K, L.mask);
             c.launches += 1;
         }
@@ -553,6 +585,8 @@ void mg_setup(Ctx& c, MG<T>& mg) {
     mg.lam_host = lam;
     std::vector<double> coef(lam.size() * kCoefStride);
     for (size_t l = 0; l < lam.size(); ++l) cheb_table(lam[l], coef.data() + l * kCoefStride);
+    // A 3^3 coarsest lattice has a single interior node: x = D^-1 b is exact.
+    if (mg.L.back().n == 3) coef[(lam.size() - 1) * kCoefStride] = 1.0;
     FTS_CUDA(cudaMemcpyAsync(mg.coef, coef.data(), coef.size() * sizeof(double),
                              cudaMemcpyHostToDevice, c.stream));
     FTS_CUDA(cudaStreamSynchronize(c.stream));
@@ -564,8 +598,8 @@ static void vcycle_level(Ctx& c, MG<T>& mg, size_t l, const int* stop) {
     const int g = grid_for(c, L.N);
     const double* lam = mg.coef + l * kCoefStride;
     if (l + 1 == mg.L.size()) {
-        k_mg_coarse_solve<T><<<1, 1024, 0, c.stream>>>(L.n, L.K, L.Di, L.b, L.x, L.r, L.d0, L.d1,
-                                                      lam, kCoarse, stop);
+        k_mg_coarse_solve<T><<<1, kCoarseThreads, 0, c.stream>>>(
+            L.n, L.K, L.Di, L.b, L.x, L.r, L.d0, L.d1, lam, L.n == 3 ? 1 : kCoarse, stop);
         c.launches += 1;
         return;
     }
