@@ -70,6 +70,20 @@ class FtsStats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class FtsBatchConfig(C.Structure):
+    _fields_ = [
+        ("threads", C.c_int32),
+        ("chunk_rows", C.c_int32),
+        ("tpr", C.c_int32),
+        ("blocks", C.c_int32),
+        ("ms_per_sweep", C.c_double),
+        ("graph", C.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_MINRES, SOLVER_BICGSTAB = 0, 1
 PC_AUTO, PC_JACOBI, PC_MULTIGRID = 0, 1, 2
@@ -100,6 +114,13 @@ SIGNATURES = {
     "fts_get_system": (C.c_int, [_vp, _P(C.c_int32), _P(C.c_int32), _dp, _dp]),
     "fts_apply": (C.c_int, [_vp, C.c_int32, _dp, _dp]),
     "fts_bsr_residual_noalloc": (C.c_int, [C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "fts_batch_create": (C.c_int, [C.c_int32, _P(FtsMesh), _P(FtsParams), _P(_vp)]),
+    "fts_batch_solve": (C.c_int, [_vp, _P(_dp), _P(_dp), _P(_dp), _P(_dp), _P(FtsStats)]),
+    "fts_batch_solve_device": (C.c_int, [_vp, _P(_vp), _P(_vp), _P(_vp), _P(_vp), _P(FtsStats)]),
+    "fts_batch_get_config": (C.c_int, [_vp, _P(FtsBatchConfig)]),
+    "fts_batch_set_stream": (C.c_int, [_vp, _vp]),
+    "fts_batch_last_error": (C.c_char_p, [_vp]),
+    "fts_batch_destroy": (None, [_vp]),
 }
 
 NOALLOC_MAX_NODES = 1048576

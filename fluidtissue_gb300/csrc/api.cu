@@ -10,13 +10,9 @@
 
 #include "fts_device.cuh"
 
-struct fts_ctx {
-    fts::Ctx c;
-};
-
 namespace fts {
 
-static void free_all(Ctx& c) {
+void free_all(Ctx& c) {
     void* ptrs[] = {c.xyz, c.tets, c.bnd, c.rowptr, c.cols, c.diag, c.p2t_ptr, c.p2t, c.geom,
                     c.phi, c.src, c.force, c.mu, c.s, c.flow, c.A64, c.A32, c.pc64, c.pc32,
                     c.b, c.x, c.r, c.w64.q, c.w64.R[0], c.w64.R[1], c.w64.Y[0], c.w64.Y[1],
@@ -46,7 +42,7 @@ static void alloc_work(Ctx& c, KrylovWork<T>& w, bool own_r0) {
     if (own_r0) w.r0 = dev_alloc<V4<T>>(c, c.np);
 }
 
-static void ensure_fp32(Ctx& c) {
+void ensure_fp32(Ctx& c) {
     if (c.have32) return;
     c.A32 = dev_alloc<float>(c, (size_t)c.nnzb * 16);
     c.pc32 = dev_alloc<float>(c, (size_t)c.np * 8);
@@ -54,7 +50,7 @@ static void ensure_fp32(Ctx& c) {
     c.have32 = true;
 }
 
-static int validate_params(const fts_params& p, std::string& err) {
+int validate_params(const fts_params& p, std::string& err) {
     if (p.velocity_degree != 1) {
         err = "only the P1-P1 stabilised element (velocity degree 1) is on this path";
         return FTS_ERR_UNSUPPORTED;
@@ -104,7 +100,7 @@ static void configure_preconditioner(Ctx& c) {
     c.crank = (c.par.eps > 0.0 && c.volume > 0.0) ? 1.0 / (c.par.eps * c.volume) : 0.0;
 }
 
-static void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
+void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
     c.par = p;
     c.device = p.device;
     FTS_CUDA(cudaSetDevice(c.device));

@@ -172,6 +172,12 @@ struct Ctx {
     bool tev_ready = false;
 };
 
+// ---- context lifecycle (api.cu) -------------------------------------------
+void create(Ctx& c, const fts_mesh& m, const fts_params& p);   // throws CudaError / int
+void free_all(Ctx& c);
+int validate_params(const fts_params& p, std::string& err);
+void ensure_fp32(Ctx& c);
+
 // ---- assembly (assemble.cu) -----------------------------------------------
 void launch_geometry(Ctx& c, int* bad);
 void launch_viscosity_profile(Ctx& c);
@@ -217,3 +223,7 @@ inline int grid_for(const Ctx& c, int64_t work, int threads = kThreads, int per_
 }
 
 }  // namespace fts
+
+struct fts_ctx {
+    fts::Ctx c;
+};

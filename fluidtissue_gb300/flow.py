@@ -212,5 +212,78 @@ class Flow:
             pass
 
 
+class Batch:
+    """Many independent Stokes solves in one batched call (fts_batch_*): each
+    instance is a ``Flow.solve`` of its own mesh, inputs and parameters."""
+
+    def __init__(self, meshes: list[Mesh], pars: list[dict], **options):
+        self._lib = N.load()
+        self._ctx = C.c_void_p()
+        self.count = len(meshes)
+        self._meshes = meshes
+        ms = (A.FtsMesh * self.count)()
+        ps = (A.FtsParams * self.count)()
+        for i, (m, par) in enumerate(zip(meshes, pars)):
+            ms[i].np = m.xyz.shape[0]
+            ms[i].nt = m.tets.shape[0]
+            ms[i].xyz = N.ptr(m.xyz, C.c_float)
+            ms[i].tets = N.ptr(m.tets, C.c_int32)
+            ms[i].boundary = N.ptr(m.boundary, C.c_uint8)
+            ps[i] = make_params(par, **options)
+        rc = self._lib.fts_batch_create(self.count, ms, ps, C.byref(self._ctx))
+        if rc != 0:
+            msg = self._lib.fts_batch_last_error(None).decode()
+            self._ctx = C.c_void_p()
+            raise FtsError(rc, msg)
+        self.last_stats: list[dict] = []
+
+    def solve(self, phis, sources, flows, mus=None) -> int:
+        D = C.c_double
+        arr = lambda xs: (C.POINTER(D) * self.count)(  # noqa: E731
+            *[N.ptr(None if x is None else np.ascontiguousarray(x, np.float64), D) for x in xs])
+        keep = [np.ascontiguousarray(x, np.float64) for x in phis + sources]
+        phis = keep[:self.count]
+        sources = keep[self.count:]
+        for f in flows:
+            assert f.dtype == np.float64 and f.flags["C_CONTIGUOUS"]
+        st = (A.FtsStats * self.count)()
+        rc = self._lib.fts_batch_solve(self._ctx, arr(phis), arr(sources),
+                                       arr(mus) if mus is not None else None, arr(flows), st)
+        self.last_stats = [s.as_dict() for s in st]
+        return rc
+
+    def solve_device(self, phi_ptrs, source_ptrs, mu_ptrs, flow_ptrs) -> int:
+        V = C.c_void_p
+        arr = lambda xs: (V * self.count)(*[V(x) if x else V() for x in xs])  # noqa: E731
+        st = (A.FtsStats * self.count)()
+        rc = self._lib.fts_batch_solve_device(self._ctx, arr(phi_ptrs), arr(source_ptrs),
+                                              arr(mu_ptrs) if mu_ptrs is not None else None,
+                                              arr(flow_ptrs), st)
+        self.last_stats = [s.as_dict() for s in st]
+        return rc
+
+    def config(self) -> dict:
+        c = A.FtsBatchConfig()
+        self._lib.fts_batch_get_config(self._ctx, C.byref(c))
+        return c.as_dict()
+
+    def set_stream(self, stream_handle: int | None) -> int:
+        return self._lib.fts_batch_set_stream(self._ctx, stream_handle or None)
+
+    def last_error(self) -> str:
+        return self._lib.fts_batch_last_error(self._ctx).decode()
+
+    def close(self) -> None:
+        if getattr(self, "_ctx", None):
+            self._lib.fts_batch_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def status_string(rc: int) -> str:
     return N.load().fts_status_string(rc).decode()

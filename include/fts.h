@@ -202,6 +202,44 @@ int fts_get_system(const fts_ctx* ctx, int32_t* rowptr, int32_t* cols, double* v
  * FTS_PREC_MIXED (the FP32 copy). */
 int fts_apply(fts_ctx* ctx, int32_t precision, const double* x, double* y);
 
+/* ---- batched solves ------------------------------------------------------ */
+
+/* Many independent Stokes solves (own mesh, viscosity and parameters each)
+ * solved together: per-instance assembly, then the MINRES iteration of all
+ * instances in one persistent cooperative launch with per-instance
+ * convergence masks, the outer FP64 loop on the device, the sequence captured
+ * as a CUDA graph.  Block-Jacobi + rank-one preconditioner (any mesh).  Each
+ * instance is a Flow::solve (src/growth/Flow.cpp:89) of its own inputs. */
+typedef struct fts_batch fts_batch;
+
+/* Launch shape of the persistent kernel, chosen by the autotuner on the first
+ * solve (threads per block, rows per work chunk, threads per block row = the
+ * SpMV work split, co-resident blocks) and its measured time per sweep. */
+typedef struct fts_batch_config {
+    int32_t threads;
+    int32_t chunk_rows;
+    int32_t tpr;
+    int32_t blocks;
+    double ms_per_sweep;
+    int32_t graph;  /* 1 when the outer loop runs as a captured CUDA graph */
+} fts_batch_config;
+
+/* count instances; meshes[count], params[count] (same precision and device). */
+int fts_batch_create(int32_t count, const fts_mesh* meshes, const fts_params* params,
+                     fts_batch** out);
+/* phi[i], source[i], flow[i] per instance (host); mu (nullable array) per
+ * instance nullable; stats[count] (nullable).  Returns the first non-OK
+ * instance status. */
+int fts_batch_solve(fts_batch* b, const double* const* phi, const double* const* source,
+                    const double* const* mu, double* const* flow, fts_stats* stats);
+/* The same with device pointers. */
+int fts_batch_solve_device(fts_batch* b, const double* const* phi, const double* const* source,
+                           const double* const* mu, double* const* flow, fts_stats* stats);
+int fts_batch_get_config(const fts_batch* b, fts_batch_config* cfg);
+int fts_batch_set_stream(fts_batch* b, void* stream);
+const char* fts_batch_last_error(const fts_batch* b);
+void fts_batch_destroy(fts_batch* b);
+
 /* ---- allocation-free residual ------------------------------------------- */
 
 /* Largest system (block rows = nodes) fts_bsr_residual_noalloc accepts: its
