@@ -146,11 +146,15 @@ def run_ours(args):
     flow_d = torch.zeros(4 * npn, dtype=torch.float64, device=dev)
     torch.cuda.synchronize()
 
+    operator = args.operator or ("matfree" if args.workload == "spheres257" else "assembled")
+    with_fp64 = not args.no_fp64 and operator == "assembled"
+
     def make(precision):
         f = Flow()
         rc = f.init(Mesh(inst.xyz, inst.tets), par, precision=precision, warm_start=False,
                     device=local, preconditioner=args.preconditioner, time_kernels=True,
-                    inner_tol=args.inner_tol)
+                    inner_tol=args.inner_tol,
+                    operator=operator if precision == "mixed" else "assembled")
         if rc != 0:
             raise RuntimeError(f"fts_create failed ({rc}): {f.last_error()}")
         f.set_stream(stream.cuda_stream)
@@ -208,16 +212,19 @@ def run_ours(args):
     flow_mixed = flow_h.copy()
 
     # ---- plain FP64 on the same workload -------------------------------------
-    f64 = make("fp64")
-    device_steps(f64, 1)
-    k64 = max(1, args.steps_fp64)
-    stats_d, ms_d, _, _ = timed(lambda k: device_steps(f64, k), k64)
-    value_fp64 = ws * k64 / (ms_d / 1e3)
-    flow64 = flow_d.cpu().numpy()
-    vel_err = float(np.linalg.norm(flow_mixed[:3 * npn] - flow64[:3 * npn]) /
-                    np.linalg.norm(flow64[:3 * npn]))
-    p_err = float(np.linalg.norm(flow_mixed[3 * npn:] - flow64[3 * npn:]) /
-                  np.linalg.norm(flow64[3 * npn:]))
+    f64 = None
+    stats_d, ms_d, value_fp64, vel_err, p_err, k64 = None, None, None, None, None, 0
+    if with_fp64:
+        f64 = make("fp64")
+        device_steps(f64, 1)
+        k64 = max(1, args.steps_fp64)
+        stats_d, ms_d, _, _ = timed(lambda k: device_steps(f64, k), k64)
+        value_fp64 = ws * k64 / (ms_d / 1e3)
+        flow64 = flow_d.cpu().numpy()
+        vel_err = float(np.linalg.norm(flow_mixed[:3 * npn] - flow64[:3 * npn]) /
+                        np.linalg.norm(flow64[:3 * npn]))
+        p_err = float(np.linalg.norm(flow_mixed[3 * npn:] - flow64[3 * npn:]) /
+                      np.linalg.norm(flow64[3 * npn:]))
 
     # ---- roofline of the dominant kernel (live CUDA-event timing) -----------
     spmv_ms = sum(s["ms_spmv"] for s in stats_m)
@@ -226,13 +233,15 @@ def run_ours(args):
     bytes_per = stats_m[0]["spmv_bytes"]
     achieved = bytes_per / (per / 1e3) / 1e9 if spmv_n else None
     peak, peak_kind = _peaks()
-    spmv64_ms = sum(s["ms_spmv"] for s in stats_d)
-    spmv64_n = sum(s["spmv_launches"] for s in stats_d)
-    ach64 = (stats_d[0]["spmv_bytes"] / (spmv64_ms / spmv64_n / 1e3) / 1e9) if spmv64_n else None
+    ach64, it_d = None, None
+    if stats_d:
+        spmv64_ms = sum(s["ms_spmv"] for s in stats_d)
+        spmv64_n = sum(s["spmv_launches"] for s in stats_d)
+        ach64 = (stats_d[0]["spmv_bytes"] / (spmv64_ms / spmv64_n / 1e3) / 1e9) if spmv64_n else None
+        it_d = statistics.mean(s["iterations"] for s in stats_d)
 
     launches = int(sum(s["kernel_launches"] for s in stats_m))
     it_m = statistics.mean(s["iterations"] for s in stats_m)
-    it_d = statistics.mean(s["iterations"] for s in stats_d)
     dofs = 4 * npn
 
     res = {
@@ -249,10 +258,12 @@ def run_ours(args):
         "e2e": {"value": round(e2e, 4), "unit": UNIT,
                 "h2d_bytes_per_step": int(phi_h.nbytes + src_h.nbytes + mu_h.nbytes),
                 "d2h_bytes_per_step": int(flow_h.nbytes)},
-        "fp64": {"value": round(value_fp64, 4), "unit": UNIT,
-                 "ms_per_step": round(ms_d / k64, 3), "iterations": it_d,
-                 "spmv_gbs": round(ach64, 1) if ach64 else None},
-        "mixed_vs_fp64": round(value / value_fp64, 3),
+        "fp64": ({"value": round(value_fp64, 4), "unit": UNIT,
+                  "ms_per_step": round(ms_d / k64, 3), "iterations": it_d,
+                  "spmv_gbs": round(ach64, 1) if ach64 else None} if value_fp64 else None),
+        "mixed_vs_fp64": round(value / value_fp64, 3) if value_fp64 else None,
+        "operator": operator,
+        "device_bytes": int(stats_m[0]["device_bytes"]),
         "mixed": {"iterations": it_m, "iterations_fp32": statistics.mean(
             s["iterations_fp32"] for s in stats_m),
                   "outer": statistics.mean(s["outer_iterations"] for s in stats_m),
@@ -262,8 +273,11 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4) if achieved else None,
-                     "traffic": _traffic("k_minres_A<float>"),
-                     "kernel": "k_minres_A<float> (FP32 BSR SpMV + MINRES dots)",
+                     "traffic": _traffic("k_mf_minres_A" if operator == "matfree"
+                                         else "k_minres_A<float>"),
+                     "kernel": ("k_mf_minres_A (FP32 matrix-free element operator + MINRES dots)"
+                                if operator == "matfree" else
+                                "k_minres_A<float> (FP32 BSR SpMV + MINRES dots)"),
                      "bytes_per_launch": bytes_per, "ms_per_launch": round(per, 5),
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
         "gpu_launches": launches,
@@ -275,7 +289,8 @@ def run_ours(args):
     if rank == 0:
         print(json.dumps(res), flush=True)
     fm.close()
-    f64.close()
+    if f64 is not None:
+        f64.close()
     if dist is not None:
         dist.destroy_process_group()
 
@@ -424,6 +439,8 @@ def main():
     ap.add_argument("--inner-tol", type=float, default=0.0)
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--batch-count", type=int, default=96)
+    ap.add_argument("--operator", default=None, choices=["assembled", "matfree"])
+    ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -44,7 +44,7 @@ static void alloc_work(Ctx& c, KrylovWork<T>& w, bool own_r0) {
 
 void ensure_fp32(Ctx& c) {
     if (c.have32) return;
-    c.A32 = dev_alloc<float>(c, (size_t)c.nnzb * 16);
+    if (!c.matfree) c.A32 = dev_alloc<float>(c, (size_t)c.nnzb * 16);
     c.pc32 = dev_alloc<float>(c, (size_t)c.np * 8);
     alloc_work<float>(c, c.w32, true);
     c.have32 = true;
@@ -97,6 +97,11 @@ static void configure_preconditioner(Ctx& c) {
         throw (int)FTS_ERR_UNSUPPORTED;
     }
     c.use_mg = mg_ok && c.par.preconditioner != FTS_PC_JACOBI;
+    if (c.matfree && (!c.use_mg || c.par.precision != FTS_PREC_MIXED)) {
+        c.last_error = "the matrix-free operator runs in mixed precision with the multigrid "
+                       "preconditioner (Kuhn lattice, odd n >= 9)";
+        throw (int)FTS_ERR_UNSUPPORTED;
+    }
     c.crank = (c.par.eps > 0.0 && c.volume > 0.0) ? 1.0 / (c.par.eps * c.volume) : 0.0;
 }
 
@@ -129,7 +134,8 @@ void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
     c.mu = dev_alloc<double>(c, c.nt);
     c.s = dev_alloc<double>(c, c.np);
     c.flow = dev_alloc<double>(c, 4 * c.np);
-    c.A64 = dev_alloc<double>(c, (size_t)c.nnzb * 16);
+    c.matfree = p.operator_kind == FTS_OP_MATFREE;
+    if (!c.matfree) c.A64 = dev_alloc<double>(c, (size_t)c.nnzb * 16);
     c.pc64 = dev_alloc<double>(c, (size_t)c.np * 8);
     c.b = dev_alloc<V4<double>>(c, c.np);
     c.x = dev_alloc<V4<double>>(c, c.np);
@@ -234,14 +240,21 @@ static int solve_device(Ctx& c, bool have_mu, bool have_force, double* flow_out,
     launch_rhs(c, have_force);
     // the zero-load exit (Flow.cpp:248-251) needs ||F||: computed with the
     // residual kernel on x = 0 below when the matrix exists; here directly.
-    launch_assemble(c);
-    launch_preconditioner(c);
-    if (P.precision == FTS_PREC_MIXED) {
-        ensure_fp32(c);
-        launch_to_f32(c);
+    if (c.matfree) {
+        // no block matrix: pressure weights and the multigrid fine level come
+        // straight from the elements
+        launch_mf_pc(c);
         setup_preconditioner<float>(c);
     } else {
-        setup_preconditioner<double>(c);
+        launch_assemble(c);
+        launch_preconditioner(c);
+        if (P.precision == FTS_PREC_MIXED) {
+            ensure_fp32(c);
+            launch_to_f32(c);
+            setup_preconditioner<float>(c);
+        } else {
+            setup_preconditioner<double>(c);
+        }
     }
     FTS_CUDA(cudaEventRecord(c.ev[1], c.stream));
     int bad = 0;
@@ -510,6 +523,8 @@ static int solve_common(fts_ctx* ctx, const double* phi, const double* source, c
         const double V = c.par.precision == FTS_PREC_MIXED ? 4.0 : 8.0;
         const double nb = (double)c.nnzb, n = (double)c.np;
         st.spmv_bytes = nb * (16.0 * V + 4.0) + 4.0 * (n + 1.0) + 3.0 * 4.0 * n * V;
+        if (c.matfree)  // tets + node->element map + mu per element; coords, flags, x, r1, q per node
+            st.spmv_bytes = (double)c.nt * (16.0 + 16.0 + 8.0) + n * (4.0 + 12.0 + 1.0 + 3.0 * 16.0);
         st.spmv_bytes_fp64 = nb * (16.0 * 8.0 + 4.0) + 4.0 * (n + 1.0) + 3.0 * 4.0 * n * 8.0;
     }
     if (stats) *stats = st;
@@ -588,6 +603,7 @@ int fts_get_sizes(const fts_ctx* ctx, int64_t* np, int64_t* nnzb, int64_t* n_red
 int fts_get_system(const fts_ctx* ctx, int32_t* rowptr, int32_t* cols, double* vals, double* rhs) {
     if (!ctx) return FTS_ERR_BAD_INPUT;
     const Ctx& c = ctx->c;
+    if (c.matfree) return FTS_ERR_UNSUPPORTED;
     try {
         FTS_CUDA(cudaSetDevice(c.device));
         FTS_CUDA(cudaStreamSynchronize(c.stream));
@@ -606,6 +622,7 @@ int fts_get_system(const fts_ctx* ctx, int32_t* rowptr, int32_t* cols, double* v
 int fts_apply(fts_ctx* ctx, int32_t precision, const double* x, double* y) {
     if (!ctx || !x || !y) return FTS_ERR_BAD_INPUT;
     Ctx& c = ctx->c;
+    if (c.matfree) return FTS_ERR_UNSUPPORTED;
     try {
         FTS_CUDA(cudaSetDevice(c.device));
         if (precision == FTS_PREC_MIXED && !c.have32) {

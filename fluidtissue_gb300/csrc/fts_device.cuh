@@ -147,6 +147,9 @@ struct Ctx {
     double* bicg = nullptr;              // scalars of the reference-algorithm BiCGSTAB
     int bicg_restarts = 0;
 
+    // operator representation: false = assembled BSR, true = element gather
+    bool matfree = false;
+
     // preconditioner
     bool use_mg = false;
     MG<double> mg64;
@@ -201,6 +204,10 @@ void launch_prepare_inner32(Ctx& c);       // r0_32 = r * scale
 void launch_update_x64(Ctx& c);            // x += d (FP64 inner)
 void launch_update_x_from32(Ctx& c);       // x += d32 / scale
 void launch_apply(Ctx& c, int precision, const V4<double>* in, V4<double>* out);
+// matrix-free operator (matfree.cu)
+void launch_mf_minres_A(Ctx& c, const V4<float>* Y, int ybuf, const V4<float>* R1, V4<float>* q);
+void launch_mf_residual64(Ctx& c);
+void launch_mf_pc(Ctx& c);
 // the reference's un-preconditioned BiCGSTAB on c.x (bicgstab.cu)
 long long bicgstab_solve(Ctx& c, double tol, long long maxit, double* err, int* status);
 template <typename T>

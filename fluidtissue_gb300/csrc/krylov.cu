@@ -108,6 +108,10 @@ __global__ void k_residual64(int64_t np, const int32_t* __restrict__ rowptr,
 }
 
 void launch_residual64(Ctx& c) {
+    if (c.matfree) {
+        launch_mf_residual64(c);
+        return;
+    }
     k_residual64<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(
         c.np, c.rowptr, c.cols, c.A64, c.x, c.b, reinterpret_cast<double*>(c.r), c.red, c.os);
     FTS_CUDA(cudaGetLastError());
@@ -437,8 +441,14 @@ long long minres_inner(Ctx& c, double rtol, long long maxit, double* achieved, i
             V4<T>* Wprev = w.W[p];
             V4<T>* Wcur = w.W[1 - p];
             if (timed) FTS_CUDA(cudaEventRecord(c.tev[2 * u], c.stream));
-            k_minres_A<T><<<ge, kThreads, 0, c.stream>>>(np, c.rowptr, c.cols, A, w.Y[yk], yk, R1,
-                                                         reinterpret_cast<T*>(w.q), c.red, c.ms);
+            if (sizeof(T) == 4 && c.matfree)
+                launch_mf_minres_A(c, reinterpret_cast<const V4<float>*>(w.Y[yk]), yk,
+                                   reinterpret_cast<const V4<float>*>(R1),
+                                   reinterpret_cast<V4<float>*>(w.q));
+            else
+                k_minres_A<T><<<ge, kThreads, 0, c.stream>>>(np, c.rowptr, c.cols, A, w.Y[yk], yk,
+                                                             R1, reinterpret_cast<T*>(w.q), c.red,
+                                                             c.ms);
             if (timed) FTS_CUDA(cudaEventRecord(c.tev[2 * u + 1], c.stream));
             launch_pc<T>(c, use_mg, 0, w.q, R1, R2, R1, w.Y[yn], yn);
             k_minres_C<T><<<gn, kThreads, 0, c.stream>>>(np, w.Y[yk], yk, Wprev, Wcur, w.X, c.red,

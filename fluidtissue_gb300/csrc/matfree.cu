@@ -1,0 +1,293 @@
+// Matrix-free element operator for the large single solve (operator_kind =
+// FTS_OP_MATFREE, mixed precision, Kuhn lattices with the multigrid
+// preconditioner).  No block matrix is stored: y = S x is gathered per node
+// over the elements around it (atomic-free, deterministic):
+//
+//   velocity row a, component r:
+//     mu V sum_c g_a[c] (G[r][c] + G[c][r])  -  V g_a[r] sum_b wq[b] p_b
+//   pressure row a:
+//     -wq[a] V div u  -  alpha h^2 V g_a . grad p  -  eps V sum_b mref[a][b] p_b
+//
+// with G[r][c] = sum_b u_{b,r} g_b[c] the element's velocity gradient — the
+// same weak forms the assembled blocks hold (src/growth/Flow.cpp:54-72,
+// :135-203, symmetric sign convention).  Dirichlet velocity rows are identity
+// and Dirichlet velocity values are read as zero.
+//
+// FP32 inner operator: element geometry recomputed in FP32 from the float
+// node coordinates (12 B per node, L2-resident) instead of streaming stored
+// geometry.  FP64 outer residual: the stored FP64 ElemGeom.
+#include <cfloat>
+
+#include "fts_device.cuh"
+#include "mg.cuh"
+#include "reduce.cuh"
+
+namespace fts {
+
+struct MfConst {
+    float wq[4];
+    float mref[4][4];
+    double wqd[4];
+    double mrefd[4][4];
+};
+
+static MfConst mf_const() {
+    RefConstants R = ref_constants();
+    MfConst m;
+    for (int i = 0; i < 4; ++i) {
+        m.wq[i] = (float)R.wq[i];
+        m.wqd[i] = R.wq[i];
+        for (int j = 0; j < 4; ++j) {
+            m.mref[i][j] = (float)R.mref[i][j];
+            m.mrefd[i][j] = R.mref[i][j];
+        }
+    }
+    return m;
+}
+
+// FP32 element geometry from float coordinates: gradients g[4][3], volume, h^2.
+__device__ __forceinline__ void geom_f32(const float* __restrict__ xyz, const int ids[4],
+                                         float g[4][3], float& vol, float& hh) {
+    float p[4][3];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) p[j][a] = __ldg(xyz + 3 * (int64_t)ids[j] + a);
+    float B[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        B[a][0] = p[1][a] - p[0][a];
+        B[a][1] = p[2][a] - p[0][a];
+        B[a][2] = p[3][a] - p[0][a];
+    }
+    const float c00 = B[1][1] * B[2][2] - B[1][2] * B[2][1];
+    const float c01 = B[1][2] * B[2][0] - B[1][0] * B[2][2];
+    const float c02 = B[1][0] * B[2][1] - B[1][1] * B[2][0];
+    const float det = B[0][0] * c00 + B[0][1] * c01 + B[0][2] * c02;
+    const float id = 1.0f / det;
+    float cof[3][3];
+    cof[0][0] = c00;
+    cof[0][1] = c01;
+    cof[0][2] = c02;
+    cof[1][0] = B[0][2] * B[2][1] - B[0][1] * B[2][2];
+    cof[1][1] = B[0][0] * B[2][2] - B[0][2] * B[2][0];
+    cof[1][2] = B[0][1] * B[2][0] - B[0][0] * B[2][1];
+    cof[2][0] = B[0][1] * B[1][2] - B[0][2] * B[1][1];
+    cof[2][1] = B[0][2] * B[1][0] - B[0][0] * B[1][2];
+    cof[2][2] = B[0][0] * B[1][1] - B[0][1] * B[1][0];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float i0 = cof[r][0] * id, i1 = cof[r][1] * id, i2 = cof[r][2] * id;
+        g[0][r] = -i0 - i1 - i2;
+        g[1][r] = i0;
+        g[2][r] = i1;
+        g[3][r] = i2;
+    }
+    const float adet = fabsf(det);
+    vol = adet * (1.0f / 6.0f);
+    const float h = cbrtf(adet);
+    hh = h * h;
+}
+
+// Row a of element k applied to the element's nodal values u[4][4] (ux,uy,uz,p).
+template <typename T>
+__device__ __forceinline__ void elem_row(const T g[4][3], T vol, T hh, T mu, int a,
+                                         const T u[4][4], T alpha, T eps, const T wq[4],
+                                         const T mref[4][4], T y[4]) {
+    T G[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            G[r][c] = u[0][r] * g[0][c] + u[1][r] * g[1][c] + u[2][r] * g[2][c] + u[3][r] * g[3][c];
+    T gp[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) gp[c] = u[0][3] * g[0][c] + u[1][3] * g[1][c] + u[2][3] * g[2][c] + u[3][3] * g[3][c];
+    const T pbar = wq[0] * u[0][3] + wq[1] * u[1][3] + wq[2] * u[2][3] + wq[3] * u[3][3];
+    const T mp = mref[a][0] * u[0][3] + mref[a][1] * u[1][3] + mref[a][2] * u[2][3] + mref[a][3] * u[3][3];
+    const T div = G[0][0] + G[1][1] + G[2][2];
+    const T mv = mu * vol;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+        y[r] += mv * (g[a][0] * (G[r][0] + G[0][r]) + g[a][1] * (G[r][1] + G[1][r]) +
+                      g[a][2] * (G[r][2] + G[2][r])) -
+                vol * g[a][r] * pbar;
+    y[3] += -wq[a] * vol * div - alpha * hh * vol * (g[a][0] * gp[0] + g[a][1] * gp[1] + g[a][2] * gp[2]) -
+            eps * vol * mp;
+}
+
+// q = S (y + ycorr e_p) / beta over nodes (FP32), fused MINRES dots v.q, v.r1.
+__global__ void __launch_bounds__(kThreads)
+k_mf_minres_A(int64_t np, const int32_t* __restrict__ p2t_ptr, const uint32_t* __restrict__ p2t,
+              const int32_t* __restrict__ tets, const float* __restrict__ xyz,
+              const double* __restrict__ mu, const uint8_t* __restrict__ bnd,
+              const V4<float>* __restrict__ Y, int ybuf, const V4<float>* __restrict__ R1,
+              V4<float>* __restrict__ q, float alpha, float eps, MfConst K, Reduction red,
+              MinresScalars* s) {
+    if (s->stop) return;
+    const float tinv = (float)(1.0 / s->beta);
+    const float wadd = (float)s->ycorr[ybuf];
+    double acc[2] = {0.0, 0.0};
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < np;
+         v += (int64_t)gridDim.x * blockDim.x) {
+        float y[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int32_t qq = p2t_ptr[v]; qq < p2t_ptr[v + 1]; ++qq) {
+            const uint32_t e = __ldg(p2t + qq);
+            const int64_t k = e >> 2;
+            const int a = e & 3;
+            const int4 t = __ldg(reinterpret_cast<const int4*>(tets) + k);
+            const int ids[4] = {t.x, t.y, t.z, t.w};
+            float g[4][3], vol, hh;
+            geom_f32(xyz, ids, g, vol, hh);
+            float u[4][4];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const V4<float> xv = Y[ids[b]];
+                const bool d = __ldg(bnd + ids[b]) != 0;
+                u[b][0] = d ? 0.f : xv.x;
+                u[b][1] = d ? 0.f : xv.y;
+                u[b][2] = d ? 0.f : xv.z;
+                u[b][3] = xv.w + wadd;
+            }
+            elem_row<float>(g, vol, hh, (float)__ldg(mu + k), a, u, alpha, eps, K.wq, K.mref, y);
+        }
+        const V4<float> yv = Y[v];
+        if (bnd[v]) {
+            y[0] = yv.x;
+            y[1] = yv.y;
+            y[2] = yv.z;
+        }
+        V4<float> o;
+        o.x = y[0] * tinv;
+        o.y = y[1] * tinv;
+        o.z = y[2] * tinv;
+        o.w = y[3] * tinv;
+        q[v] = o;
+        const V4<float> r1 = R1[v];
+        const float v0 = yv.x * tinv, v1 = yv.y * tinv, v2 = yv.z * tinv, v3 = (yv.w + wadd) * tinv;
+        acc[0] += (double)(v0 * o.x) + (double)(v1 * o.y) + (double)(v2 * o.z) + (double)(v3 * o.w);
+        acc[1] += (double)(v0 * r1.x) + (double)(v1 * r1.y) + (double)(v2 * r1.z) + (double)(v3 * r1.w);
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
+        const double c1 = s->iters >= 1 ? s->beta / s->oldb : 0.0;
+        s->alfa = tot[0] - c1 * tot[1];
+    }
+}
+
+// FP64 outer residual r = b - S x (stored FP64 geometry), ||r||^2, ||b||^2.
+__global__ void __launch_bounds__(kThreads)
+k_mf_residual64(int64_t np, const int32_t* __restrict__ p2t_ptr, const uint32_t* __restrict__ p2t,
+                const int32_t* __restrict__ tets, const ElemGeom* __restrict__ geom,
+                const double* __restrict__ mu, const uint8_t* __restrict__ bnd,
+                const V4<double>* __restrict__ x, const V4<double>* __restrict__ b,
+                V4<double>* __restrict__ r, double alpha, double eps, MfConst K, Reduction red,
+                OuterScalars* os) {
+    double acc[2] = {0.0, 0.0};
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < np;
+         v += (int64_t)gridDim.x * blockDim.x) {
+        double y[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int32_t qq = p2t_ptr[v]; qq < p2t_ptr[v + 1]; ++qq) {
+            const uint32_t e = __ldg(p2t + qq);
+            const int64_t k = e >> 2;
+            const int a = e & 3;
+            const int4 t = __ldg(reinterpret_cast<const int4*>(tets) + k);
+            const int ids[4] = {t.x, t.y, t.z, t.w};
+            const ElemGeom& G = geom[k];
+            double g[4][3];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) g[j][c] = G.g[j][c];
+            double u[4][4];
+#pragma unroll
+            for (int bb = 0; bb < 4; ++bb) {
+                const V4<double> xv = x[ids[bb]];
+                const bool d = __ldg(bnd + ids[bb]) != 0;
+                u[bb][0] = d ? 0.0 : xv.x;
+                u[bb][1] = d ? 0.0 : xv.y;
+                u[bb][2] = d ? 0.0 : xv.z;
+                u[bb][3] = xv.w;
+            }
+            elem_row<double>(g, G.vol, G.hh, mu[k], a, u, alpha, eps, K.wqd, K.mrefd, y);
+        }
+        const V4<double> xv = x[v];
+        if (bnd[v]) {
+            y[0] = xv.x;
+            y[1] = xv.y;
+            y[2] = xv.z;
+        }
+        const V4<double> bv = b[v];
+        V4<double> o;
+        o.x = bv.x - y[0];
+        o.y = bv.y - y[1];
+        o.z = bv.z - y[2];
+        o.w = bv.w - y[3];
+        r[v] = o;
+        acc[0] += o.x * o.x + o.y * o.y + o.z * o.z + o.w * o.w;
+        acc[1] += bv.x * bv.x + bv.y * bv.y + bv.z * bv.z + bv.w * bv.w;
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
+        os->rr = tot[0];
+        os->bb = tot[1];
+        os->scale = tot[0] > 0.0 ? 1.0 / sqrt(tot[0]) : 0.0;
+        os->nonfinite = isfinite(tot[0]) ? 0 : 1;
+    }
+}
+
+// Pressure weight of the preconditioner per node (the velocity part is the
+// multigrid V-cycle): 1 / (alpha D_ii + eps M_ii + sum_e vol/(4 mu_e)).
+__global__ void k_mf_pc(int64_t np, const int32_t* __restrict__ p2t_ptr,
+                        const uint32_t* __restrict__ p2t, const ElemGeom* __restrict__ geom,
+                        const double* __restrict__ mu, double alpha, double eps, MfConst K,
+                        float* __restrict__ pc) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < np;
+         v += (int64_t)gridDim.x * blockDim.x) {
+        double d = 0.0;
+        for (int32_t qq = p2t_ptr[v]; qq < p2t_ptr[v + 1]; ++qq) {
+            const uint32_t e = p2t[qq];
+            const int64_t k = e >> 2;
+            const int a = e & 3;
+            const ElemGeom& G = geom[k];
+            const double gg = G.g[a][0] * G.g[a][0] + G.g[a][1] * G.g[a][1] + G.g[a][2] * G.g[a][2];
+            d += alpha * G.hh * G.vol * gg + eps * G.vol * K.mrefd[a][a] + G.vol / (4.0 * mu[k]);
+        }
+        float* o = pc + 8 * v;
+        o[0] = 1.f;
+        o[1] = 0.f;
+        o[2] = 0.f;
+        o[3] = 1.f;
+        o[4] = 0.f;
+        o[5] = 1.f;
+        o[6] = (float)(1.0 / d);
+        o[7] = 0.f;
+    }
+}
+
+void launch_mf_minres_A(Ctx& c, const V4<float>* Y, int ybuf, const V4<float>* R1, V4<float>* q) {
+    static const MfConst K = mf_const();
+    k_mf_minres_A<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
+        c.np, c.p2t_ptr, c.p2t, c.tets, c.xyz, c.mu, c.bnd, Y, ybuf, R1, q, (float)c.par.alpha,
+        (float)c.par.eps, K, c.red, c.ms);
+    c.launches += 1;
+}
+
+void launch_mf_residual64(Ctx& c) {
+    static const MfConst K = mf_const();
+    k_mf_residual64<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
+        c.np, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.bnd, c.x, c.b, c.r, c.par.alpha,
+        c.par.eps, K, c.red, c.os);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+void launch_mf_pc(Ctx& c) {
+    static const MfConst K = mf_const();
+    k_mf_pc<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(c.np, c.p2t_ptr, c.p2t, c.geom, c.mu,
+                                                         c.par.alpha, c.par.eps, K, c.pc32);
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
+}  // namespace fts

@@ -134,6 +134,55 @@ __global__ void k_mg_extract(int n, const int32_t* __restrict__ rowptr,
     }
 }
 
+// Fine level straight from the elements (matrix-free mode: no block matrix
+// exists).  One thread per (node v, stored direction d): the 3x3 block
+// K(v, v + off[d]) = sum over elements holding both nodes of
+// mu vol (delta_rc g_a.g_b + g_a[c] g_b[r]) (Flow.cpp:136-153); Dirichlet rows
+// identity, Dirichlet columns zero.
+template <typename T>
+__global__ void k_mg_from_elements(int n, const int32_t* __restrict__ p2t_ptr,
+                                   const uint32_t* __restrict__ p2t,
+                                   const int32_t* __restrict__ tets,
+                                   const ElemGeom* __restrict__ geom,
+                                   const double* __restrict__ mu,
+                                   const uint8_t* __restrict__ bnd, T* __restrict__ K) {
+    const int64_t N = (int64_t)n * n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * 8;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int d = (int)(t / N);
+        const int64_t v = t - d * N;
+        const int i = (int)(v % n), j = (int)((v / n) % n), k = (int)(v / ((int64_t)n * n));
+        const int w = nbr(i, j, k, d, n);
+        double blk[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (bnd[v]) {
+            if (d == 0) blk[0] = blk[4] = blk[8] = 1.0;
+        } else if (w >= 0 && !bnd[w]) {
+            for (int32_t q = p2t_ptr[v]; q < p2t_ptr[v + 1]; ++q) {
+                const uint32_t e = p2t[q];
+                const int64_t el = e >> 2;
+                const int a = e & 3;
+                const int4 tt = reinterpret_cast<const int4*>(tets)[el];
+                const int ids[4] = {tt.x, tt.y, tt.z, tt.w};
+                int b = -1;
+#pragma unroll
+                for (int m = 0; m < 4; ++m)
+                    if (ids[m] == w) b = m;
+                if (b < 0) continue;
+                const ElemGeom& G = geom[el];
+                const double mv = mu[el] * G.vol;
+                const double gg = G.g[a][0] * G.g[b][0] + G.g[a][1] * G.g[b][1] + G.g[a][2] * G.g[b][2];
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int cc = 0; cc < 3; ++cc)
+                        blk[3 * r + cc] += mv * ((r == cc ? gg : 0.0) + G.g[a][cc] * G.g[b][r]);
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < 9; ++e) K[kidx(d * 9 + e, v)] = (T)blk[e];
+    }
+}
+
 // Dirichlet mask of a coarse level: node I is Dirichlet when the fine node 2I is.
 __global__ void k_mg_coarse_mask(int nf, const uint8_t* __restrict__ mf, int nc,
                                  uint8_t* __restrict__ mc) {
@@ -547,8 +596,12 @@ template <typename T>
 void mg_setup(Ctx& c, MG<T>& mg) {
     mg_build<T>(c, mg);
     MGLevel<T>& F = mg.L[0];
-    k_mg_extract<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(F.n, c.rowptr, c.cols,
-                                                                       c.A64, F.K);
+    if (c.matfree)
+        k_mg_from_elements<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
+            F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.bnd, F.K);
+    else
+        k_mg_extract<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(F.n, c.rowptr, c.cols,
+                                                                           c.A64, F.K);
     c.launches += 1;
     for (size_t l = 0; l < mg.L.size(); ++l) {
         MGLevel<T>& L = mg.L[l];

@@ -1,0 +1,55 @@
+"""Matrix-free element operator (operator_kind = FTS_OP_MATFREE): the same
+solution as the assembled path and the oracle, within the mixed-precision bar."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import workload
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n", [17, 33])
+def test_matfree_matches_assembled_and_oracle(n):
+    import oracle as O
+    from fluidtissue_gb300.flow import Flow, Mesh
+    inst = workload("spheres257", n)
+    par = dict(inst.params)
+    par["Stokes tolerance"] = 1e-10
+    flows = {}
+    for op in ("matfree", "assembled"):
+        f = Flow()
+        assert f.init(Mesh(inst.xyz, inst.tets), par, precision="mixed", operator=op,
+                      warm_start=False) == 0, f.last_error()
+        flow = np.zeros(4 * inst.np)
+        rc = f.solve(inst.phi, inst.source, flow, mu=inst.mu)
+        assert rc == 0, f.last_error()
+        assert f.last_stats["rel_residual"] <= 1e-10
+        flows[op] = flow
+        f.close()
+    npn = inst.np
+    rel = lambda a, b, s: np.linalg.norm(a[s] - b[s]) / np.linalg.norm(b[s])  # noqa: E731
+    vel, prs = slice(0, 3 * npn), slice(3 * npn, 4 * npn)
+    assert rel(flows["matfree"], flows["assembled"], vel) <= 1e-7
+    if n == 17:
+        R, _, _, mu = O.system(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source,
+                               inst.mu, par)
+        x, tr, _ = O.solve_tight(R, inst.xyz, inst.tets, mu, tol=1e-13)
+        ref = O.scatter(R, x)
+        assert rel(flows["matfree"], ref, vel) <= 1e-7
+        assert rel(flows["matfree"], ref, prs) <= 1e-7
+
+
+def test_matfree_refuses_fp64_and_inspection():
+    from fluidtissue_gb300.flow import Flow, Mesh
+    inst = workload("spheres257", 9)
+    f = Flow()
+    assert f.init(Mesh(inst.xyz, inst.tets), inst.params, precision="fp64",
+                  operator="matfree") == 6
+    f = Flow()
+    assert f.init(Mesh(inst.xyz, inst.tets), inst.params, precision="mixed",
+                  operator="matfree") == 0
+    with pytest.raises(Exception):
+        f.system()
+    f.close()
