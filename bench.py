@@ -371,41 +371,47 @@ def run_batch(args):
 
 
 def cpu_baseline(inst, seconds: float) -> dict:
-    """The oracle (restated reference: row-gather assembly + un-preconditioned
-    BiCGSTAB, OpenMP) on this host's cores, bounded to ~``seconds``: full
-    assembly plus as many BiCGSTAB iterations as fit; solves/s extrapolated
-    with the reference algorithm's iteration count to 1e-8 on this workload."""
+    """The CPU oracle on this host's cores (OpenMP, FP64), bounded to about
+    ``seconds``: the restated reference assembly (row gather, block
+    composition, restriction to the reduced system) in full, plus a sample of
+    preconditioned MINRES iterations with the block-Jacobi + rank-one
+    preconditioner of the GPU's Jacobi mode.  The reference's own
+    un-preconditioned BiCGSTAB does not converge on this workload (see
+    profiles/cpu_baseline.md), so the CPU baseline uses the oracle's
+    preconditioned method; solves/s = 1 / (t_assembly + N t_iteration) with N
+    the iterations that method needs to the tolerance (measured with the same
+    FP64 method on the GPU, profiles/cpu_baseline.md)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as O
     threads = O.num_threads()
     t0 = time.perf_counter()
-    R, _, _, _ = O.system(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source, inst.mu,
-                          inst.params)
+    R, _, _, mu = O.system(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source, inst.mu,
+                           inst.params)
+    pre = O.block_jacobi(R, inst.xyz, inst.tets, mu, inst.params["eps"])
     t_asm = time.perf_counter() - t0
     it = 8
-    t_it = None
     while True:
         t1 = time.perf_counter()
-        O.bicgstab(R, None, tol=1e-30, maxit=it)
+        _, _, done = O.minres_blockjacobi(R, pre, rtol=1e-30, maxit=it)
         t_run = time.perf_counter() - t1
-        t_it = t_run / it
-        if t_asm + t_run > seconds * 0.5 or it >= 4096:
+        t_it = t_run / max(done, 1)
+        if t_asm + t_run > seconds * 0.5 or it >= 8192:
             break
         it *= 2
-    n_ref = REFERENCE_ITERATIONS.get(inst.name)
-    value = 1.0 / (t_asm + n_ref * t_it) if n_ref else None
+    n_it = CPU_BASELINE_ITERATIONS.get(inst.name)
+    value = 1.0 / (t_asm + n_it * t_it) if n_it else None
     return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": (f"oracle on {inst.name}: full assembly ({t_asm:.2f} s) + {it} BiCGSTAB "
-                       f"iterations ({t_it * 1e3:.1f} ms each); solves/s = 1/(t_asm + "
-                       f"N_ref t_iter) with N_ref = {n_ref} (reference BiCGSTAB iterations "
-                       f"to the tolerance, profiles/reference_iterations.md)"),
+            "sample": (f"oracle on {inst.name} ({threads} threads): full assembly + "
+                       f"preconditioner set-up ({t_asm:.2f} s) + {done} block-Jacobi MINRES "
+                       f"iterations ({t_it * 1e3:.1f} ms each); solves/s = 1/(t_asm + N t_iter) "
+                       f"with N = {n_it} iterations of the same FP64 method to tol "
+                       f"{inst.params['Stokes tolerance']} (profiles/cpu_baseline.md)"),
             "t_assembly_s": t_asm, "t_iteration_s": t_it}
 
 
-# Iterations the reference's un-preconditioned BiCGSTAB needs to reach the
-# workload tolerance (measured with the GPU implementation of that algorithm;
-# see profiles/reference_iterations.md).  None = not yet measured.
-REFERENCE_ITERATIONS: dict = {}
+# Iterations of FP64 block-Jacobi + rank-one MINRES to the workload tolerance
+# (profiles/cpu_baseline.md): the CPU baseline's iteration count.
+CPU_BASELINE_ITERATIONS: dict = {}
 
 
 def run_reference(args):

@@ -1,9 +1,11 @@
 // C ABI of libfts (include/fts.h): context lifecycle and the Stokes solve
 // pipeline, the GB300 counterpart of Flow::init / Flow::solve
 // (src/growth/Flow.cpp:20-94, :218-302).
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <vector>
 #include <cstring>
 #include <exception>
 #include <new>
@@ -14,7 +16,8 @@ namespace fts {
 
 void free_all(Ctx& c) {
     void* ptrs[] = {c.xyz, c.tets, c.bnd, c.rowptr, c.cols, c.diag, c.p2t_ptr, c.p2t, c.geom,
-                    c.phi, c.src, c.force, c.mu, c.s, c.flow, c.A64, c.A32, c.pc64, c.pc32,
+                    c.phi, c.src, c.force, c.mu, c.s, c.flow, c.A64, c.A32, c.ell_val,
+                    c.ell_col, c.ell_ptr, c.pc64, c.pc32,
                     c.b, c.x, c.r, c.w64.q, c.w64.R[0], c.w64.R[1], c.w64.Y[0], c.w64.Y[1],
                     c.w64.W[0], c.w64.W[1], c.w64.X, c.w32.q, c.w32.R[0], c.w32.R[1],
                     c.w32.Y[0], c.w32.Y[1], c.w32.W[0], c.w32.W[1], c.w32.X, c.w32.r0, c.ms,
@@ -42,9 +45,43 @@ static void alloc_work(Ctx& c, KrylovWork<T>& w, bool own_r0) {
     if (own_r0) w.r0 = dev_alloc<V4<T>>(c, c.np);
 }
 
+// Sliced-ELL structure (host) of the block graph: slices of 8 rows padded to
+// the longest row of the slice.
+static void build_ell(Ctx& c) {
+    const HostTopology& T = c.topo;
+    c.nslices = (c.np + 7) / 8;
+    std::vector<int32_t> ptr((size_t)c.nslices + 1, 0);
+    for (int64_t s = 0; s < c.nslices; ++s) {
+        int32_t kmax = 0;
+        for (int64_t r = 8 * s; r < std::min<int64_t>(c.np, 8 * s + 8); ++r)
+            kmax = std::max(kmax, T.rowptr[r + 1] - T.rowptr[r]);
+        ptr[s + 1] = ptr[s] + 8 * kmax;
+    }
+    c.ell_slots = ptr[c.nslices];
+    std::vector<int32_t> col((size_t)c.ell_slots, 0);
+    for (int64_t s = 0; s < c.nslices; ++s) {
+        const int32_t kmax = (ptr[s + 1] - ptr[s]) / 8;
+        for (int l = 0; l < 8; ++l) {
+            const int64_t r = 8 * s + l;
+            const int32_t len = r < c.np ? T.rowptr[r + 1] - T.rowptr[r] : 0;
+            for (int32_t k = 0; k < kmax; ++k)
+                col[ptr[s] + 8 * k + l] = k < len ? T.cols[T.rowptr[r] + k] : 0;
+        }
+    }
+    c.ell_ptr = dev_alloc<int32_t>(c, (size_t)c.nslices + 1);
+    c.ell_col = dev_alloc<int32_t>(c, (size_t)c.ell_slots);
+    c.ell_val = dev_alloc<float>(c, (size_t)c.ell_slots * 16);
+    FTS_CUDA(cudaMemcpy(c.ell_ptr, ptr.data(), ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    FTS_CUDA(cudaMemcpy(c.ell_col, col.data(), col.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    c.use_ell = true;
+}
+
 void ensure_fp32(Ctx& c) {
     if (c.have32) return;
-    if (!c.matfree) c.A32 = dev_alloc<float>(c, (size_t)c.nnzb * 16);
+    if (!c.matfree) {
+        if (c.in_batch) c.A32 = dev_alloc<float>(c, (size_t)c.nnzb * 16);
+        else build_ell(c);
+    }
     c.pc32 = dev_alloc<float>(c, (size_t)c.np * 8);
     alloc_work<float>(c, c.w32, true);
     c.have32 = true;
@@ -79,21 +116,32 @@ int validate_params(const fts_params& p, std::string& err) {
 }
 
 // Multigrid needs the Kuhn lattice structure and at least three levels
-// (odd n >= 9); otherwise node 3x3 block Jacobi.
+// (n >= 9); for even n every node on the last layer of each axis must be a
+// Dirichlet node (the coarse lattice's last layer sits there).
 static int mg_levels(int n) {
     int l = 1;
-    while (n % 2 == 1 && n >= 5) {
-        n = (n + 1) / 2;
+    while (n >= 5) {
+        n = mg_coarse_n(n);
         ++l;
     }
     return l;
 }
 
+static bool last_layers_dirichlet(const HostTopology& T, int n) {
+    for (int64_t v = 0; v < T.np; ++v) {
+        const int64_t i = v % n, j = (v / n) % n, k = v / ((int64_t)n * n);
+        if ((i == n - 1 || j == n - 1 || k == n - 1) && !T.bnd[v]) return false;
+    }
+    return true;
+}
+
 static void configure_preconditioner(Ctx& c) {
     const int n = c.topo.lattice_n;
-    const bool mg_ok = n > 0 && n % 2 == 1 && mg_levels(n) >= 3;
+    const bool mg_ok = n > 0 && mg_levels(n) >= 3 &&
+                       (n % 2 == 1 || last_layers_dirichlet(c.topo, n));
     if (c.par.preconditioner == FTS_PC_MULTIGRID && !mg_ok) {
-        c.last_error = "multigrid needs a Kuhn lattice mesh with odd n >= 9";
+        c.last_error = "multigrid needs a Kuhn lattice mesh with n >= 9 (even n: Dirichlet "
+                       "nodes on the last layer of every axis)";
         throw (int)FTS_ERR_UNSUPPORTED;
     }
     c.use_mg = mg_ok && c.par.preconditioner != FTS_PC_JACOBI;
@@ -433,6 +481,14 @@ const char* fts_last_error(const fts_ctx* ctx) {
 }
 
 int fts_create(const fts_mesh* mesh, const fts_params* params, fts_ctx** out) {
+    return fts::create_context(mesh, params, out, false);
+}
+
+}  // extern "C"
+
+namespace fts {
+
+int create_context(const fts_mesh* mesh, const fts_params* params, fts_ctx** out, bool in_batch) {
     if (!mesh || !out) {
         g_create_error = "null mesh or output pointer";
         return FTS_ERR_BAD_INPUT;
@@ -456,6 +512,7 @@ int fts_create(const fts_mesh* mesh, const fts_params* params, fts_ctx** out) {
             delete h;
             return rc;
         }
+        h->c.in_batch = in_batch;
         create(h->c, *mesh, p);
     } catch (const CudaError& e) {
         g_create_error = e.what;
@@ -476,6 +533,10 @@ int fts_create(const fts_mesh* mesh, const fts_params* params, fts_ctx** out) {
     *out = h;
     return FTS_OK;
 }
+
+}  // namespace fts
+
+extern "C" {
 
 static int solve_common(fts_ctx* ctx, const double* phi, const double* source, const double* mu,
                         const double* force, double* flow, fts_stats* stats, bool device) {

@@ -438,8 +438,40 @@ __global__ void k_to_f32(int64_t n, const double* __restrict__ in, float* __rest
     }
 }
 
+// FP64 BSR -> FP32 sliced ELL: one warp per slice of 8 block rows; lane l
+// handles row 8s + l/4, block row r = l%4, so every k writes 512 contiguous bytes.
+__global__ void k_to_ell(int64_t np, int64_t nslices, const int32_t* __restrict__ rowptr,
+                         const double* __restrict__ A, const int32_t* __restrict__ ell_ptr,
+                         float* __restrict__ ell_val) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; s < nslices;
+         s += warps) {
+        const int32_t p0 = ell_ptr[s];
+        const int32_t kmax = (ell_ptr[s + 1] - p0) >> 3;
+        const int64_t row = 8 * s + (lane >> 2);
+        const int r = lane & 3;
+        const int32_t b0 = row < np ? rowptr[row] : 0;
+        const int32_t len = row < np ? rowptr[row + 1] - b0 : 0;
+        for (int32_t k = 0; k < kmax; ++k) {
+            float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k < len) {
+                const double* a = A + (int64_t)(b0 + k) * 16 + r * 4;
+                const double2 a01 = *reinterpret_cast<const double2*>(a);
+                const double2 a23 = *reinterpret_cast<const double2*>(a + 2);
+                o = make_float4((float)a01.x, (float)a01.y, (float)a23.x, (float)a23.y);
+            }
+            reinterpret_cast<float4*>(ell_val)[((int64_t)p0 + 8 * k + (lane >> 2)) * 4 + r] = o;
+        }
+    }
+}
+
 void launch_to_f32(Ctx& c) {
-    k_to_f32<<<grid_for(c, c.nnzb * 8), kThreads, 0, c.stream>>>(c.nnzb * 16, c.A64, c.A32);
+    if (c.use_ell)
+        k_to_ell<<<grid_for(c, c.nslices * 32), kThreads, 0, c.stream>>>(
+            c.np, c.nslices, c.rowptr, c.A64, c.ell_ptr, c.ell_val);
+    else
+        k_to_f32<<<grid_for(c, c.nnzb * 8), kThreads, 0, c.stream>>>(c.nnzb * 16, c.A64, c.A32);
     k_to_f32<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(c.np * 8, c.pc64, c.pc32);
     FTS_CUDA(cudaGetLastError());
     c.launches += 2;

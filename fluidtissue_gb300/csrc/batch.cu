@@ -886,7 +886,7 @@ int fts_batch_create(int32_t count, const fts_mesh* meshes, const fts_params* pa
             }
             p.preconditioner = FTS_PC_JACOBI;  // the persistent kernel applies block Jacobi
             fts_ctx* c = nullptr;
-            rc = fts_create(&meshes[i], &p, &c);
+            rc = create_context(&meshes[i], &p, &c, true);
             if (rc != FTS_OK) {
                 B->last_error = std::string("instance ") + std::to_string(i) + ": " +
                                 fts_last_error(nullptr);

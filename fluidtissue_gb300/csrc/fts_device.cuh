@@ -10,6 +10,8 @@
 #include "fts_internal.h"
 #include "mg.cuh"
 
+struct fts_ctx;
+
 namespace fts {
 
 #define FTS_CUDA(call)                                                        \
@@ -127,7 +129,16 @@ struct Ctx {
 
     // system
     double* A64 = nullptr;
-    float* A32 = nullptr;
+    float* A32 = nullptr;     // FP32 BSR copy (batch instances)
+    // FP32 sliced-ELL copy (single solves): slices of 8 block rows; the k-th
+    // blocks of a slice are contiguous (8 x 64 B), padding points at node 0
+    // with zero values
+    float* ell_val = nullptr;   // [slots * 16]
+    int32_t* ell_col = nullptr; // [slots]
+    int32_t* ell_ptr = nullptr; // [nslices + 1] first slot of each slice
+    int64_t nslices = 0, ell_slots = 0;
+    bool use_ell = false;
+    bool in_batch = false;
     double* pc64 = nullptr;   // 8 per node: inverse of the 3x3 velocity block (xx,xy,xz,yy,yz,zz),
     float* pc32 = nullptr;    // inverse pressure weight, pad
     V4<double>* b = nullptr;
@@ -177,6 +188,7 @@ struct Ctx {
 
 // ---- context lifecycle (api.cu) -------------------------------------------
 void create(Ctx& c, const fts_mesh& m, const fts_params& p);   // throws CudaError / int
+int create_context(const fts_mesh* mesh, const fts_params* params, fts_ctx** out, bool in_batch);
 void free_all(Ctx& c);
 int validate_params(const fts_params& p, std::string& err);
 void ensure_fp32(Ctx& c);

@@ -63,13 +63,45 @@ __global__ void k_cast_f2d(int64_t n, const float* __restrict__ a, double* __res
         b[i] = (double)a[i];
 }
 
+__global__ void k_apply_ell(int64_t np, int64_t nslices, const int32_t* __restrict__ ell_ptr,
+                            const int32_t* __restrict__ ell_col, const float* __restrict__ ell_val,
+                            const V4<float>* __restrict__ in, float* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int r = lane & 3;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t sl = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; sl < nslices;
+         sl += warps) {
+        const int32_t p0 = ell_ptr[sl];
+        const int32_t kmax = (ell_ptr[sl + 1] - p0) >> 3;
+        float ax = 0.f;
+        for (int32_t k = 0; k < kmax; ++k) {
+            const int64_t slot = (int64_t)p0 + (lane >> 2) + 8 * k;
+            const int32_t j = ell_col[slot];
+            const float4 a = reinterpret_cast<const float4*>(ell_val)[slot * 4 + r];
+            const V4<float> xj = in[j];
+            ax = fmaf(a.x, xj.x, ax);
+            ax = fmaf(a.y, xj.y, ax);
+            ax = fmaf(a.z, xj.z, ax);
+            ax = fmaf(a.w, xj.w, ax);
+        }
+        const int64_t row = 8 * sl + (lane >> 2);
+        if (row < np) out[row * 4 + r] = ax;
+    }
+}
+
 void launch_apply(Ctx& c, int precision, const V4<double>* in, V4<double>* out) {
     int grid = grid_for(c, c.np * 4);
     if (precision == FTS_PREC_MIXED) {
         k_cast_d2f<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(
             c.np * 4, reinterpret_cast<const double*>(in), reinterpret_cast<float*>(c.w32.q));
-        k_apply<float><<<grid, kThreads, 0, c.stream>>>(c.np, c.rowptr, c.cols, c.A32, c.w32.q,
-                                                        reinterpret_cast<float*>(c.w32.r0));
+        if (c.use_ell)
+            k_apply_ell<<<grid_for(c, c.nslices * 32), kThreads, 0, c.stream>>>(
+                c.np, c.nslices, c.ell_ptr, c.ell_col, c.ell_val, c.w32.q,
+                reinterpret_cast<float*>(c.w32.r0));
+        else
+            k_apply<float><<<grid, kThreads, 0, c.stream>>>(c.np, c.rowptr, c.cols, c.A32,
+                                                            c.w32.q,
+                                                            reinterpret_cast<float*>(c.w32.r0));
         k_cast_f2d<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(
             c.np * 4, reinterpret_cast<const float*>(c.w32.r0), reinterpret_cast<double*>(out));
     } else {
@@ -237,6 +269,56 @@ k_minres_A(int64_t np, const int32_t* __restrict__ rowptr, const int32_t* __rest
         const T ve = (y[e] + (r == 3 ? wadd : T(0))) * tinv;
         acc[0] += (double)(ve * qv);
         acc[1] += (double)(ve * r1[e]);
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
+        const double c1 = s->iters >= 1 ? s->beta / s->oldb : 0.0;
+        s->alfa = tot[0] - c1 * tot[1];
+    }
+}
+
+// A on the FP32 sliced-ELL copy: one warp per slice of 8 block rows, lane l =
+// (row 8s + l/4, block row l%4); the k-th blocks of the slice are one
+// contiguous 512-byte segment.
+__global__ void __launch_bounds__(kThreads)
+k_minres_A_ell(int64_t np, int64_t nslices, const int32_t* __restrict__ ell_ptr,
+               const int32_t* __restrict__ ell_col, const float* __restrict__ ell_val,
+               const V4<float>* __restrict__ Y, int ybuf, const V4<float>* __restrict__ R1,
+               float* __restrict__ q, Reduction red, MinresScalars* s) {
+    if (s->stop) return;
+    const float tinv = (float)(1.0 / s->beta);
+    const float wadd = (float)s->ycorr[ybuf];
+    const int lane = threadIdx.x & 31;
+    const int r = lane & 3;
+    const float* y = reinterpret_cast<const float*>(Y);
+    const float* r1 = reinterpret_cast<const float*>(R1);
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double acc[2] = {0.0, 0.0};
+    for (int64_t sl = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; sl < nslices;
+         sl += warps) {
+        const int32_t p0 = ell_ptr[sl];
+        const int32_t kmax = (ell_ptr[sl + 1] - p0) >> 3;
+        const int64_t slot0 = (int64_t)p0 + (lane >> 2);
+        float ax = 0.f;
+        for (int32_t k = 0; k < kmax; ++k) {
+            const int64_t slot = slot0 + 8 * k;
+            const int32_t j = __ldg(ell_col + slot);
+            const float4 a = __ldg(reinterpret_cast<const float4*>(ell_val) + slot * 4 + r);
+            const V4<float> xj = Y[j];
+            ax = fmaf(a.x, xj.x, ax);
+            ax = fmaf(a.y, xj.y, ax);
+            ax = fmaf(a.z, xj.z, ax);
+            ax = fmaf(a.w, xj.w + wadd, ax);
+        }
+        const int64_t row = 8 * sl + (lane >> 2);
+        if (row < np) {
+            const float qv = ax * tinv;
+            const int64_t e = row * 4 + r;
+            q[e] = qv;
+            const float ve = (y[e] + (r == 3 ? wadd : 0.f)) * tinv;
+            acc[0] += (double)(ve * qv);
+            acc[1] += (double)(ve * r1[e]);
+        }
     }
     double tot[2];
     if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
@@ -445,6 +527,12 @@ long long minres_inner(Ctx& c, double rtol, long long maxit, double* achieved, i
                 launch_mf_minres_A(c, reinterpret_cast<const V4<float>*>(w.Y[yk]), yk,
                                    reinterpret_cast<const V4<float>*>(R1),
                                    reinterpret_cast<V4<float>*>(w.q));
+            else if (sizeof(T) == 4 && c.use_ell)
+                k_minres_A_ell<<<grid_for(c, c.nslices * 32), kThreads, 0, c.stream>>>(
+                    np, c.nslices, c.ell_ptr, c.ell_col, c.ell_val,
+                    reinterpret_cast<const V4<float>*>(w.Y[yk]), yk,
+                    reinterpret_cast<const V4<float>*>(R1), reinterpret_cast<float*>(w.q),
+                    c.red, c.ms);
             else
                 k_minres_A<T><<<ge, kThreads, 0, c.stream>>>(np, c.rowptr, c.cols, A, w.Y[yk], yk,
                                                              R1, reinterpret_cast<T*>(w.q), c.red,

@@ -5,7 +5,10 @@
 // Structure.  On an n^3 Kuhn lattice (n odd) the coarse lattice is every other
 // node; each fine node is either a coarse node or the midpoint of a coarse
 // Kuhn edge, so the prolongation P is linear interpolation with weights 1 or
-// 1/2 along the 14 Kuhn directions.  The Galerkin operator P^T K P keeps the
+// 1/2 along the 14 Kuhn directions.  For even n the coarse lattice has n/2 + 1
+// nodes per axis and its last layer sits on the fine boundary layer n - 1;
+// those nodes are Dirichlet (their rows and columns of P vanish), so the same
+// index formulas give the exact Galerkin operator on every interior node.  The Galerkin operator P^T K P keeps the
 // 15-point Kuhn stencil.  K is symmetric, so every level stores only the self
 // block and the 7 positive-direction 3x3 blocks per node (72 values) in tiles
 // of 32 nodes: K[((node/32)*72 + 9d + 3r + c)*32 + node%32]; the block in the
@@ -190,7 +193,10 @@ __global__ void k_mg_coarse_mask(int nf, const uint8_t* __restrict__ mf, int nc,
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < Nc;
          v += (int64_t)gridDim.x * blockDim.x) {
         int i = (int)(v % nc), j = (int)((v / nc) % nc), k = (int)(v / ((int64_t)nc * nc));
-        mc[v] = mf[(2 * i) + nf * ((2 * j) + (int64_t)nf * (2 * k))];
+        // coarse node I sits on fine node min(2I, nf-1): for even nf the last
+        // coarse layer is the fine boundary layer
+        const int fi = min(2 * i, nf - 1), fj = min(2 * j, nf - 1), fk = min(2 * k, nf - 1);
+        mc[v] = mf[fi + nf * (fj + (int64_t)nf * fk)];
     }
 }
 
@@ -574,8 +580,8 @@ void mg_build(Ctx& c, MG<T>& mg) {
         for (auto** p : {&L.b, &L.x, &L.r, &L.d0, &L.d1}) *p = dev_alloc<T>(c, (size_t)L.N * 3);
         L.mask = dev_alloc<uint8_t>(c, (size_t)L.N);
         mg.L.push_back(L);
-        if (n % 2 == 0 || n < 5) break;
-        n = (n + 1) / 2;
+        if (n < 5) break;
+        n = mg_coarse_n(n);
     }
     mg.lam = dev_alloc<double>(c, mg.L.size() + 1);
     mg.coef = dev_alloc<double>(c, mg.L.size() * kCoefStride);

@@ -36,6 +36,9 @@ struct MG {
     bool built = false;
 };
 
+// Nodes per axis of the next coarser lattice.
+inline int mg_coarse_n(int n) { return n % 2 ? (n + 1) / 2 : n / 2 + 1; }
+
 template <typename T>
 void mg_setup(Ctx& c, MG<T>& mg);
 template <typename T>

@@ -699,6 +699,93 @@ double ora_minres_tight(int64_t N, int64_t nI, const int64_t* rp, const int32_t*
     return tr;
 }
 
+// MINRES with the block-diagonal preconditioner of the GPU's Jacobi mode, on
+// the symmetric form of the reduced system (used as the CPU baseline): for
+// interior node m the 3x3 velocity block of rows (m, nI+m, 2nI+m) is inverted
+// (vinv6[6m..]: xx xy xz yy yz zz), pressure row k is weighted by pinv[k], and
+// the rank-one term crank * sum(r_p) is added to every pressure component.
+// Runs at most maxit iterations from x (no restarts); returns the
+// preconditioned residual reduction phibar / beta1.
+double ora_minres_blockjacobi(int64_t N, int64_t nI, const int64_t* rp, const int32_t* ci,
+                              const double* v, const double* b, const double* vinv6,
+                              const double* pinv, double crank, double* x, double rtol,
+                              int64_t maxit, int64_t* iters_out) {
+    std::vector<double> r1(N), r2(N), y(N), vv(N), w(N, 0.0), w1(N, 0.0), w2(N, 0.0);
+    const int64_t np = N - 3 * nI;
+    auto apply = [&](const double* in, double* out) {
+        spmv(N, rp, ci, v, in, out);
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 3 * nI; q < N; ++q) out[q] = -out[q];
+    };
+    auto prec = [&](const double* in, double* out) {
+#pragma omp parallel for schedule(static)
+        for (int64_t m = 0; m < nI; ++m) {
+            const double* B = vinv6 + 6 * m;
+            const double a0 = in[m], a1 = in[nI + m], a2 = in[2 * nI + m];
+            out[m] = B[0] * a0 + B[1] * a1 + B[2] * a2;
+            out[nI + m] = B[1] * a0 + B[3] * a1 + B[4] * a2;
+            out[2 * nI + m] = B[2] * a0 + B[4] * a1 + B[5] * a2;
+        }
+        double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+        for (int64_t k = 0; k < np; ++k) s += in[3 * nI + k];
+#pragma omp parallel for schedule(static)
+        for (int64_t k = 0; k < np; ++k) out[3 * nI + k] = pinv[k] * in[3 * nI + k] + crank * s;
+    };
+    apply(x, r1.data());
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < N; ++q) r1[q] = (q < 3 * nI ? b[q] : -b[q]) - r1[q];
+    r2 = r1;
+    prec(r1.data(), y.data());
+    const double beta1 = std::sqrt(dot(N, r1.data(), y.data()));
+    double oldb = 0.0, beta = beta1, dbar = 0.0, epsln = 0.0, phibar = beta1, cs = -1.0, sn = 0.0;
+    int64_t it = 0;
+    while (it < maxit && phibar > rtol * beta1 && beta1 > 0.0) {
+        ++it;
+        const double s = 1.0 / beta;
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < N; ++q) vv[q] = s * y[q];
+        apply(vv.data(), y.data());
+        if (it >= 2) {
+            const double f = beta / oldb;
+#pragma omp parallel for schedule(static)
+            for (int64_t q = 0; q < N; ++q) y[q] -= f * r1[q];
+        }
+        const double alfa = dot(N, vv.data(), y.data());
+        const double f2 = alfa / beta;
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < N; ++q) {
+            y[q] -= f2 * r2[q];
+            r1[q] = r2[q];
+            r2[q] = y[q];
+        }
+        prec(r2.data(), y.data());
+        oldb = beta;
+        beta = std::sqrt(dot(N, r2.data(), y.data()));
+        const double oldeps = epsln;
+        const double delta = cs * dbar + sn * alfa;
+        const double gbar = sn * dbar - cs * alfa;
+        epsln = sn * beta;
+        dbar = -cs * beta;
+        double gamma = std::sqrt(gbar * gbar + beta * beta);
+        if (gamma < DBL_MIN) gamma = DBL_MIN;
+        cs = gbar / gamma;
+        sn = beta / gamma;
+        const double phi = cs * phibar;
+        phibar = sn * phibar;
+        const double ig = 1.0 / gamma;
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < N; ++q) {
+            const double wn = (vv[q] - oldeps * w1[q] - delta * w2[q]) * ig;
+            w1[q] = w2[q];
+            w2[q] = wn;
+            x[q] += phi * wn;
+        }
+    }
+    if (iters_out) *iters_out = it;
+    return beta1 > 0.0 ? phibar / beta1 : 0.0;
+}
+
 // Scatter of the reduced solution to flow = [ux(np), uy(np), uz(np), p(np)],
 // zero on boundary velocity dofs (Flow.cpp:290-300).
 int ora_scatter(int64_t np, int64_t N, const int32_t* sidx, const double* x, double* flow) {

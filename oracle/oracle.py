@@ -66,6 +66,8 @@ def lib():
         "ora_now_ms": (dbl, []),
         "ora_minres_tight": (dbl, [i64, i64, _p(i64), _p(i32), _p(dbl), _p(dbl), _p(dbl),
                                    _p(dbl), dbl, i64, C.c_int, _p(i64)]),
+        "ora_minres_blockjacobi": (dbl, [i64, i64, _p(i64), _p(i32), _p(dbl), _p(dbl), _p(dbl),
+                                         _p(dbl), dbl, _p(dbl), dbl, i64, _p(i64)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -270,6 +272,45 @@ def solve_tight(R: Reduced, xyz, tets, mu, x0=None, tol=1e-13, maxit=2_000_000,
                                 _ptr(R.vals, D), _ptr(R.F, D), _ptr(minv, D), _ptr(x, D), tol,
                                 maxit, max_restarts, C.byref(it))
     return x, float(tr), it.value
+
+
+def block_jacobi(R: Reduced, xyz, tets, mu, eps):
+    """The GPU Jacobi-mode preconditioner on the reduced system: inverse 3x3
+    velocity blocks per interior node, pressure weights 1/(|A_pp| + lumped
+    mass/mu), and the rank-one weight 1/(eps * volume)."""
+    npn = R.np_
+    nI = (R.N - npn) // 3
+    A = R.scipy().tocsr()
+    idx = np.arange(nI)
+    blocks = np.empty((nI, 3, 3))
+    for a in range(3):
+        for c in range(3):
+            blocks[:, a, c] = np.asarray(A[a * nI + idx, c * nI + idx]).ravel()
+    blocks = 0.5 * (blocks + blocks.transpose(0, 2, 1))
+    inv = np.linalg.inv(blocks)
+    vinv6 = np.ascontiguousarray(np.stack([inv[:, 0, 0], inv[:, 0, 1], inv[:, 0, 2],
+                                           inv[:, 1, 1], inv[:, 1, 2], inv[:, 2, 2]], axis=1))
+    P = np.asarray(xyz, np.float64)[np.asarray(tets)]
+    Bm = np.stack([P[:, 1] - P[:, 0], P[:, 2] - P[:, 0], P[:, 3] - P[:, 0]], axis=2)
+    vol = np.abs(np.linalg.det(Bm)) / 6.0
+    w = np.zeros(npn)
+    np.add.at(w, np.asarray(tets).ravel(), np.repeat(vol / (4.0 * mu), 4))
+    d = A.diagonal()[3 * nI:]
+    pinv = 1.0 / (np.abs(d) + w)
+    crank = 1.0 / (eps * vol.sum()) if eps > 0 else 0.0
+    return vinv6, pinv, crank, nI
+
+
+def minres_blockjacobi(R: Reduced, pre, x0=None, rtol=1e-10, maxit=1000):
+    """MINRES iterations with the block-Jacobi preconditioner (CPU baseline)."""
+    vinv6, pinv, crank, nI = pre
+    x = np.zeros(R.N) if x0 is None else np.array(x0, np.float64, copy=True)
+    it = C.c_int64()
+    red = lib().ora_minres_blockjacobi(R.N, nI, _ptr(R.rowptr, I64), _ptr(R.cols, I32),
+                                       _ptr(R.vals, D), _ptr(R.F, D), _ptr(vinv6, D),
+                                       _ptr(pinv, D), crank, _ptr(x, D), rtol, maxit,
+                                       C.byref(it))
+    return x, float(red), it.value
 
 
 def flow_solve(xyz, tets, boundary, phi, c, mu, par, x_warm=None, flow=None):

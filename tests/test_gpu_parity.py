@@ -154,3 +154,25 @@ def test_sphere65_fp64_parity():
     ev, ep = _errors(flow, O.scatter(R, x), inst.np)
     assert ev <= VEL_TOL_FP64 and ep <= P_TOL_FP64, (ev, ep, f.last_stats)
     f.close()
+
+
+@pytest.mark.parametrize("n", [16, 10])
+def test_even_n_multigrid_parity(n):
+    """Even lattice sizes coarsen to n/2 + 1 (the last coarse layer on the
+    Dirichlet boundary layer); FP64 parity and fewer iterations than Jacobi."""
+    import oracle as O
+    inst = workload("sphere17", n)
+    par = dict(inst.params)
+    its = {}
+    for pc in ("multigrid", "jacobi"):
+        f, rc, flow = _solve(inst, par=par, precision="fp64", preconditioner=pc)
+        assert rc == 0, f.last_error()
+        its[pc] = f.last_stats["iterations"]
+        if pc == "multigrid":
+            R, _, _, mu = O.system(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source,
+                                   inst.mu, par)
+            x, tr, _ = O.solve_tight(R, inst.xyz, inst.tets, mu, tol=1e-13)
+            ev, ep = _errors(flow, O.scatter(R, x), inst.np)
+            assert ev <= VEL_TOL_FP64 and ep <= P_TOL_FP64, (ev, ep)
+        f.close()
+    assert its["multigrid"] < its["jacobi"], its
