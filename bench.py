@@ -48,12 +48,17 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _traffic(kernel: str):
+def _traffic(kernel: str, bytes_per_launch: float | None):
+    """DRAM bytes per launch: the ratio of measured DRAM traffic to algorithmic
+    bytes from one ncu capture of this kernel (profiles/traffic.json), scaled to
+    this launch's algorithmic bytes (traffic grows with the rows processed)."""
     p = ROOT / "profiles" / "traffic.json"
-    if p.exists():
-        d = json.loads(p.read_text())
-        return d.get(kernel)
-    return None
+    if not p.exists() or not bytes_per_launch:
+        return None
+    d = json.loads(p.read_text()).get(kernel)
+    if not d:
+        return None
+    return round(d["traffic_over_algorithmic"] * bytes_per_launch)
 
 
 class Clocks:
@@ -113,12 +118,20 @@ def _setup_dist(ws, local, backend="nccl"):
 
 
 def _max_over_ranks(v: float, dist) -> float:
+    """Max of a per-rank time over all ranks (NCCL on GPUs, gloo on CPU)."""
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_ids(count: int, rank: int, world: int) -> list[int]:
+    """Instances a rank solves: independent solves are dealt round-robin over
+    the ranks (replicas, no data exchange)."""
+    return list(range(rank, count, world))
 
 
 def _barrier(dist):
@@ -274,10 +287,10 @@ def run_ours(args):
                      "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4) if achieved else None,
                      "traffic": _traffic("k_mf_minres_A" if operator == "matfree"
-                                         else "k_minres_A<float>"),
+                                         else "k_minres_A_ell", bytes_per),
                      "kernel": ("k_mf_minres_A (FP32 matrix-free element operator + MINRES dots)"
                                 if operator == "matfree" else
-                                "k_minres_A<float> (FP32 BSR SpMV + MINRES dots)"),
+                                "k_minres_A_ell (FP32 sliced-ELL 4x4-block SpMV + MINRES dots)"),
                      "bytes_per_launch": bytes_per, "ms_per_launch": round(per, 5),
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
         "gpu_launches": launches,
@@ -309,7 +322,7 @@ def run_batch(args):
     dev = torch.device("cuda", local)
     count = args.batch_count
     # replicas: rank r solves instances r, r + ws, ... of the batch (no collective)
-    ids = list(range(rank, count, ws))
+    ids = replica_ids(count, rank, ws)
     insts = [W.batch_instance(i) for i in ids]
     stream = torch.cuda.Stream(device=dev)
     phis = [torch.from_numpy(i.phi).to(dev) for i in insts]
@@ -411,7 +424,7 @@ def cpu_baseline(inst, seconds: float) -> dict:
 
 # Iterations of FP64 block-Jacobi + rank-one MINRES to the workload tolerance
 # (profiles/cpu_baseline.md): the CPU baseline's iteration count.
-CPU_BASELINE_ITERATIONS: dict = {}
+CPU_BASELINE_ITERATIONS: dict = {"sphere17": 1940, "sphere65": 4204, "ellipsoid129": 42647}
 
 
 def run_reference(args):

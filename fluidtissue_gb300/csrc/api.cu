@@ -21,7 +21,7 @@ void free_all(Ctx& c) {
                     c.b, c.x, c.r, c.w64.q, c.w64.R[0], c.w64.R[1], c.w64.Y[0], c.w64.Y[1],
                     c.w64.W[0], c.w64.W[1], c.w64.X, c.w32.q, c.w32.R[0], c.w32.R[1],
                     c.w32.Y[0], c.w32.Y[1], c.w32.W[0], c.w32.W[1], c.w32.X, c.w32.r0, c.ms,
-                    c.os, c.red.partials, c.red.ticket, c.err_flag, c.bicg};
+                    c.os, c.red.partials, c.red.ticket, c.err_flag, c.bicg, c.mf_rec};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     mg_free(c.mg64);
@@ -74,6 +74,10 @@ static void build_ell(Ctx& c) {
     FTS_CUDA(cudaMemcpy(c.ell_ptr, ptr.data(), ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     FTS_CUDA(cudaMemcpy(c.ell_col, col.data(), col.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     c.use_ell = true;
+}
+
+void ensure_fp64_work(Ctx& c) {
+    if (!c.w64.q) alloc_work<double>(c, c.w64, false);
 }
 
 void ensure_fp32(Ctx& c) {
@@ -178,7 +182,6 @@ void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
     c.geom = dev_alloc<ElemGeom>(c, c.nt);
     c.phi = dev_alloc<double>(c, c.np);
     c.src = dev_alloc<double>(c, c.np);
-    c.force = dev_alloc<double>(c, 3 * c.np);
     c.mu = dev_alloc<double>(c, c.nt);
     c.s = dev_alloc<double>(c, c.np);
     c.flow = dev_alloc<double>(c, 4 * c.np);
@@ -188,7 +191,7 @@ void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
     c.b = dev_alloc<V4<double>>(c, c.np);
     c.x = dev_alloc<V4<double>>(c, c.np);
     c.r = dev_alloc<V4<double>>(c, c.np);
-    alloc_work<double>(c, c.w64, false);
+    if (p.precision == FTS_PREC_FP64) alloc_work<double>(c, c.w64, false);
     c.w64.r0 = c.r;
     c.ms = dev_alloc<MinresScalars>(c, 1);
     c.os = dev_alloc<OuterScalars>(c, 1);
@@ -555,7 +558,11 @@ static int solve_common(fts_ctx* ctx, const double* phi, const double* source, c
         FTS_CUDA(cudaMemcpyAsync(c.phi, phi, c.np * sizeof(double), k, c.stream));
         FTS_CUDA(cudaMemcpyAsync(c.src, source, c.np * sizeof(double), k, c.stream));
         if (mu) FTS_CUDA(cudaMemcpyAsync(c.mu, mu, c.nt * sizeof(double), k, c.stream));
-        if (force) FTS_CUDA(cudaMemcpyAsync(c.force, force, 3 * c.np * sizeof(double), k, c.stream));
+        if (force) {
+            if (!c.force) c.force = dev_alloc<double>(c, 3 * c.np);
+            FTS_CUDA(cudaMemcpyAsync(c.force, force, 3 * c.np * sizeof(double), k, c.stream));
+        }
+        if (c.par.precision == FTS_PREC_FP64) ensure_fp64_work(c);
         double* out = device ? flow : c.flow;
         rc = solve_device(c, mu != nullptr, force != nullptr, out, st);
         if (rc == FTS_OK && st.solved && !device) {
@@ -584,8 +591,9 @@ static int solve_common(fts_ctx* ctx, const double* phi, const double* source, c
         const double V = c.par.precision == FTS_PREC_MIXED ? 4.0 : 8.0;
         const double nb = (double)c.nnzb, n = (double)c.np;
         st.spmv_bytes = nb * (16.0 * V + 4.0) + 4.0 * (n + 1.0) + 3.0 * 4.0 * n * V;
-        if (c.matfree)  // tets + node->element map + mu per element; coords, flags, x, r1, q per node
-            st.spmv_bytes = (double)c.nt * (16.0 + 16.0 + 8.0) + n * (4.0 + 12.0 + 1.0 + 3.0 * 16.0);
+        if (c.matfree)  // tets + node->element map + 64 B record per element; map offsets,
+                        // flags, x, r1, q per node
+            st.spmv_bytes = (double)c.nt * (16.0 + 16.0 + 64.0) + n * (4.0 + 1.0 + 3.0 * 16.0);
         st.spmv_bytes_fp64 = nb * (16.0 * 8.0 + 4.0) + 4.0 * (n + 1.0) + 3.0 * 4.0 * n * 8.0;
     }
     if (stats) *stats = st;
@@ -692,8 +700,9 @@ int fts_apply(fts_ctx* ctx, int32_t precision, const double* x, double* y) {
         }
         FTS_CUDA(cudaMemcpyAsync(c.r, x, c.np * 4 * sizeof(double), cudaMemcpyHostToDevice,
                                  c.stream));
-        launch_apply(c, precision, c.r, c.w64.q);
-        FTS_CUDA(cudaMemcpyAsync(y, c.w64.q, c.np * 4 * sizeof(double), cudaMemcpyDeviceToHost,
+        V4<double>* out = reinterpret_cast<V4<double>*>(c.flow);  // 4*np doubles of scratch
+        launch_apply(c, precision, c.r, out);
+        FTS_CUDA(cudaMemcpyAsync(y, out, c.np * 4 * sizeof(double), cudaMemcpyDeviceToHost,
                                  c.stream));
         FTS_CUDA(cudaStreamSynchronize(c.stream));
     } catch (const CudaError& e) {

@@ -893,6 +893,7 @@ int fts_batch_create(int32_t count, const fts_mesh* meshes, const fts_params* pa
                 break;
             }
             if (p.precision == FTS_PREC_MIXED) ensure_fp32(c->c);
+            else ensure_fp64_work(c->c);
             B->ctx.push_back(c);
         }
         if (rc == FTS_OK) batch_build(*B);

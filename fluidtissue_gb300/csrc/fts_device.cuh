@@ -160,6 +160,7 @@ struct Ctx {
 
     // operator representation: false = assembled BSR, true = element gather
     bool matfree = false;
+    float* mf_rec = nullptr;   // FP32 element records of the matrix-free operator
 
     // preconditioner
     bool use_mg = false;
@@ -192,6 +193,7 @@ int create_context(const fts_mesh* mesh, const fts_params* params, fts_ctx** out
 void free_all(Ctx& c);
 int validate_params(const fts_params& p, std::string& err);
 void ensure_fp32(Ctx& c);
+void ensure_fp64_work(Ctx& c);
 
 // ---- assembly (assemble.cu) -----------------------------------------------
 void launch_geometry(Ctx& c, int* bad);

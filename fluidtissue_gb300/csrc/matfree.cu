@@ -13,9 +13,9 @@
 // :135-203, symmetric sign convention).  Dirichlet velocity rows are identity
 // and Dirichlet velocity values are read as zero.
 //
-// FP32 inner operator: element geometry recomputed in FP32 from the float
-// node coordinates (12 B per node, L2-resident) instead of streaming stored
-// geometry.  FP64 outer residual: the stored FP64 ElemGeom.
+// FP32 inner operator: a 64-byte FP32 record per element (gradients, volume,
+// h^2, mu) built from the FP64 geometry; each record is read by the element's
+// 4 nodes (L2 reuse).  FP64 outer residual: the stored FP64 ElemGeom.
 #include <cfloat>
 
 #include "fts_device.cuh"
@@ -45,50 +45,6 @@ static MfConst mf_const() {
     return m;
 }
 
-// FP32 element geometry from float coordinates: gradients g[4][3], volume, h^2.
-__device__ __forceinline__ void geom_f32(const float* __restrict__ xyz, const int ids[4],
-                                         float g[4][3], float& vol, float& hh) {
-    float p[4][3];
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int a = 0; a < 3; ++a) p[j][a] = __ldg(xyz + 3 * (int64_t)ids[j] + a);
-    float B[3][3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        B[a][0] = p[1][a] - p[0][a];
-        B[a][1] = p[2][a] - p[0][a];
-        B[a][2] = p[3][a] - p[0][a];
-    }
-    const float c00 = B[1][1] * B[2][2] - B[1][2] * B[2][1];
-    const float c01 = B[1][2] * B[2][0] - B[1][0] * B[2][2];
-    const float c02 = B[1][0] * B[2][1] - B[1][1] * B[2][0];
-    const float det = B[0][0] * c00 + B[0][1] * c01 + B[0][2] * c02;
-    const float id = 1.0f / det;
-    float cof[3][3];
-    cof[0][0] = c00;
-    cof[0][1] = c01;
-    cof[0][2] = c02;
-    cof[1][0] = B[0][2] * B[2][1] - B[0][1] * B[2][2];
-    cof[1][1] = B[0][0] * B[2][2] - B[0][2] * B[2][0];
-    cof[1][2] = B[0][1] * B[2][0] - B[0][0] * B[2][1];
-    cof[2][0] = B[0][1] * B[1][2] - B[0][2] * B[1][1];
-    cof[2][1] = B[0][2] * B[1][0] - B[0][0] * B[1][2];
-    cof[2][2] = B[0][0] * B[1][1] - B[0][1] * B[1][0];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-        const float i0 = cof[r][0] * id, i1 = cof[r][1] * id, i2 = cof[r][2] * id;
-        g[0][r] = -i0 - i1 - i2;
-        g[1][r] = i0;
-        g[2][r] = i1;
-        g[3][r] = i2;
-    }
-    const float adet = fabsf(det);
-    vol = adet * (1.0f / 6.0f);
-    const float h = cbrtf(adet);
-    hh = h * h;
-}
-
 // Row a of element k applied to the element's nodal values u[4][4] (ux,uy,uz,p).
 template <typename T>
 __device__ __forceinline__ void elem_row(const T g[4][3], T vol, T hh, T mu, int a,
@@ -116,11 +72,36 @@ __device__ __forceinline__ void elem_row(const T g[4][3], T vol, T hh, T mu, int
             eps * vol * mp;
 }
 
+// FP32 element records for the inner operator, 64 B per element: gradients
+// g[4][3], volume, h^2, mu (mu refreshed every solve), pad.
+struct alignas(64) ElemF32 {
+    float g[4][3];
+    float vol, hh, mu, pad;
+};
+
+__global__ void k_mf_records(int64_t nt, const ElemGeom* __restrict__ geom,
+                             const double* __restrict__ mu, ElemF32* __restrict__ rec) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nt;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const ElemGeom& G = geom[k];
+        ElemF32 R;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) R.g[j][c] = (float)G.g[j][c];
+        R.vol = (float)G.vol;
+        R.hh = (float)G.hh;
+        R.mu = (float)mu[k];
+        R.pad = 0.f;
+        rec[k] = R;
+    }
+}
+
 // q = S (y + ycorr e_p) / beta over nodes (FP32), fused MINRES dots v.q, v.r1.
 __global__ void __launch_bounds__(kThreads)
 k_mf_minres_A(int64_t np, const int32_t* __restrict__ p2t_ptr, const uint32_t* __restrict__ p2t,
-              const int32_t* __restrict__ tets, const float* __restrict__ xyz,
-              const double* __restrict__ mu, const uint8_t* __restrict__ bnd,
+              const int32_t* __restrict__ tets, const ElemF32* __restrict__ rec,
+              const uint8_t* __restrict__ bnd,
               const V4<float>* __restrict__ Y, int ybuf, const V4<float>* __restrict__ R1,
               V4<float>* __restrict__ q, float alpha, float eps, MfConst K, Reduction red,
               MinresScalars* s) {
@@ -137,8 +118,11 @@ k_mf_minres_A(int64_t np, const int32_t* __restrict__ p2t_ptr, const uint32_t* _
             const int a = e & 3;
             const int4 t = __ldg(reinterpret_cast<const int4*>(tets) + k);
             const int ids[4] = {t.x, t.y, t.z, t.w};
-            float g[4][3], vol, hh;
-            geom_f32(xyz, ids, g, vol, hh);
+            const float4* rp = reinterpret_cast<const float4*>(rec + k);
+            const float4 r0 = __ldg(rp), r1v = __ldg(rp + 1), r2 = __ldg(rp + 2), r3 = __ldg(rp + 3);
+            const float g[4][3] = {{r0.x, r0.y, r0.z}, {r0.w, r1v.x, r1v.y},
+                                   {r1v.z, r1v.w, r2.x}, {r2.y, r2.z, r2.w}};
+            const float vol = r3.x, hh = r3.y, mue = r3.z;
             float u[4][4];
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
@@ -149,7 +133,7 @@ k_mf_minres_A(int64_t np, const int32_t* __restrict__ p2t_ptr, const uint32_t* _
                 u[b][2] = d ? 0.f : xv.z;
                 u[b][3] = xv.w + wadd;
             }
-            elem_row<float>(g, vol, hh, (float)__ldg(mu + k), a, u, alpha, eps, K.wq, K.mref, y);
+            elem_row<float>(g, vol, hh, mue, a, u, alpha, eps, K.wq, K.mref, y);
         }
         const V4<float> yv = Y[v];
         if (bnd[v]) {
@@ -268,8 +252,8 @@ __global__ void k_mf_pc(int64_t np, const int32_t* __restrict__ p2t_ptr,
 void launch_mf_minres_A(Ctx& c, const V4<float>* Y, int ybuf, const V4<float>* R1, V4<float>* q) {
     static const MfConst K = mf_const();
     k_mf_minres_A<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
-        c.np, c.p2t_ptr, c.p2t, c.tets, c.xyz, c.mu, c.bnd, Y, ybuf, R1, q, (float)c.par.alpha,
-        (float)c.par.eps, K, c.red, c.ms);
+        c.np, c.p2t_ptr, c.p2t, c.tets, reinterpret_cast<const ElemF32*>(c.mf_rec), c.bnd, Y,
+        ybuf, R1, q, (float)c.par.alpha, (float)c.par.eps, K, c.red, c.ms);
     c.launches += 1;
 }
 
@@ -284,6 +268,11 @@ void launch_mf_residual64(Ctx& c) {
 
 void launch_mf_pc(Ctx& c) {
     static const MfConst K = mf_const();
+    static_assert(sizeof(ElemF32) == 64, "64-byte element record");
+    if (!c.mf_rec) c.mf_rec = dev_alloc<float>(c, (size_t)c.nt * 16);
+    k_mf_records<<<grid_for(c, c.nt), kThreads, 0, c.stream>>>(
+        c.nt, c.geom, c.mu, reinterpret_cast<ElemF32*>(c.mf_rec));
+    c.launches += 1;
     k_mf_pc<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(c.np, c.p2t_ptr, c.p2t, c.geom, c.mu,
                                                          c.par.alpha, c.par.eps, K, c.pc32);
     FTS_CUDA(cudaGetLastError());
