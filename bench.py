@@ -48,6 +48,14 @@ def _peaks():
     return 6800.0, "fallback"
 
 
+# the operator kernel of the FP32 inner solve, per operator storage
+KERNELS = {
+    "stencil": ("k_minres_A_lat", "FP32 lattice half-stencil 4x4-block SpMV + MINRES dots"),
+    "assembled": ("k_minres_A_ell", "FP32 sliced-ELL 4x4-block SpMV + MINRES dots"),
+    "matfree": ("k_mf_minres_A", "FP32 matrix-free element operator + MINRES dots"),
+}
+
+
 def _traffic(kernel: str, bytes_per_launch: float | None):
     """DRAM bytes per launch: the ratio of measured DRAM traffic to algorithmic
     bytes from one ncu capture of this kernel (profiles/traffic.json), scaled to
@@ -159,8 +167,10 @@ def run_ours(args):
     flow_d = torch.zeros(4 * npn, dtype=torch.float64, device=dev)
     torch.cuda.synchronize()
 
-    operator = args.operator or ("matfree" if args.workload == "spheres257" else "assembled")
-    with_fp64 = not args.no_fp64 and operator == "assembled"
+    operator = args.operator or ("matfree" if args.workload == "spheres257" else "auto")
+    if operator == "auto":  # every bench workload is a Kuhn lattice: the half-stencil copy
+        operator = "stencil"
+    with_fp64 = not args.no_fp64 and operator != "matfree"
 
     def make(precision):
         f = Flow()
@@ -286,11 +296,8 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4) if achieved else None,
-                     "traffic": _traffic("k_mf_minres_A" if operator == "matfree"
-                                         else "k_minres_A_ell", bytes_per),
-                     "kernel": ("k_mf_minres_A (FP32 matrix-free element operator + MINRES dots)"
-                                if operator == "matfree" else
-                                "k_minres_A_ell (FP32 sliced-ELL 4x4-block SpMV + MINRES dots)"),
+                     "traffic": _traffic(KERNELS[operator][0], bytes_per),
+                     "kernel": f"{KERNELS[operator][0]} ({KERNELS[operator][1]})",
                      "bytes_per_launch": bytes_per, "ms_per_launch": round(per, 5),
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
         "gpu_launches": launches,
@@ -332,7 +339,8 @@ def run_batch(args):
     out = {}
     for prec in ("mixed", "fp64"):
         b = Batch([Mesh(i.xyz, i.tets) for i in insts], [i.params for i in insts],
-                  precision=prec, warm_start=False, device=local)
+                  precision=prec, warm_start=False, device=local,
+                  preconditioner=args.preconditioner)
         b.set_stream(stream.cuda_stream)
 
         def step():
@@ -458,7 +466,7 @@ def main():
     ap.add_argument("--inner-tol", type=float, default=0.0)
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--batch-count", type=int, default=96)
-    ap.add_argument("--operator", default=None, choices=["assembled", "matfree"])
+    ap.add_argument("--operator", default=None, choices=["stencil", "assembled", "matfree"])
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

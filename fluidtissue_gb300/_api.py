@@ -87,7 +87,7 @@ class FtsBatchConfig(C.Structure):
 PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_MINRES, SOLVER_BICGSTAB = 0, 1
 PC_AUTO, PC_JACOBI, PC_MULTIGRID = 0, 1, 2
-OP_AUTO, OP_ASSEMBLED, OP_MATFREE = 0, 1, 2
+OP_AUTO, OP_ASSEMBLED, OP_MATFREE, OP_STENCIL = 0, 1, 2, 3
 
 STATUS = {
     0: "FTS_OK", 1: "FTS_ERR_BAD_INPUT", 2: "FTS_ERR_DEGENERATE_ELEMENT",

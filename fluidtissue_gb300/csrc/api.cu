@@ -17,7 +17,7 @@ namespace fts {
 void free_all(Ctx& c) {
     void* ptrs[] = {c.xyz, c.tets, c.bnd, c.rowptr, c.cols, c.diag, c.p2t_ptr, c.p2t, c.geom,
                     c.phi, c.src, c.force, c.mu, c.s, c.flow, c.A64, c.A32, c.ell_val,
-                    c.ell_col, c.ell_ptr, c.pc64, c.pc32,
+                    c.ell_col, c.ell_ptr, c.lat_val, c.lat_src, c.pc64, c.pc32,
                     c.b, c.x, c.r, c.w64.q, c.w64.R[0], c.w64.R[1], c.w64.Y[0], c.w64.Y[1],
                     c.w64.W[0], c.w64.W[1], c.w64.X, c.w32.q, c.w32.R[0], c.w32.R[1],
                     c.w32.Y[0], c.w32.Y[1], c.w32.W[0], c.w32.W[1], c.w32.X, c.w32.r0, c.ms,
@@ -76,16 +76,52 @@ static void build_ell(Ctx& c) {
     c.use_ell = true;
 }
 
+// Source block of every lattice half-stencil entry: for node v and direction d
+// (0 = self, 1..7 = the positive Kuhn directions) the BSR block (v, v + d), or
+// -1 where the neighbour is outside the lattice or the block is absent.
+static void build_lattice(Ctx& c) {
+    const HostTopology& T = c.topo;
+    const int64_t n = T.lattice_n;
+    const int64_t tiles = (c.np + 31) / 32;
+    static const int ox[8] = {0, 1, 0, 0, 1, 1, 0, 1}, oy[8] = {0, 0, 1, 0, 1, 0, 1, 1},
+                     oz[8] = {0, 0, 0, 1, 0, 1, 1, 1};
+    std::vector<int32_t> src((size_t)tiles * 32 * 8, -1);
+#pragma omp parallel for schedule(static)
+    for (int64_t v = 0; v < c.np; ++v) {
+        const int64_t i = v % n, j = (v / n) % n, k = v / (n * n);
+        for (int d = 0; d < 8; ++d) {
+            if (i + ox[d] >= n || j + oy[d] >= n || k + oz[d] >= n) continue;
+            const int64_t w = v + ox[d] + n * (oy[d] + n * oz[d]);
+            for (int32_t q = T.rowptr[v]; q < T.rowptr[v + 1]; ++q)
+                if (T.cols[q] == w) {
+                    src[(size_t)v * 8 + d] = q;
+                    break;
+                }
+        }
+    }
+    c.lat_src = dev_alloc<int32_t>(c, src.size());
+    c.lat_val = dev_alloc<float>(c, (size_t)tiles * 128 * 32);
+    FTS_CUDA(cudaMemcpy(c.lat_src, src.data(), src.size() * sizeof(int32_t),
+                        cudaMemcpyHostToDevice));
+}
+
 void ensure_fp64_work(Ctx& c) {
     if (!c.w64.q) alloc_work<double>(c, c.w64, false);
 }
 
+// FP32 operator copy in the storage the context currently selects (built on
+// first use; a later parameter update may select the other storage).
 void ensure_fp32(Ctx& c) {
-    if (c.have32) return;
     if (!c.matfree) {
-        if (c.in_batch) c.A32 = dev_alloc<float>(c, (size_t)c.nnzb * 16);
-        else build_ell(c);
+        if (c.in_batch) {
+            if (!c.A32) c.A32 = dev_alloc<float>(c, (size_t)c.nnzb * 16);
+        } else if (c.use_lat) {
+            if (!c.lat_val) build_lattice(c);
+        } else if (!c.ell_val) {
+            build_ell(c);
+        }
     }
+    if (c.have32) return;
     c.pc32 = dev_alloc<float>(c, (size_t)c.np * 8);
     alloc_work<float>(c, c.w32, true);
     c.have32 = true;
@@ -102,6 +138,10 @@ int validate_params(const fts_params& p, std::string& err) {
     }
     if (p.precision != FTS_PREC_FP64 && p.precision != FTS_PREC_MIXED) {
         err = "unknown precision";
+        return FTS_ERR_BAD_INPUT;
+    }
+    if (p.operator_kind < FTS_OP_AUTO || p.operator_kind > FTS_OP_STENCIL) {
+        err = "unknown operator kind";
         return FTS_ERR_BAD_INPUT;
     }
     if (p.solver != FTS_SOLVER_MINRES && p.solver != FTS_SOLVER_BICGSTAB) {
@@ -122,14 +162,7 @@ int validate_params(const fts_params& p, std::string& err) {
 // Multigrid needs the Kuhn lattice structure and at least three levels
 // (n >= 9); for even n every node on the last layer of each axis must be a
 // Dirichlet node (the coarse lattice's last layer sits there).
-static int mg_levels(int n) {
-    int l = 1;
-    while (n >= 5) {
-        n = mg_coarse_n(n);
-        ++l;
-    }
-    return l;
-}
+static int mg_levels(int n) { return (int)mg_chain(n).size(); }
 
 static bool last_layers_dirichlet(const HostTopology& T, int n) {
     for (int64_t v = 0; v < T.np; ++v) {
@@ -149,6 +182,12 @@ static void configure_preconditioner(Ctx& c) {
         throw (int)FTS_ERR_UNSUPPORTED;
     }
     c.use_mg = mg_ok && c.par.preconditioner != FTS_PC_JACOBI;
+    if (c.par.operator_kind == FTS_OP_STENCIL && n == 0) {
+        c.last_error = "the stencil operator needs a Kuhn lattice mesh";
+        throw (int)FTS_ERR_UNSUPPORTED;
+    }
+    c.use_lat = !c.matfree && !c.in_batch && n > 0 &&
+                (c.par.operator_kind == FTS_OP_AUTO || c.par.operator_kind == FTS_OP_STENCIL);
     if (c.matfree && (!c.use_mg || c.par.precision != FTS_PREC_MIXED)) {
         c.last_error = "the matrix-free operator runs in mixed precision with the multigrid "
                        "preconditioner (Kuhn lattice, odd n >= 9)";
@@ -218,7 +257,6 @@ void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
                              cudaMemcpyHostToDevice, c.stream));
     FTS_CUDA(cudaMemcpyAsync(c.p2t, T.p2t.data(), 4 * c.nt * sizeof(uint32_t),
                              cudaMemcpyHostToDevice, c.stream));
-    if (p.precision == FTS_PREC_MIXED) ensure_fp32(c);
     // total volume (for the rank-one constant-pressure term of the preconditioner)
     double vol = 0.0;
 #pragma omp parallel for reduction(+ : vol) schedule(static)
@@ -238,7 +276,8 @@ void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
         vol += std::fabs(det) / 6.0;
     }
     c.volume = vol;
-    configure_preconditioner(c);
+    configure_preconditioner(c);  // decides the operator storage before any FP32 copy exists
+    if (p.precision == FTS_PREC_MIXED) ensure_fp32(c);
     launch_geometry(c, c.err_flag);
     int bad = 0;
     FTS_CUDA(cudaMemcpyAsync(&bad, c.err_flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
@@ -591,6 +630,8 @@ static int solve_common(fts_ctx* ctx, const double* phi, const double* source, c
         const double V = c.par.precision == FTS_PREC_MIXED ? 4.0 : 8.0;
         const double nb = (double)c.nnzb, n = (double)c.np;
         st.spmv_bytes = nb * (16.0 * V + 4.0) + 4.0 * (n + 1.0) + 3.0 * 4.0 * n * V;
+        if (c.use_lat && c.par.precision == FTS_PREC_MIXED)  // 8 blocks per node; x, r1, q
+            st.spmv_bytes = n * (8.0 * 16.0 * 4.0) + 3.0 * 4.0 * n * 4.0;
         if (c.matfree)  // tets + node->element map + 64 B record per element; map offsets,
                         // flags, x, r1, q per node
             st.spmv_bytes = (double)c.nt * (16.0 + 16.0 + 64.0) + n * (4.0 + 1.0 + 3.0 * 16.0);

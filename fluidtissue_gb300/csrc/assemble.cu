@@ -466,8 +466,41 @@ __global__ void k_to_ell(int64_t np, int64_t nslices, const int32_t* __restrict_
     }
 }
 
+// FP64 BSR -> FP32 lattice half stencil.  Thread t handles node v = 32 tile +
+// (t % 32) and direction d = (t / 32) % 8; row r of the block goes to float4
+// ((tile * 32 + 4 d + r) * 32 + v % 32), so a warp's store is 512 contiguous bytes.
+__global__ void k_to_lat(int64_t tiles, const int32_t* __restrict__ src,
+                         const double* __restrict__ A, float4* __restrict__ L) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < tiles * 256;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t tile = t >> 8;
+        const int d = (int)((t >> 5) & 7);
+        const int lane = (int)(t & 31);
+        const int32_t b = src[(tile * 32 + lane) * 8 + d];
+        float4* out = L + (tile * 32 + 4 * d) * 32 + lane;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (b >= 0) {
+                const double2* a = reinterpret_cast<const double2*>(A + (int64_t)b * 16 + 4 * r);
+                const double2 u = a[0], w = a[1];
+                o = make_float4((float)u.x, (float)u.y, (float)w.x, (float)w.y);
+            }
+            out[r * 32] = o;
+        }
+    }
+}
+
 void launch_to_f32(Ctx& c) {
-    if (c.use_ell)
+    if ((c.use_lat && !c.lat_val) || (c.use_ell && !c.ell_val) ||
+        (!c.use_lat && !c.use_ell && !c.A32) || !c.pc32)
+        throw CudaError(cudaErrorInvalidValue, "FP32 operator copy used before allocation",
+                        __FILE__, __LINE__);
+    if (c.use_lat) {
+        const int64_t tiles = (c.np + 31) / 32;
+        k_to_lat<<<grid_for(c, tiles * 256), kThreads, 0, c.stream>>>(
+            tiles, c.lat_src, c.A64, reinterpret_cast<float4*>(c.lat_val));
+    } else if (c.use_ell)
         k_to_ell<<<grid_for(c, c.nslices * 32), kThreads, 0, c.stream>>>(
             c.np, c.nslices, c.rowptr, c.A64, c.ell_ptr, c.ell_val);
     else

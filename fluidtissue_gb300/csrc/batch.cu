@@ -1,18 +1,22 @@
 // Batched Stokes solves: many independent systems (uneven mesh sizes, their
 // own viscosities and parameters) solved together.  Each instance is assembled
 // by the single-solve kernels into its own context; the Krylov iteration of all
-// instances then runs in ONE persistent cooperative launch: block-Jacobi +
-// rank-one preconditioned MINRES over a global list of row chunks, with a grid
-// barrier between phases, per-instance reductions finished in a fixed order,
-// and per-instance stop flags (converged instances drop out of the work).
+// instances then runs in ONE persistent cooperative launch: MINRES over a
+// global list of row chunks, with a grid barrier between phases, per-instance
+// reductions finished in a fixed order, and per-instance stop flags (converged
+// instances drop out of the work).  The velocity preconditioner of an instance
+// is the multigrid V-cycle where its mesh is a Kuhn lattice (all instances'
+// levels of the same depth are smoothed in one phase, over per-depth chunk
+// lists; each coarsest level is solved by one CTA), else 3x3 block Jacobi; the
+// pressure block is the diagonal + rank-one term of the single solve.
 // The FP64 outer loop (true residual, solution update) runs per instance
 // between persistent launches; the whole sequence is captured as a CUDA graph
 // and replayed.  An autotuner picks the block size, the chunk length and the
 // number of threads per block row (the work split of the SpMV).
 //
-// Grid barrier: counter + generation word; the spin has an iteration limit
-// after which the kernel records an error and leaves its loop (no unbounded
-// wait).  With the cooperative launch all blocks are co-resident.
+// Grid barrier (grid_sync.cuh): the spin has an iteration limit after which the
+// kernel records an error and leaves its loop (no unbounded wait).  With the
+// cooperative launch all blocks are co-resident.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -21,9 +25,13 @@
 #include <vector>
 
 #include "fts_device.cuh"
+#include "grid_sync.cuh"
+#include "mg_device.cuh"
 #include "reduce.cuh"
 
 namespace fts {
+
+constexpr int kMaxLevels = 10;  // multigrid levels per instance (n <= 513)
 
 static std::string& g_batch_error() {
     static thread_local std::string e;
@@ -49,47 +57,26 @@ struct BInst {
     double rtol;
     long long maxit;
     double crank;
+    int use_mg;          // multigrid velocity preconditioner (else block Jacobi)
+    int nlev;            // multigrid levels
+    LevelView<T> lv[kMaxLevels];
 };
 
+// Rows [row0, row1) of level `depth` of instance `inst` (depth 0: the system's
+// block rows).
 struct BChunk {
     int inst;
     int row0, row1;
+    int depth;
 };
 
-struct BarrierState {
-    unsigned count;
-    unsigned gen;
-    int error;
-    int active;
+// Multigrid schedule of the persistent kernel.
+struct BSched {
+    const int* cptr;    // chunks of depth d are [cptr[d], cptr[d + 1])
+    int max_depth;      // deepest non-coarsest level + 1 over all instances (0: no multigrid)
+    const int* coarse;  // instances with multigrid (one coarsest-level solve each)
+    int ncoarse;
 };
-
-constexpr long long kSpinLimit = 1LL << 26;  // ~ seconds with the 64 ns back-off
-
-__device__ __forceinline__ bool grid_barrier(BarrierState* b) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned* vgen = &b->gen;
-        const unsigned g = *vgen;
-        __threadfence();
-        if (atomicAdd(&b->count, 1u) == gridDim.x - 1) {
-            b->count = 0;
-            __threadfence();
-            atomicAdd(&b->gen, 1u);
-        } else {
-            long long spins = 0;
-            while (*vgen == g) {
-                if (++spins > kSpinLimit) {
-                    atomicOr(&b->error, 1);
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return *((volatile int*)&b->error) == 0;
-}
 
 template <typename T>
 __device__ __forceinline__ void pc_jacobi_b(const T* __restrict__ pc, int64_t i, const V4<T>& v,
@@ -159,13 +146,146 @@ __device__ __forceinline__ void bsum(double (&v)[NV]) {
     block_sum<NV>(v);
 }
 
+// Smoothing-type phase over the depth-d chunks: nodes of level d of every
+// active multigrid instance for which level d is not the coarsest.
+template <typename T, typename F>
+__device__ __forceinline__ void level_phase(const BInst<T>* __restrict__ inst,
+                                            const BChunk* __restrict__ chunks, const BSched& S,
+                                            int d, F f) {
+    for (int ch = S.cptr[d] + blockIdx.x; ch < S.cptr[d + 1]; ch += gridDim.x) {
+        const BChunk C = chunks[ch];
+        const BInst<T>& I = inst[C.inst];
+        if (!I.use_mg || I.s->stop || d + 1 >= I.nlev) continue;
+        const LevelView<T> L = I.lv[d];
+        for (int64_t v = C.row0 + threadIdx.x; v < C.row1; v += blockDim.x) f(I, L, v);
+    }
+}
+
+// One V-cycle of every active multigrid instance, level by level across the
+// batch; the last post-smoothing step of the finest level is left to the
+// caller (fused with preconditioner stage 2).  Returns false when a barrier
+// failed.
+template <typename T>
+__device__ bool batch_vcycle(const BInst<T>* __restrict__ inst, const BChunk* __restrict__ chunks,
+                             const BSched& S, BarrierState* bar) {
+    const int D = S.max_depth;
+    for (int d = 0; d < D; ++d) {
+        for (int s = 1; s < kSmooth; ++s) {
+            const int mode = s == 1 ? kStepFromZero : kStepRegular;
+            level_phase<T>(inst, chunks, S, d, [&](const BInst<T>&, const LevelView<T>& L, int64_t v) {
+                T xo[3];
+                mg_step_node<T>(L, v, s, mode, (s & 1) ? L.d0 : L.d1, (s & 1) ? L.d1 : L.d0, xo,
+                                true, true);
+            });
+            if (!grid_barrier(bar)) return false;
+        }
+        level_phase<T>(inst, chunks, S, d, [&](const BInst<T>&, const LevelView<T>& L, int64_t v) {
+            mg_resid_node<T>(L, v);
+        });
+        if (!grid_barrier(bar)) return false;
+        // restriction onto level d + 1 (which may be an instance's coarsest)
+        for (int ch = S.cptr[d + 1] + blockIdx.x; ch < S.cptr[d + 2]; ch += gridDim.x) {
+            const BChunk C = chunks[ch];
+            const BInst<T>& I = inst[C.inst];
+            if (!I.use_mg || I.s->stop || d + 1 >= I.nlev) continue;
+            const LevelView<T> F = I.lv[d], Cv = I.lv[d + 1];
+            for (int64_t v = C.row0 + threadIdx.x; v < C.row1; v += blockDim.x)
+                mg_restrict_node<T>(F, Cv, v);
+        }
+        if (!grid_barrier(bar)) return false;
+    }
+    // coarsest levels: one CTA per instance
+    for (int k = blockIdx.x; k < S.ncoarse; k += gridDim.x) {
+        const BInst<T>& I = inst[S.coarse[k]];
+        if (I.s->stop) continue;
+        const LevelView<T> L = I.lv[I.nlev - 1];
+        mg_coarse_block<T>(L, L.n == 3 ? 1 : kCoarse);
+    }
+    if (!grid_barrier(bar)) return false;
+    for (int d = D - 1; d >= 0; --d) {
+        level_phase<T>(inst, chunks, S, d, [&](const BInst<T>& I, const LevelView<T>& L, int64_t v) {
+            mg_prolong_node<T>(L, I.lv[d + 1], v);
+        });
+        if (!grid_barrier(bar)) return false;
+        level_phase<T>(inst, chunks, S, d, [&](const BInst<T>&, const LevelView<T>& L, int64_t v) {
+            mg_resid_first_node<T>(L, v);
+        });
+        if (!grid_barrier(bar)) return false;
+        const int last = d == 0 ? kSmooth - 2 : kSmooth - 1;
+        for (int s = 1; s <= last; ++s) {
+            const int mode = s == 1 ? kStepAfterFirst : kStepRegular;
+            level_phase<T>(inst, chunks, S, d, [&](const BInst<T>&, const LevelView<T>& L, int64_t v) {
+                T xo[3];
+                mg_step_node<T>(L, v, s, mode, (s & 1) ? L.d0 : L.d1, (s & 1) ? L.d1 : L.d0, xo,
+                                true, true);
+            });
+            if (!grid_barrier(bar)) return false;
+        }
+    }
+    return true;
+}
+
+// Multigrid preconditioner stage 2 over the row chunks: the finest level's
+// last post-smoothing step gives y.xyz (into Yn); partial n.xyz . y.xyz.
+template <typename T>
+__device__ void batch_pc2(const BInst<T>* __restrict__ inst, int nchunks,
+                          const BChunk* __restrict__ chunks, int rn, int yn,
+                          double* __restrict__ part) {
+    constexpr int s = kSmooth - 1;
+    const int mode = s == 1 ? kStepAfterFirst : kStepRegular;
+    for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const BChunk C = chunks[ch];
+        const BInst<T>& I = inst[C.inst];
+        if (!I.use_mg || I.s->stop) continue;
+        const LevelView<T> L = I.lv[0];
+        const V4<T>* Rn = I.R[rn];
+        V4<T>* Yn = I.Y[yn];
+        double acc[1] = {0.0};
+        for (int64_t i = C.row0 + threadIdx.x; i < C.row1; i += blockDim.x) {
+            T xo[3];
+            mg_step_node<T>(L, i, s, mode, (s & 1) ? L.d0 : L.d1, nullptr, xo, false, false);
+            const V4<T> n = Rn[i];
+            V4<T> z = Yn[i];
+            z.x = xo[0];
+            z.y = xo[1];
+            z.z = xo[2];
+            Yn[i] = z;
+            acc[0] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z);
+        }
+        block_sum<1>(acc);
+        if (threadIdx.x == 0) part[(int64_t)ch * 3 + 2] = acc[0];
+    }
+}
+
+// Preconditioner stage 1 at row i: y.w from the pressure weight; Jacobi gives
+// y.xyz, multigrid takes n.xyz as the finest right-hand side (y.xyz follows
+// in stage 2).
+template <typename T>
+__device__ __forceinline__ void batch_pc1(const BInst<T>& I, const LevelView<T>& L0, int64_t i,
+                                          const V4<T>& n, V4<T>& z, double (&acc)[3]) {
+    if (I.use_mg) {
+        z.x = z.y = z.z = T(0);
+        z.w = I.pc[8 * i + 6] * n.w;
+        L0.b[i] = n.x;
+        L0.b[L0.N + i] = n.y;
+        L0.b[2 * L0.N + i] = n.z;
+        const T bv[3] = {n.x, n.y, n.z};
+        mg_first_dir<T>(L0, i, bv);
+    } else {
+        pc_jacobi_b<T>(I.pc, i, n, z);
+        acc[2] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z);
+    }
+    acc[0] += (double)n.w;
+    acc[1] += (double)(n.w * z.w);
+}
+
 // The persistent batched MINRES.  TPR threads per block row (4 or 8): with 8,
 // two threads share one output component and split the block columns.
 template <typename T, int TPR>
 __global__ void __launch_bounds__(512)
 k_batch_minres(int ninst, BInst<T>* __restrict__ inst, int nchunks,
                const BChunk* __restrict__ chunks, double* __restrict__ part,
-               BarrierState* bar, long long max_sweeps) {
+               BarrierState* bar, long long max_sweeps, BSched S) {
     constexpr int NP = 3;  // partial values per chunk
     // ---- initialisation: scalars, first Lanczos vector, beta1 --------------
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < ninst; b += gridDim.x * blockDim.x) {
@@ -185,19 +305,17 @@ k_batch_minres(int ninst, BInst<T>* __restrict__ inst, int nchunks,
         const BInst<T>& I = inst[C.inst];
         double acc[NP] = {0.0, 0.0, 0.0};
         if (!I.s->stop) {
+            const LevelView<T> L0 = I.use_mg ? I.lv[0] : LevelView<T>{};
             for (int64_t i = C.row0 + threadIdx.x; i < C.row1; i += blockDim.x) {
                 const V4<T> n = I.r0[i];
                 I.R[0][i] = n;
                 I.R[1][i] = V4<T>{T(0), T(0), T(0), T(0)};
                 V4<T> z;
-                pc_jacobi_b<T>(I.pc, i, n, z);
+                batch_pc1<T>(I, L0, i, n, z, acc);
                 I.Y[0][i] = z;
                 I.W[0][i] = V4<T>{T(0), T(0), T(0), T(0)};
                 I.W[1][i] = V4<T>{T(0), T(0), T(0), T(0)};
                 I.X[i] = V4<T>{T(0), T(0), T(0), T(0)};
-                acc[0] += (double)n.w;
-                acc[1] += (double)(n.w * z.w);
-                acc[2] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z);
             }
         }
         bsum<NP>(acc);
@@ -205,6 +323,11 @@ k_batch_minres(int ninst, BInst<T>* __restrict__ inst, int nchunks,
             for (int k = 0; k < NP; ++k) part[(int64_t)ch * NP + k] = acc[k];
     }
     if (!grid_barrier(bar)) return;
+    if (S.max_depth > 0) {
+        if (!batch_vcycle<T>(inst, chunks, S, bar)) return;
+        batch_pc2<T>(inst, nchunks, chunks, 0, 0, part);
+        if (!grid_barrier(bar)) return;
+    }
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < ninst; b += gridDim.x * blockDim.x) {
         MinresScalars* s = inst[b].s;
         if (s->stop) continue;
@@ -295,6 +418,7 @@ k_batch_minres(int ninst, BInst<T>* __restrict__ inst, int nchunks,
                 V4<T>* R1 = I.R[p];
                 const V4<T>* R2 = I.R[1 - p];
                 V4<T>* Yn = I.Y[yn];
+                const LevelView<T> L0 = I.use_mg ? I.lv[0] : LevelView<T>{};
                 for (int64_t i = C.row0 + threadIdx.x; i < C.row1; i += blockDim.x) {
                     const V4<T> qv = I.q[i], a = R1[i], b2 = R2[i];
                     V4<T> n;
@@ -304,11 +428,8 @@ k_batch_minres(int ninst, BInst<T>* __restrict__ inst, int nchunks,
                     n.w = qv.w - c1 * a.w - c2 * b2.w;
                     R1[i] = n;
                     V4<T> z;
-                    pc_jacobi_b<T>(I.pc, i, n, z);
+                    batch_pc1<T>(I, L0, i, n, z, acc);
                     Yn[i] = z;
-                    acc[0] += (double)n.w;
-                    acc[1] += (double)(n.w * z.w);
-                    acc[2] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z);
                 }
             }
             bsum<NP>(acc);
@@ -316,6 +437,11 @@ k_batch_minres(int ninst, BInst<T>* __restrict__ inst, int nchunks,
                 for (int kk = 0; kk < NP; ++kk) part[(int64_t)ch * NP + kk] = acc[kk];
         }
         if (!grid_barrier(bar)) return;
+        if (S.max_depth > 0) {
+            if (!batch_vcycle<T>(inst, chunks, S, bar)) return;
+            batch_pc2<T>(inst, nchunks, chunks, p, yn, part);
+            if (!grid_barrier(bar)) return;
+        }
         for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < ninst;
              b += gridDim.x * blockDim.x) {
             MinresScalars* s = inst[b].s;
@@ -561,9 +687,15 @@ struct fts_batch {
     fts_batch_config cfg{256, 1024, 4, 0, 0.0, 0};
     bool tuned = false;
     // device state
-    std::vector<BChunk> chunks;
+    std::vector<BChunk> chunks;   // row chunks (depth 0), then the multigrid levels by depth
+    std::vector<int> cptr;        // chunks of depth d: [cptr[d], cptr[d + 1])
+    std::vector<int> coarse;      // instances with a multigrid hierarchy
+    int nch0 = 0;                 // row chunks
+    int max_depth = 0;            // non-coarsest multigrid depths
     BChunk* d_chunks = nullptr;
     size_t chunk_cap = 0;
+    int* d_sched = nullptr;       // cptr then coarse (device)
+    size_t sched_cap = 0;
     double* d_part = nullptr;
     size_t part_cap = 0;
     BarrierState* d_bar = nullptr;
@@ -581,24 +713,69 @@ struct fts_batch {
 
 namespace fts {
 
+// Multigrid level sizes of instance i (empty: block Jacobi).
+static std::vector<int> batch_chain(const fts_batch& B, int i) {
+    const Ctx& c = B.ctx[i]->c;
+    return c.use_mg ? mg_chain(c.topo.lattice_n) : std::vector<int>();
+}
+
 static void batch_chunks(fts_batch& B, int chunk_rows) {
     B.chunks.clear();
+    B.coarse.clear();
+    B.max_depth = 0;
+    std::vector<std::vector<int>> chains(B.count);
     for (int i = 0; i < B.count; ++i) {
         const Ctx& c = B.ctx[i]->c;
+        chains[i] = batch_chain(B, i);
+        if ((int)chains[i].size() > kMaxLevels)
+            throw CudaError(cudaErrorInvalidValue, "too many multigrid levels for a batch",
+                            __FILE__, __LINE__);
+        const int nlev = (int)chains[i].size();
+        B.h_inst64[i].use_mg = B.h_inst32[i].use_mg = nlev > 0;
+        B.h_inst64[i].nlev = B.h_inst32[i].nlev = nlev;
+        if (nlev > 0) {
+            B.coarse.push_back(i);
+            B.max_depth = std::max(B.max_depth, nlev - 1);
+        }
         const int first = (int)B.chunks.size();
         for (int64_t r0 = 0; r0 < c.np; r0 += chunk_rows)
-            B.chunks.push_back({i, (int)r0, (int)std::min<int64_t>(c.np, r0 + chunk_rows)});
+            B.chunks.push_back({i, (int)r0, (int)std::min<int64_t>(c.np, r0 + chunk_rows), 0});
         B.h_inst64[i].chunk0 = B.h_inst32[i].chunk0 = first;
         B.h_inst64[i].chunk1 = B.h_inst32[i].chunk1 = (int)B.chunks.size();
+    }
+    B.nch0 = (int)B.chunks.size();
+    B.cptr.assign(1, 0);
+    B.cptr.push_back(B.nch0);
+    for (int d = 1; d <= B.max_depth; ++d) {
+        for (int i = 0; i < B.count; ++i) {
+            if ((int)chains[i].size() <= d) continue;
+            const int64_t n = chains[i][d];
+            const int64_t N = n * n * n;
+            for (int64_t r0 = 0; r0 < N; r0 += chunk_rows)
+                B.chunks.push_back({i, (int)r0, (int)std::min<int64_t>(N, r0 + chunk_rows), d});
+        }
+        B.cptr.push_back((int)B.chunks.size());
     }
     const size_t n = B.chunks.size();
     if (n > B.chunk_cap) {
         if (B.d_chunks) cudaFree(B.d_chunks);
         if (B.d_part) cudaFree(B.d_part);
+        B.d_chunks = nullptr;
+        B.d_part = nullptr;
         FTS_CUDA(cudaMalloc(&B.d_chunks, n * sizeof(BChunk)));
         FTS_CUDA(cudaMalloc(&B.d_part, n * 3 * sizeof(double)));
         B.chunk_cap = n;
     }
+    std::vector<int> sched(B.cptr);
+    sched.insert(sched.end(), B.coarse.begin(), B.coarse.end());
+    if (sched.size() > B.sched_cap) {
+        if (B.d_sched) cudaFree(B.d_sched);
+        B.d_sched = nullptr;
+        FTS_CUDA(cudaMalloc(&B.d_sched, sched.size() * sizeof(int)));
+        B.sched_cap = sched.size();
+    }
+    FTS_CUDA(cudaMemcpyAsync(B.d_sched, sched.data(), sched.size() * sizeof(int),
+                             cudaMemcpyHostToDevice, B.stream));
     FTS_CUDA(cudaMemcpyAsync(B.d_chunks, B.chunks.data(), n * sizeof(BChunk),
                              cudaMemcpyHostToDevice, B.stream));
     FTS_CUDA(cudaMemcpyAsync(B.d_inst64, B.h_inst64.data(), B.count * sizeof(BInst<double>),
@@ -615,13 +792,32 @@ static int coresident_blocks(int threads, int num_sms) {
     return std::max(1, per_sm) * num_sms;
 }
 
+// Level views of the instances' multigrid hierarchies (built by the first
+// assembly), uploaded with the instance table.
+static void batch_levels(fts_batch& B) {
+    for (int i = 0; i < B.count; ++i) {
+        Ctx& c = B.ctx[i]->c;
+        if (!c.use_mg) continue;
+        if (B.precision == FTS_PREC_MIXED) {
+            for (size_t l = 0; l < c.mg32.L.size(); ++l) B.h_inst32[i].lv[l] = level_view(c.mg32, l);
+        } else {
+            for (size_t l = 0; l < c.mg64.L.size(); ++l) B.h_inst64[i].lv[l] = level_view(c.mg64, l);
+        }
+    }
+    FTS_CUDA(cudaMemcpyAsync(B.d_inst64, B.h_inst64.data(), B.count * sizeof(BInst<double>),
+                             cudaMemcpyHostToDevice, B.stream));
+    FTS_CUDA(cudaMemcpyAsync(B.d_inst32, B.h_inst32.data(), B.count * sizeof(BInst<float>),
+                             cudaMemcpyHostToDevice, B.stream));
+}
+
 template <typename T>
 static void launch_persistent(fts_batch& B, long long sweeps) {
     BInst<T>* inst = sizeof(T) == 8 ? reinterpret_cast<BInst<T>*>(B.d_inst64)
                                     : reinterpret_cast<BInst<T>*>(B.d_inst32);
     FTS_CUDA(cudaMemsetAsync(B.d_bar, 0, sizeof(BarrierState), B.stream));
     const int threads = B.cfg.threads;
-    const int nch = (int)B.chunks.size();
+    const int nch = B.nch0;
+    const BSched S{B.d_sched, B.max_depth, B.d_sched + B.cptr.size(), (int)B.coarse.size()};
     int blocks = B.cfg.tpr == 8 ? coresident_blocks<T, 8>(threads, B.num_sms)
                                 : coresident_blocks<T, 4>(threads, B.num_sms);
     blocks = std::min(blocks, std::max(nch, B.num_sms));
@@ -638,10 +834,10 @@ static void launch_persistent(fts_batch& B, long long sweeps) {
     lc.numAttrs = 1;
     if (B.cfg.tpr == 8)
         FTS_CUDA(cudaLaunchKernelEx(&lc, k_batch_minres<T, 8>, B.count, inst, nch,
-                                    (const BChunk*)B.d_chunks, B.d_part, B.d_bar, sweeps));
+                                    (const BChunk*)B.d_chunks, B.d_part, B.d_bar, sweeps, S));
     else
         FTS_CUDA(cudaLaunchKernelEx(&lc, k_batch_minres<T, 4>, B.count, inst, nch,
-                                    (const BChunk*)B.d_chunks, B.d_part, B.d_bar, sweeps));
+                                    (const BChunk*)B.d_chunks, B.d_part, B.d_bar, sweeps, S));
 }
 
 // Assembly of every instance (the single-solve kernels, no host waits).
@@ -658,7 +854,12 @@ static void batch_assemble(fts_batch& B, const std::vector<int>& have_mu) {
         launch_rhs(c, false);
         launch_assemble(c);
         launch_preconditioner(c);
-        if (B.precision == FTS_PREC_MIXED) launch_to_f32(c);
+        if (B.precision == FTS_PREC_MIXED) {
+            launch_to_f32(c);
+            if (c.use_mg) setup_preconditioner<float>(c);
+        } else if (c.use_mg) {
+            setup_preconditioner<double>(c);
+        }
         if (!c.par.warm_start)
             FTS_CUDA(cudaMemsetAsync(c.x, 0, c.np * sizeof(V4<double>), c.stream));
     }
@@ -666,7 +867,7 @@ static void batch_assemble(fts_batch& B, const std::vector<int>& have_mu) {
 
 // The outer loop for all instances, outer_passes times (device-side decisions).
 static void batch_outer_passes(fts_batch& B, int passes, long long sweeps) {
-    const int nch = (int)B.chunks.size();
+    const int nch = B.nch0;
     const int g = std::min(nch, B.num_sms * 8);
     const bool mixed = B.precision == FTS_PREC_MIXED;
     for (int o = 0; o <= passes; ++o) {
@@ -782,7 +983,7 @@ static void batch_tune(fts_batch& B) {
     const bool mixed = B.precision == FTS_PREC_MIXED;
     // a residual pass so that every instance has a right-hand side and a tolerance
     batch_reset_outer(B);
-    const int nch0 = (int)B.chunks.size();
+    const int nch0 = B.nch0;
     k_batch_residual<<<std::min(nch0, B.num_sms * 8), 256, 0, B.stream>>>(B.d_inst64, B.d_out, nch0,
                                                                         B.d_chunks, B.d_part);
     if (mixed) {
@@ -841,7 +1042,7 @@ static void batch_tune(fts_batch& B) {
 
 static void batch_free(fts_batch& B) {
     for (void* p : {(void*)B.d_chunks, (void*)B.d_part, (void*)B.d_bar, (void*)B.d_inst64,
-                    (void*)B.d_inst32, (void*)B.d_out})
+                    (void*)B.d_inst32, (void*)B.d_out, (void*)B.d_sched})
         if (p) cudaFree(p);
     if (B.graph) cudaGraphExecDestroy(B.graph);
     for (auto& e : B.ev)
@@ -884,7 +1085,6 @@ int fts_batch_create(int32_t count, const fts_mesh* meshes, const fts_params* pa
                 rc = FTS_ERR_UNSUPPORTED;
                 break;
             }
-            p.preconditioner = FTS_PC_JACOBI;  // the persistent kernel applies block Jacobi
             fts_ctx* c = nullptr;
             rc = create_context(&meshes[i], &p, &c, true);
             if (rc != FTS_OK) {
@@ -935,6 +1135,7 @@ static int batch_solve_common(fts_batch* B, const double* const* phi, const doub
         }
         FTS_CUDA(cudaEventRecord(B->ev[0], B->stream));
         batch_assemble(*B, have_mu);
+        batch_levels(*B);
         if (!B->tuned) batch_tune(*B);
         batch_reset_outer(*B);
         const int passes = B->precision == FTS_PREC_MIXED ? 4 : 2;

@@ -138,6 +138,12 @@ struct Ctx {
     int32_t* ell_ptr = nullptr; // [nslices + 1] first slot of each slice
     int64_t nslices = 0, ell_slots = 0;
     bool use_ell = false;
+    // FP32 lattice half stencil (Kuhn lattices): per node the blocks to itself
+    // and its 7 positive-direction neighbours, in tiles of 32 nodes x 128
+    // values; the other 7 blocks are the neighbours' blocks transposed
+    float* lat_val = nullptr;   // [ceil(np / 32) * 128 * 32]
+    int32_t* lat_src = nullptr; // [ceil(np / 32) * 32 * 8] BSR block of (v, v + d) or -1
+    bool use_lat = false;
     bool in_batch = false;
     double* pc64 = nullptr;   // 8 per node: inverse of the 3x3 velocity block (xx,xy,xz,yy,yz,zz),
     float* pc32 = nullptr;    // inverse pressure weight, pad

@@ -17,9 +17,60 @@
 
 #include "fts_device.cuh"
 #include "mg.cuh"
+#include "mg_device.cuh"
 #include "reduce.cuh"
 
 namespace fts {
+
+// Lattice half stencil: row r of node v's block towards direction d (0 = self,
+// 1..7 positive Kuhn directions) is one float4 at lat_idx(d, r, v); tiles of 32
+// nodes, so a warp's load of one (d, r) is 512 contiguous bytes.
+__device__ __forceinline__ int64_t lat_idx(int d, int r, int64_t v) {
+    return ((v >> 5) * 32 + d * 4 + r) * 32 + (v & 31);
+}
+
+// (S x)_v from the half stencil: own blocks towards v + d, and the blocks of
+// the neighbours v - d towards v, transposed (S is symmetric).  `wadd` is added
+// to the pressure component of every x read (the lazily applied rank-one term).
+__device__ __forceinline__ float4 lat_row(int n, int64_t v64, const float4* __restrict__ L,
+                                          const V4<float>* __restrict__ X, float wadd) {
+    const int v = (int)v64;
+    const int nn = n * n;
+    const int k = v / nn;
+    const int rem = v - k * nn;
+    const int j = rem / n;
+    const int i = rem - j * n;
+    const bool inner = i > 0 && j > 0 && k > 0 && i < n - 1 && j < n - 1 && k < n - 1;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+    for (int d = 0; d < 8; ++d) {
+        const int w = inner ? v + off_x(d) + n * off_y(d) + nn * off_z(d) : nbr(i, j, k, d, n);
+        if (w < 0) continue;
+        const V4<float> xv = X[w];
+        const float x3 = xv.w + wadd;
+        const float4 b0 = __ldg(L + lat_idx(d, 0, v64)), b1 = __ldg(L + lat_idx(d, 1, v64)),
+                     b2 = __ldg(L + lat_idx(d, 2, v64)), b3 = __ldg(L + lat_idx(d, 3, v64));
+        a0 = fmaf(b0.x, xv.x, fmaf(b0.y, xv.y, fmaf(b0.z, xv.z, fmaf(b0.w, x3, a0))));
+        a1 = fmaf(b1.x, xv.x, fmaf(b1.y, xv.y, fmaf(b1.z, xv.z, fmaf(b1.w, x3, a1))));
+        a2 = fmaf(b2.x, xv.x, fmaf(b2.y, xv.y, fmaf(b2.z, xv.z, fmaf(b2.w, x3, a2))));
+        a3 = fmaf(b3.x, xv.x, fmaf(b3.y, xv.y, fmaf(b3.z, xv.z, fmaf(b3.w, x3, a3))));
+    }
+#pragma unroll
+    for (int d = 1; d < 8; ++d) {
+        const int w = inner ? v - off_x(d) - n * off_y(d) - nn * off_z(d) : nbr(i, j, k, d + 7, n);
+        if (w < 0) continue;
+        const V4<float> xv = X[w];
+        const float x3 = xv.w + wadd;
+        const int64_t w64 = w;
+        const float4 b0 = __ldg(L + lat_idx(d, 0, w64)), b1 = __ldg(L + lat_idx(d, 1, w64)),
+                     b2 = __ldg(L + lat_idx(d, 2, w64)), b3 = __ldg(L + lat_idx(d, 3, w64));
+        a0 = fmaf(b0.x, xv.x, fmaf(b1.x, xv.y, fmaf(b2.x, xv.z, fmaf(b3.x, x3, a0))));
+        a1 = fmaf(b0.y, xv.x, fmaf(b1.y, xv.y, fmaf(b2.y, xv.z, fmaf(b3.y, x3, a1))));
+        a2 = fmaf(b0.z, xv.x, fmaf(b1.z, xv.y, fmaf(b2.z, xv.z, fmaf(b3.z, x3, a2))));
+        a3 = fmaf(b0.w, xv.x, fmaf(b1.w, xv.y, fmaf(b2.w, xv.z, fmaf(b3.w, x3, a3))));
+    }
+    return make_float4(a0, a1, a2, a3);
+}
 
 template <typename T>
 __device__ __forceinline__ T bsr_row_dot(const T* __restrict__ A, const int32_t* __restrict__ cols,
@@ -89,12 +140,27 @@ __global__ void k_apply_ell(int64_t np, int64_t nslices, const int32_t* __restri
     }
 }
 
+__global__ void k_apply_lat(int n, int64_t np, const float4* __restrict__ L,
+                            const V4<float>* __restrict__ in, float4* __restrict__ out) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < np;
+         v += (int64_t)gridDim.x * blockDim.x)
+        out[v] = lat_row(n, v, L, in, 0.f);
+}
+
 void launch_apply(Ctx& c, int precision, const V4<double>* in, V4<double>* out) {
     int grid = grid_for(c, c.np * 4);
     if (precision == FTS_PREC_MIXED) {
+        if ((c.use_lat && !c.lat_val) || (!c.use_lat && c.use_ell && !c.ell_val) ||
+            (!c.use_lat && !c.use_ell && !c.A32))
+            throw CudaError(cudaErrorInvalidValue, "FP32 operator copy not built", __FILE__,
+                            __LINE__);
         k_cast_d2f<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(
             c.np * 4, reinterpret_cast<const double*>(in), reinterpret_cast<float*>(c.w32.q));
-        if (c.use_ell)
+        if (c.use_lat)
+            k_apply_lat<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
+                c.topo.lattice_n, c.np, reinterpret_cast<const float4*>(c.lat_val), c.w32.q,
+                reinterpret_cast<float4*>(c.w32.r0));
+        else if (c.use_ell)
             k_apply_ell<<<grid_for(c, c.nslices * 32), kThreads, 0, c.stream>>>(
                 c.np, c.nslices, c.ell_ptr, c.ell_col, c.ell_val, c.w32.q,
                 reinterpret_cast<float*>(c.w32.r0));
@@ -300,6 +366,7 @@ k_minres_A_ell(int64_t np, int64_t nslices, const int32_t* __restrict__ ell_ptr,
         const int32_t kmax = (ell_ptr[sl + 1] - p0) >> 3;
         const int64_t slot0 = (int64_t)p0 + (lane >> 2);
         float ax = 0.f;
+#pragma unroll 4
         for (int32_t k = 0; k < kmax; ++k) {
             const int64_t slot = slot0 + 8 * k;
             const int32_t j = __ldg(ell_col + slot);
@@ -327,6 +394,39 @@ k_minres_A_ell(int64_t np, int64_t nslices, const int32_t* __restrict__ ell_ptr,
     }
 }
 
+// Kernel A on the lattice half stencil: thread per node.
+__global__ void __launch_bounds__(kThreads)
+k_minres_A_lat(int n, int64_t np, const float4* __restrict__ L, const V4<float>* __restrict__ Y,
+               int ybuf, const V4<float>* __restrict__ R1, V4<float>* __restrict__ q,
+               Reduction red, MinresScalars* s) {
+    if (s->stop) return;
+    const float tinv = (float)(1.0 / s->beta);
+    const float wadd = (float)s->ycorr[ybuf];
+    double acc[2] = {0.0, 0.0};
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < np;
+         v += (int64_t)gridDim.x * blockDim.x) {
+        const float4 a = lat_row(n, v, L, Y, wadd);
+        V4<float> qv;
+        qv.x = a.x * tinv;
+        qv.y = a.y * tinv;
+        qv.z = a.z * tinv;
+        qv.w = a.w * tinv;
+        q[v] = qv;
+        const V4<float> yv = Y[v], r1 = R1[v];
+        const float e0 = yv.x * tinv, e1 = yv.y * tinv, e2 = yv.z * tinv,
+                    e3 = (yv.w + wadd) * tinv;
+        acc[0] += (double)(e0 * qv.x) + (double)(e1 * qv.y) + (double)(e2 * qv.z) +
+                  (double)(e3 * qv.w);
+        acc[1] += (double)(e0 * r1.x) + (double)(e1 * r1.y) + (double)(e2 * r1.z) +
+                  (double)(e3 * r1.w);
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
+        const double c1 = s->iters >= 1 ? s->beta / s->oldb : 0.0;
+        s->alfa = tot[0] - c1 * tot[1];
+    }
+}
+
 // Preconditioner stage 1.
 //   init: n = r0 (written to Rn)      else: n = q - c1 R1 - c2 R2 (written to Rn = R1)
 //   y.w = ip * n.w;  Jacobi: y.xyz = D3^-1 n.xyz;  multigrid: b0 = n.xyz (SoA)
@@ -335,7 +435,7 @@ template <typename T, bool MGV>
 __global__ void __launch_bounds__(kThreads)
 k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
              const V4<T>* __restrict__ R2, V4<T>* Rn, const T* __restrict__ pc,
-             V4<T>* __restrict__ Ynew, int ybuf, T* __restrict__ b0, Reduction red,
+             V4<T>* __restrict__ Ynew, int ybuf, LevelView<T> L0, Reduction red,
              MinresScalars* s) {
     if (s->stop) return;
     T c1 = T(0), c2 = T(0);
@@ -361,9 +461,11 @@ k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
         if (MGV) {
             z.x = z.y = z.z = T(0);
             z.w = pc[8 * i + 6] * n.w;
-            b0[i] = n.x;
-            b0[np + i] = n.y;
-            b0[2 * np + i] = n.z;
+            L0.b[i] = n.x;
+            L0.b[np + i] = n.y;
+            L0.b[2 * np + i] = n.z;
+            const T bv[3] = {n.x, n.y, n.z};
+            mg_first_dir<T>(L0, i, bv);
         } else {
             pc_jacobi<T>(pc, i, n, z);
             acc[2] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z);
@@ -385,20 +487,24 @@ k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
     }
 }
 
-// Multigrid stage 2: y.xyz = V-cycle output x0 (SoA); beta.
+// Multigrid stage 2, fused with the V-cycle's last post-smoothing step on the
+// finest level: y.xyz = the step's new x (not stored in the level); beta.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_minres_pc2(int64_t np, int init, const V4<T>* __restrict__ Rn, const T* __restrict__ x0,
-             V4<T>* __restrict__ Ynew, int ybuf, Reduction red, MinresScalars* s) {
+k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, int init,
+             const V4<T>* __restrict__ Rn, V4<T>* __restrict__ Ynew, int ybuf, Reduction red,
+             MinresScalars* s) {
     if (s->stop) return;
     double acc[1] = {0.0};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L0.N;
          i += (int64_t)gridDim.x * blockDim.x) {
+        T xo[3];
+        mg_step_node<T>(L0, i, step, mode, din, nullptr, xo, false, false);
         const V4<T> n = Rn[i];
         V4<T> z = Ynew[i];
-        z.x = x0[i];
-        z.y = x0[np + i];
-        z.z = x0[2 * np + i];
+        z.x = xo[0];
+        z.y = xo[1];
+        z.z = xo[2];
         Ynew[i] = z;
         acc[0] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z);
     }
@@ -472,15 +578,19 @@ static void launch_pc(Ctx& c, bool use_mg, int init, const V4<T>* q, V4<T>* R1, 
     const T* pc = pc_of<T>(c);
     if (use_mg) {
         MG<T>& mg = mg_of<T>(c);
+        const LevelView<T> L0 = level_view(mg, 0);
         k_minres_pc1<T, true><<<gn, kThreads, 0, c.stream>>>(c.np, init, q, R1, R2, Rn, pc, Ynew,
-                                                             ybuf, mg.L[0].b, c.red, c.ms);
-        mg_vcycle<T>(c, mg, &c.ms->stop);
-        k_minres_pc2<T><<<gn, kThreads, 0, c.stream>>>(c.np, init, Rn, mg.L[0].x, Ynew, ybuf,
-                                                       c.red, c.ms);
+                                                             ybuf, L0, c.red, c.ms);
+        mg_vcycle<T>(c, mg, &c.ms->stop, true);
+        // the last post-smoothing step: step kSmooth - 1 reads d0 when it is odd
+        constexpr int s = kSmooth - 1;
+        k_minres_pc2<T><<<gn, kThreads, 0, c.stream>>>(
+            L0, s, s == 1 ? kStepAfterFirst : kStepRegular, (s & 1) ? L0.d0 : L0.d1, init, Rn,
+            Ynew, ybuf, c.red, c.ms);
         c.launches += 2;
     } else {
         k_minres_pc1<T, false><<<gn, kThreads, 0, c.stream>>>(c.np, init, q, R1, R2, Rn, pc, Ynew,
-                                                              ybuf, nullptr, c.red, c.ms);
+                                                              ybuf, LevelView<T>{}, c.red, c.ms);
         c.launches += 1;
     }
     (void)w;
@@ -527,6 +637,12 @@ long long minres_inner(Ctx& c, double rtol, long long maxit, double* achieved, i
                 launch_mf_minres_A(c, reinterpret_cast<const V4<float>*>(w.Y[yk]), yk,
                                    reinterpret_cast<const V4<float>*>(R1),
                                    reinterpret_cast<V4<float>*>(w.q));
+            else if (sizeof(T) == 4 && c.use_lat)
+                k_minres_A_lat<<<gn, kThreads, 0, c.stream>>>(
+                    c.topo.lattice_n, np, reinterpret_cast<const float4*>(c.lat_val),
+                    reinterpret_cast<const V4<float>*>(w.Y[yk]),
+                    yk, reinterpret_cast<const V4<float>*>(R1), reinterpret_cast<V4<float>*>(w.q),
+                    c.red, c.ms);
             else if (sizeof(T) == 4 && c.use_ell)
                 k_minres_A_ell<<<grid_for(c, c.nslices * 32), kThreads, 0, c.stream>>>(
                     np, c.nslices, c.ell_ptr, c.ell_col, c.ell_val,
@@ -560,6 +676,8 @@ long long minres_inner(Ctx& c, double rtol, long long maxit, double* achieved, i
         c.spmv_runs += ran;
         if (c.ms_host->stop) break;
     }
+    if (use_mg && mg_barrier_failed<T>(c, mg_of<T>(c)))
+        throw CudaError(cudaErrorLaunchTimeout, "multigrid grid barrier", __FILE__, __LINE__);
     const MinresScalars& S = *c.ms_host;
     *achieved = S.beta1 > 0.0 ? S.phibar / S.beta1 : 0.0;
     *status = S.status;

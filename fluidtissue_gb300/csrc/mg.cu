@@ -21,17 +21,26 @@
 // polynomial before and after the coarse correction keeps the V-cycle
 // symmetric positive definite, as MINRES requires.  Coarsest level: Chebyshev
 // of degree kCoarse in one CTA.
+//
+// Precision.  The FP32 hierarchy is built in FP32 (Galerkin products, D^-1)
+// and the V-cycle then reads an FP16 copy of every stencil, scaled per level so
+// that max |K| maps to 16384; the arithmetic stays FP32.  The stored half
+// stencil is symmetric by construction, so the V-cycle stays an SPD
+// preconditioner, of the FP16-rounded operator.  The FP64 hierarchy reads its
+// FP64 stencils.
 #include <cmath>
 #include <cstring>
+#include <utility>
 #include <vector>
 
 #include "fts_device.cuh"
+#include "grid_sync.cuh"
 #include "mg.cuh"
+#include "mg_device.cuh"
 #include "reduce.cuh"
 
 namespace fts {
 
-__constant__ int c_off[15][3];
 __constant__ int c_gal_start[16];
 __constant__ unsigned short c_gal_term[512];  // a | e << 4 | (weight code) << 8
 __constant__ float c_gal_w[512];
@@ -70,19 +79,10 @@ static void init_tables(int device) {
         }
     }
     start[15] = (int)term.size();
-    FTS_CUDA(cudaMemcpyToSymbol(c_off, kOff, sizeof(kOff)));
     FTS_CUDA(cudaMemcpyToSymbol(c_gal_start, start.data(), 16 * sizeof(int)));
     FTS_CUDA(cudaMemcpyToSymbol(c_gal_term, term.data(), term.size() * sizeof(unsigned short)));
     FTS_CUDA(cudaMemcpyToSymbol(c_gal_w, w.data(), w.size() * sizeof(float)));
     if (device < 64) done[device] = true;
-}
-
-// Tiled stencil layout: 32 consecutive nodes share one tile of kStored x 32
-// values (entry q = 9 d + 3 r + c, d = 0..7), so the loads of a warp stay
-// inside one contiguous 9 KB (FP32) region.
-constexpr int kStored = 72;
-__device__ __forceinline__ int64_t kidx(int q, int64_t v) {
-    return ((v >> 5) * kStored + q) * 32 + (v & 31);
 }
 
 // Entry x = 3r + c of the block K(f, f + off[e]) for any of the 15 directions.
@@ -90,14 +90,8 @@ template <typename T>
 __device__ __forceinline__ T kblock(const T* __restrict__ K, int e, int x, int64_t f, int n) {
     if (e < 8) return K[kidx(9 * e + x, f)];
     const int ep = e - 7;  // positive direction; the block is stored at f - off[ep]
-    const int64_t w = f - (c_off[ep][0] + (int64_t)n * (c_off[ep][1] + (int64_t)n * c_off[ep][2]));
+    const int64_t w = f - (off_x(ep) + (int64_t)n * (off_y(ep) + (int64_t)n * off_z(ep)));
     return K[kidx(9 * ep + 3 * (x % 3) + x / 3, w)];
-}
-
-__device__ __forceinline__ int nbr(int i, int j, int k, int d, int n) {
-    int a = i + c_off[d][0], b = j + c_off[d][1], c = k + c_off[d][2];
-    if (a < 0 || b < 0 || c < 0 || a >= n || b >= n || c >= n) return -1;
-    return a + n * (b + n * c);
 }
 
 // ---------------------------------------------------------------------------
@@ -219,8 +213,7 @@ __global__ void k_mg_galerkin(int nf, const T* __restrict__ Kf, const uint8_t* _
         } else if (J >= 0 && !mc[J]) {
             for (int q = c_gal_start[dJ]; q < c_gal_start[dJ + 1]; ++q) {
                 const int a = c_gal_term[q] & 15, e = (c_gal_term[q] >> 4) & 15;
-                const int fi = 2 * ci + c_off[a][0], fj = 2 * cj + c_off[a][1],
-                          fk = 2 * ck + c_off[a][2];
+                const int fi = 2 * ci + off_x(a), fj = 2 * cj + off_y(a), fk = 2 * ck + off_z(a);
                 if (fi < 0 || fj < 0 || fk < 0 || fi >= nf || fj >= nf || fk >= nf) continue;
                 const int64_t f = fi + (int64_t)nf * (fj + (int64_t)nf * fk);
                 if (mf[f]) continue;
@@ -266,73 +259,24 @@ __global__ void k_mg_dinv(int64_t N, const T* __restrict__ K, T* __restrict__ Di
     }
 }
 
-// y = K x at node v (3 components); x SoA [3][N].  32-bit lattice
-// coordinates; interior nodes take the neighbour offsets without range checks.
-template <typename T>
-__device__ __forceinline__ void stencil_apply(int n, int64_t N, int64_t v64,
-                                              const T* __restrict__ K,
-                                              const T* __restrict__ x, T y[3]) {
-    const int v = (int)v64;
-    const int nn = n * n;
-    const int k = v / nn;
-    const int rem = v - k * nn;
-    const int j = rem / n;
-    const int i = rem - j * n;
-    const bool inner = i > 0 && j > 0 && k > 0 && i < n - 1 && j < n - 1 && k < n - 1;
-    T a0 = T(0), a1 = T(0), a2 = T(0);
-#pragma unroll
-    for (int d = 0; d < 8; ++d) {  // self and positive directions: own blocks
-        const int w = inner ? v + c_off[d][0] + n * c_off[d][1] + nn * c_off[d][2]
-                            : nbr(i, j, k, d, n);
-        if (w < 0) continue;
-        const T x0 = x[w], x1 = x[N + w], x2 = x[2 * N + w];
-        const T* kb = K + kidx(d * 9, v64);
-        a0 = fma(kb[0], x0, fma(kb[32], x1, fma(kb[64], x2, a0)));
-        a1 = fma(kb[96], x0, fma(kb[128], x1, fma(kb[160], x2, a1)));
-        a2 = fma(kb[192], x0, fma(kb[224], x1, fma(kb[256], x2, a2)));
-    }
-#pragma unroll
-    for (int d = 1; d < 8; ++d) {  // negative directions: neighbour's block, transposed
-        const int w = inner ? v - c_off[d][0] - n * c_off[d][1] - nn * c_off[d][2]
-                            : nbr(i, j, k, d + 7, n);
-        if (w < 0) continue;
-        const T x0 = x[w], x1 = x[N + w], x2 = x[2 * N + w];
-        const T* kb = K + kidx(d * 9, (int64_t)w);
-        a0 = fma(kb[0], x0, fma(kb[96], x1, fma(kb[192], x2, a0)));
-        a1 = fma(kb[32], x0, fma(kb[128], x1, fma(kb[224], x2, a1)));
-        a2 = fma(kb[64], x0, fma(kb[160], x1, fma(kb[256], x2, a2)));
-    }
-    y[0] = a0;
-    y[1] = a1;
-    y[2] = a2;
-}
-
-template <typename T>
-__device__ __forceinline__ void dinv_apply(int64_t N, int64_t v, const T* __restrict__ Di,
-                                           const T r[3], T z[3]) {
-    const T d0 = Di[v], d1 = Di[N + v], d2 = Di[2 * N + v], d3 = Di[3 * N + v],
-            d4 = Di[4 * N + v], d5 = Di[5 * N + v];
-    z[0] = d0 * r[0] + d1 * r[1] + d2 * r[2];
-    z[1] = d1 * r[0] + d3 * r[1] + d4 * r[2];
-    z[2] = d2 * r[0] + d4 * r[1] + d5 * r[2];
-}
-
 // Power iteration step: w = D^-1 K v / ||v||; the norm of w goes to lam[l].
 template <typename T>
-__global__ void k_mg_power(int n, const T* __restrict__ K, const T* __restrict__ Di,
-                           const uint8_t* __restrict__ mask, const T* __restrict__ v,
-                           T* __restrict__ w, double* __restrict__ nrm, int first, Reduction red) {
-    const int64_t N = (int64_t)n * n * n;
+__global__ void k_mg_power(LevelView<T> L, const T* __restrict__ v, T* __restrict__ w,
+                           double* __restrict__ nrm, int first, Reduction red) {
+    const int64_t N = L.N;
     const double inv = first ? 1.0 : (*nrm > 0.0 ? 1.0 / *nrm : 0.0);
+    const T ks = (T)*L.ks;
     double acc[1] = {0.0};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N;
          i += (int64_t)gridDim.x * blockDim.x) {
         T y[3], z[3];
-        stencil_apply<T>(n, N, i, K, v, y);
-        dinv_apply<T>(N, i, Di, y, z);
+        stencil_apply<T>(L.n, N, i, L.K, v, y);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) y[c] *= ks;
+        dinv_apply<T>(N, i, L.Di, y, z);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            T o = mask[i] ? T(0) : (T)(z[c] * inv);
+            T o = L.mask[i] ? T(0) : (T)(z[c] * inv);
             w[c * N + i] = o;
             acc[0] += (double)o * (double)o;
         }
@@ -354,6 +298,33 @@ __global__ void k_mg_power_init(int64_t N, const uint8_t* __restrict__ mask, T* 
     }
 }
 
+// max |K| of a level (bits of a non-negative float compare as unsigned).
+__global__ void k_mg_absmax(int64_t n, const float* __restrict__ K, unsigned* __restrict__ out) {
+    float m = 0.f;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(K[i]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(out, __float_as_uint(m));
+}
+
+// FP16 copy of a level's stencil, scaled so that max |K| maps to 16384.
+__global__ void k_mg_to_half(int64_t n, const float* __restrict__ K,
+                             const unsigned* __restrict__ maxbits, __half* __restrict__ Kh,
+                             double* __restrict__ scale) {
+    const float mx = __uint_as_float(*maxbits);
+    const float sc = mx > 0.f ? mx / 16384.f : 1.f;
+    const float inv = 1.f / sc;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *scale = (double)sc;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        Kh[i] = __float2half_rn(K[i] * inv);
+}
+
+__global__ void k_mg_unit_scale(int levels, double* __restrict__ scale) {
+    for (int l = threadIdx.x; l < levels; l += blockDim.x) scale[l] = 1.0;
+}
+
 // ---------------------------------------------------------------------------
 // V-cycle kernels.  All skip when the MINRES run has stopped (*stop != 0).
 // Chebyshev on [lmin, lmax] = [lambda*kLowFrac, lambda]:
@@ -362,7 +333,6 @@ __global__ void k_mg_power_init(int64_t N, const uint8_t* __restrict__ mask, T* 
 //   d_0 = D^-1 r / theta;  d_i = rho_i rho_{i-1} d_{i-1} + (2 rho_i/delta) D^-1 r_i.
 // ---------------------------------------------------------------------------
 constexpr double kLowFrac = 0.1;
-constexpr int kCoefStride = 64;      // per level: 1/theta, then (ca_s, cb_s) for s >= 1
 constexpr int kCoarseThreads = 256;  // one CTA for the coarsest level (<= 9^3 nodes)
 
 // Chebyshev coefficients of one level, computed once per solve on the host.
@@ -379,186 +349,111 @@ static void cheb_table(double lam, double* out) {
     }
 }
 
-// First smoothing step.  has_x = 0: from x = 0 (r = b, x = d).  has_x = 1: r
-// already holds b - K x (computed by k_mg_residual, so that no thread reads x
-// at a neighbour while x is updated here); x += d.
 template <typename T>
-__global__ void k_mg_smooth_first(int n, const T* __restrict__ K, const T* __restrict__ Di,
-                                  const T* __restrict__ b, T* __restrict__ x, T* __restrict__ r,
-                                  T* __restrict__ d, const double* __restrict__ coef, int has_x,
-                                  const int* __restrict__ stop) {
+__global__ void __launch_bounds__(kThreads, 4)
+k_mg_step(LevelView<T> L, int step, int mode, const T* __restrict__ din, T* __restrict__ dout,
+          const int* __restrict__ stop) {
     if (stop && *stop) return;
-    const int64_t N = (int64_t)n * n * n;
-    const T ith = (T)coef[0];
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        T rr[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) rr[c] = has_x ? r[c * N + i] : b[c * N + i];
-        T z[3];
-        dinv_apply<T>(N, i, Di, rr, z);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            r[c * N + i] = rr[c];
-            const T dd = z[c] * ith;
-            d[c * N + i] = dd;
-            x[c * N + i] = has_x ? x[c * N + i] + dd : dd;
-        }
-    }
+    T xo[3];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.N;
+         i += (int64_t)gridDim.x * blockDim.x)
+        mg_step_node<T>(L, i, step, mode, din, dout, xo, true, true);
 }
 
-// Later smoothing steps: r -= K d_in; d_out = ca d_in + cb D^-1 r; x += d_out.
-// (has_x kernels must not read x at neighbours while another thread updates it:
-// x is only touched at the thread's own node here.)
 template <typename T>
-__global__ void __launch_bounds__(kThreads, 4) k_mg_smooth_step(int n, const T* __restrict__ K, const T* __restrict__ Di,
-                                 const T* __restrict__ din, T* __restrict__ dout,
-                                 T* __restrict__ r, T* __restrict__ x,
-                                 const double* __restrict__ coef, int step,
-                                 const int* __restrict__ stop) {
+__global__ void __launch_bounds__(kThreads, 4)
+k_mg_residual(LevelView<T> L, const int* __restrict__ stop) {
     if (stop && *stop) return;
-    const int64_t N = (int64_t)n * n * n;
-    const T A = (T)coef[2 * step - 1], B = (T)coef[2 * step];
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        T y[3], rr[3], z[3];
-        stencil_apply<T>(n, N, i, K, din, y);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) rr[c] = r[c * N + i] - y[c];
-        dinv_apply<T>(N, i, Di, rr, z);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            r[c * N + i] = rr[c];
-            const T dd = A * din[c * N + i] + B * z[c];
-            dout[c * N + i] = dd;
-            x[c * N + i] += dd;
-        }
-    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.N;
+         i += (int64_t)gridDim.x * blockDim.x)
+        mg_resid_node<T>(L, i);
 }
 
-// r = b - K x
 template <typename T>
-__global__ void __launch_bounds__(kThreads, 4) k_mg_residual(int n, const T* __restrict__ K, const T* __restrict__ b,
-                              const T* __restrict__ x, T* __restrict__ r,
-                              const int* __restrict__ stop) {
+__global__ void __launch_bounds__(kThreads, 4)
+k_mg_resid_first(LevelView<T> L, const int* __restrict__ stop) {
     if (stop && *stop) return;
-    const int64_t N = (int64_t)n * n * n;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        T y[3];
-        stencil_apply<T>(n, N, i, K, x, y);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) r[c * N + i] = b[c * N + i] - y[c];
-    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.N;
+         i += (int64_t)gridDim.x * blockDim.x)
+        mg_resid_first_node<T>(L, i);
 }
 
-// b_c(I) = sum_a w_a r_f(2I + off[a])  (P^T r), zero on Dirichlet nodes.
 template <typename T>
-__global__ void k_mg_restrict(int nf, const T* __restrict__ rf, const uint8_t* __restrict__ mf,
-                              int nc, T* __restrict__ bc, const uint8_t* __restrict__ mc,
-                              const int* __restrict__ stop) {
+__global__ void k_mg_restrict(LevelView<T> F, LevelView<T> C, const int* __restrict__ stop) {
     if (stop && *stop) return;
-    const int64_t Nf = (int64_t)nf * nf * nf, Nc = (int64_t)nc * nc * nc;
-    for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < Nc;
-         I += (int64_t)gridDim.x * blockDim.x) {
-        T a0 = T(0), a1 = T(0), a2 = T(0);
-        if (!mc[I]) {
-            const int ci = (int)(I % nc), cj = (int)((I / nc) % nc),
-                      ck = (int)(I / ((int64_t)nc * nc));
-#pragma unroll
-            for (int a = 0; a < 15; ++a) {
-                const int f = nbr(2 * ci, 2 * cj, 2 * ck, a, nf);
-                if (f < 0 || mf[f]) continue;
-                const T w = a == 0 ? T(1) : T(0.5);
-                a0 += w * rf[f];
-                a1 += w * rf[Nf + f];
-                a2 += w * rf[2 * Nf + f];
-            }
-        }
-        bc[I] = a0;
-        bc[Nc + I] = a1;
-        bc[2 * Nc + I] = a2;
-    }
+    for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < C.N;
+         I += (int64_t)gridDim.x * blockDim.x)
+        mg_restrict_node<T>(F, C, I);
 }
 
-// x_f(f) += sum_{parents J} w x_c(J)  (P e)
 template <typename T>
-__global__ void k_mg_prolong(int nf, T* __restrict__ xf, const uint8_t* __restrict__ mf, int nc,
-                             const T* __restrict__ xc, const uint8_t* __restrict__ mc,
-                             const int* __restrict__ stop) {
+__global__ void k_mg_prolong(LevelView<T> F, LevelView<T> C, const int* __restrict__ stop) {
     if (stop && *stop) return;
-    const int64_t Nf = (int64_t)nf * nf * nf, Nc = (int64_t)nc * nc * nc;
-    for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < Nf;
-         f += (int64_t)gridDim.x * blockDim.x) {
-        if (mf[f]) continue;
-        const int fi = (int)(f % nf), fj = (int)((f / nf) % nf), fk = (int)(f / ((int64_t)nf * nf));
-        const int Ai = fi >> 1, Aj = fj >> 1, Ak = fk >> 1;
-        const int oi = fi & 1, oj = fj & 1, ok = fk & 1;
-        T s0 = T(0), s1 = T(0), s2 = T(0);
-        const int64_t A = Ai + (int64_t)nc * (Aj + (int64_t)nc * Ak);
-        if ((oi | oj | ok) == 0) {
-            if (!mc[A]) {
-                s0 = xc[A];
-                s1 = xc[Nc + A];
-                s2 = xc[2 * Nc + A];
-            }
-        } else {
-            const int64_t Bn = (Ai + oi) + (int64_t)nc * ((Aj + oj) + (int64_t)nc * (Ak + ok));
-            if (!mc[A]) {
-                s0 += T(0.5) * xc[A];
-                s1 += T(0.5) * xc[Nc + A];
-                s2 += T(0.5) * xc[2 * Nc + A];
-            }
-            if (!mc[Bn]) {
-                s0 += T(0.5) * xc[Bn];
-                s1 += T(0.5) * xc[Nc + Bn];
-                s2 += T(0.5) * xc[2 * Nc + Bn];
-            }
-        }
-        xf[f] += s0;
-        xf[Nf + f] += s1;
-        xf[2 * Nf + f] += s2;
-    }
+    for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < F.N;
+         f += (int64_t)gridDim.x * blockDim.x)
+        mg_prolong_node<T>(F, C, f);
 }
 
-// Coarsest level: kCoarse Chebyshev steps from zero in a single CTA.
 template <typename T>
-__global__ void __launch_bounds__(kCoarseThreads) k_mg_coarse_solve(int n, const T* __restrict__ K, const T* __restrict__ Di,
-                                  const T* __restrict__ b, T* __restrict__ x, T* __restrict__ r,
-                                  T* __restrict__ d0, T* __restrict__ d1,
-                                  const double* __restrict__ coef, int steps,
-                                  const int* __restrict__ stop) {
+__global__ void __launch_bounds__(kCoarseThreads)
+k_mg_coarse_solve(LevelView<T> L, int steps, const int* __restrict__ stop) {
     if (stop && *stop) return;
-    const int64_t N = (int64_t)n * n * n;
-    const T ith = (T)coef[0];
-    for (int64_t i = threadIdx.x; i < N; i += blockDim.x) {
-        T rr[3], z[3];
-        for (int c = 0; c < 3; ++c) rr[c] = b[c * N + i];
-        dinv_apply<T>(N, i, Di, rr, z);
-        for (int c = 0; c < 3; ++c) {
-            r[c * N + i] = rr[c];
-            d0[c * N + i] = z[c] * ith;
-            x[c * N + i] = z[c] * ith;
+    mg_coarse_block<T>(L, steps);
+}
+
+// The levels l0.. of one V-cycle in one cooperative launch: the small levels
+// are latency bound as separate launches, so their phases are separated by
+// grid barriers instead.  Level l0's right-hand side and first direction are
+// ready; its corrected x is the result.  skip_final (l0 == 0) leaves the last
+// post-smoothing step of the finest level to the caller.
+template <typename T>
+struct MGTailArgs {
+    LevelView<T> lv[kMaxMGLevels];
+    int l0, nlev, skip_final;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_mg_tail(const __grid_constant__ MGTailArgs<T> a, BarrierState* bar,
+          const int* __restrict__ stop) {
+    if (stop && *stop) return;  // uniform: nothing writes the flag during the V-cycle
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    T xo[3];
+    for (int l = a.l0; l + 1 < a.nlev; ++l) {
+        const LevelView<T> L = a.lv[l];
+        for (int s = 1; s < kSmooth; ++s) {
+            const int mode = s == 1 ? kStepFromZero : kStepRegular;
+            for (int64_t v = tid; v < L.N; v += nth)
+                mg_step_node<T>(L, v, s, mode, (s & 1) ? L.d0 : L.d1, (s & 1) ? L.d1 : L.d0, xo,
+                                true, true);
+            if (!grid_barrier(bar)) return;
         }
+        for (int64_t v = tid; v < L.N; v += nth) mg_resid_node<T>(L, v);
+        if (!grid_barrier(bar)) return;
+        const LevelView<T> C = a.lv[l + 1];
+        for (int64_t v = tid; v < C.N; v += nth) mg_restrict_node<T>(L, C, v);
+        if (!grid_barrier(bar)) return;
     }
-    __syncthreads();
-    for (int s = 1; s < steps; ++s) {
-        const T A = (T)coef[2 * s - 1], B = (T)coef[2 * s];
-        const T* din = (s & 1) ? d0 : d1;
-        T* dout = (s & 1) ? d1 : d0;
-        for (int64_t i = threadIdx.x; i < N; i += blockDim.x) {
-            T y[3], rr[3], z[3];
-            stencil_apply<T>(n, N, i, K, din, y);
-            for (int c = 0; c < 3; ++c) rr[c] = r[c * N + i] - y[c];
-            dinv_apply<T>(N, i, Di, rr, z);
-            for (int c = 0; c < 3; ++c) {
-                r[c * N + i] = rr[c];
-                const T dd = A * din[c * N + i] + B * z[c];
-                dout[c * N + i] = dd;
-                x[c * N + i] += dd;
-            }
+    if (blockIdx.x == 0) {
+        const LevelView<T> L = a.lv[a.nlev - 1];
+        mg_coarse_block<T>(L, L.n == 3 ? 1 : kCoarse);
+    }
+    if (!grid_barrier(bar)) return;
+    for (int l = a.nlev - 2; l >= a.l0; --l) {
+        const LevelView<T> L = a.lv[l], C = a.lv[l + 1];
+        for (int64_t v = tid; v < L.N; v += nth) mg_prolong_node<T>(L, C, v);
+        if (!grid_barrier(bar)) return;
+        for (int64_t v = tid; v < L.N; v += nth) mg_resid_first_node<T>(L, v);
+        if (!grid_barrier(bar)) return;
+        const int last = (l == 0 && a.skip_final) ? kSmooth - 2 : kSmooth - 1;
+        for (int s = 1; s <= last; ++s) {
+            const int mode = s == 1 ? kStepAfterFirst : kStepRegular;
+            for (int64_t v = tid; v < L.N; v += nth)
+                mg_step_node<T>(L, v, s, mode, (s & 1) ? L.d0 : L.d1, (s & 1) ? L.d1 : L.d0, xo,
+                                true, true);
+            if (!grid_barrier(bar)) return;
         }
-        __syncthreads();
     }
 }
 
@@ -569,22 +464,46 @@ template <typename T>
 void mg_build(Ctx& c, MG<T>& mg) {
     if (mg.built) return;
     init_tables(c.device);
-    const int n0 = c.topo.lattice_n;
-    int n = n0;
-    while (true) {
+    for (const int n : mg_chain(c.topo.lattice_n)) {
         MGLevel<T> L;
         L.n = n;
         L.N = (int64_t)n * n * n;
-        L.K = dev_alloc<T>(c, (size_t)((L.N + 31) / 32) * 32 * kStored);
+        const size_t stored = (size_t)((L.N + 31) / 32) * 32 * kStored;
+        L.K = dev_alloc<T>(c, stored);
+        if (sizeof(typename MGStore<T>::type) == sizeof(T))
+            L.Kh = reinterpret_cast<typename MGStore<T>::type*>(L.K);
+        else
+            L.Kh = dev_alloc<typename MGStore<T>::type>(c, stored);
         L.Di = dev_alloc<T>(c, (size_t)L.N * 6);
         for (auto** p : {&L.b, &L.x, &L.r, &L.d0, &L.d1}) *p = dev_alloc<T>(c, (size_t)L.N * 3);
         L.mask = dev_alloc<uint8_t>(c, (size_t)L.N);
         mg.L.push_back(L);
-        if (n < 5) break;
-        n = mg_coarse_n(n);
     }
     mg.lam = dev_alloc<double>(c, mg.L.size() + 1);
     mg.coef = dev_alloc<double>(c, mg.L.size() * kCoefStride);
+    mg.scale = dev_alloc<double>(c, mg.L.size());
+    mg.maxbits = dev_alloc<unsigned>(c, mg.L.size());
+    if (mg.L.size() > (size_t)kMaxMGLevels) {
+        c.last_error = "lattice too large for the multigrid hierarchy";
+        throw (int)FTS_ERR_UNSUPPORTED;
+    }
+    // persistent launch for the small levels: the first level (below the
+    // finest, unless the whole hierarchy is small) with at most kTailNodes nodes
+    mg.tail_level = -1;
+    for (size_t l = 0; l + 1 < mg.L.size(); ++l)
+        if (mg.L[l].N <= kTailNodes) {
+            mg.tail_level = (int)l;
+            break;
+        }
+    if (mg.tail_level >= 0) {
+        int per_sm = 0;
+        FTS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mg_tail<T>, kThreads, 0));
+        const int64_t want = (mg.L[mg.tail_level].N + kThreads - 1) / kThreads;
+        mg.tail_blocks = (int)std::min<int64_t>(want, (int64_t)std::max(per_sm, 0) * c.num_sms);
+        if (mg.tail_blocks < 1) mg.tail_level = -1;
+        mg.bar = dev_alloc<BarrierState>(c, 1);
+        FTS_CUDA(cudaMemsetAsync(mg.bar, 0, sizeof(BarrierState), c.stream));
+    }
     FTS_CUDA(cudaMemcpyAsync(mg.L[0].mask, c.bnd, (size_t)mg.L[0].N, cudaMemcpyDeviceToDevice,
                              c.stream));
     for (size_t l = 1; l < mg.L.size(); ++l) {
@@ -596,8 +515,25 @@ void mg_build(Ctx& c, MG<T>& mg) {
     mg.built = true;
 }
 
+// The smoothing copy of level l's stencil (FP16 for the FP32 hierarchy).
+static void mg_store(Ctx& c, MG<float>& mg, size_t l) {
+    MGLevel<float>& L = mg.L[l];
+    const int64_t stored = ((L.N + 31) / 32) * 32 * kStored;
+    FTS_CUDA(cudaMemsetAsync(mg.maxbits + l, 0, sizeof(unsigned), c.stream));
+    k_mg_absmax<<<grid_for(c, stored), kThreads, 0, c.stream>>>(stored, L.K, mg.maxbits + l);
+    k_mg_to_half<<<grid_for(c, stored), kThreads, 0, c.stream>>>(stored, L.K, mg.maxbits + l,
+                                                                  L.Kh, mg.scale + l);
+    c.launches += 2;
+}
+static void mg_store(Ctx& c, MG<double>& mg, size_t l) {
+    if (l == 0) {
+        k_mg_unit_scale<<<1, 32, 0, c.stream>>>((int)mg.L.size(), mg.scale);
+        c.launches += 1;
+    }
+}
+
 // Per-solve set-up after assembly: fine operator, Galerkin hierarchy, D^-1,
-// lambda_max per level.
+// smoothing stencils, lambda_max per level.
 template <typename T>
 void mg_setup(Ctx& c, MG<T>& mg) {
     mg_build<T>(c, mg);
@@ -618,13 +554,15 @@ void mg_setup(Ctx& c, MG<T>& mg) {
             c.launches += 1;
         }
         k_mg_dinv<T><<<grid_for(c, L.N), kThreads, 0, c.stream>>>(L.N, L.K, L.Di);
+        mg_store(c, mg, l);
         k_mg_power_init<T><<<grid_for(c, L.N), kThreads, 0, c.stream>>>(L.N, L.mask, L.d0);
         c.launches += 2;
+        const LevelView<T> V = level_view(mg, l);
         T* v = L.d0;
         T* w = L.d1;
         for (int it = 0; it < kPowerIters; ++it) {
-            k_mg_power<T><<<grid_for(c, L.N), kThreads, 0, c.stream>>>(
-                L.n, L.K, L.Di, L.mask, v, w, mg.lam + l, it == 0, c.red);
+            k_mg_power<T><<<grid_for(c, L.N), kThreads, 0, c.stream>>>(V, v, w, mg.lam + l,
+                                                                        it == 0, c.red);
             c.launches += 1;
             T* t = v;
             v = w;
@@ -651,76 +589,105 @@ void mg_setup(Ctx& c, MG<T>& mg) {
     FTS_CUDA(cudaStreamSynchronize(c.stream));
 }
 
+// One level of the V-cycle; L.d0 holds the first Chebyshev direction of L.b.
 template <typename T>
-static void vcycle_level(Ctx& c, MG<T>& mg, size_t l, const int* stop) {
-    MGLevel<T>& L = mg.L[l];
+static void vcycle_level(Ctx& c, MG<T>& mg, size_t l, const int* stop, bool skip_final) {
+    const LevelView<T> L = level_view(mg, l);
     const int g = grid_for(c, L.N);
-    const double* lam = mg.coef + l * kCoefStride;
-    if (l + 1 == mg.L.size()) {
-        k_mg_coarse_solve<T><<<1, kCoarseThreads, 0, c.stream>>>(
-            L.n, L.K, L.Di, L.b, L.x, L.r, L.d0, L.d1, lam, L.n == 3 ? 1 : kCoarse, stop);
+    if ((int)l == mg.tail_level) {
+        MGTailArgs<T> a{};
+        for (size_t k = 0; k < mg.L.size(); ++k) a.lv[k] = level_view(mg, k);
+        a.l0 = (int)l;
+        a.nlev = (int)mg.L.size();
+        a.skip_final = skip_final ? 1 : 0;
+        cudaLaunchConfig_t lc = {};
+        lc.gridDim = dim3((unsigned)mg.tail_blocks);
+        lc.blockDim = dim3((unsigned)kThreads);
+        lc.stream = c.stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        lc.attrs = attr;
+        lc.numAttrs = 1;
+        FTS_CUDA(cudaLaunchKernelEx(&lc, k_mg_tail<T>, a, mg.bar, stop));
         c.launches += 1;
         return;
     }
-    MGLevel<T>& C = mg.L[l + 1];
-    // pre-smoothing from zero
-    k_mg_smooth_first<T><<<g, kThreads, 0, c.stream>>>(L.n, L.K, L.Di, L.b, L.x, L.r, L.d0, lam,
-                                                      0, stop);
+    if (l + 1 == mg.L.size()) {
+        k_mg_coarse_solve<T><<<1, kCoarseThreads, 0, c.stream>>>(L, L.n == 3 ? 1 : kCoarse, stop);
+        c.launches += 1;
+        return;
+    }
+    const LevelView<T> C = level_view(mg, l + 1);
+    // pre-smoothing from zero (d_0 is already in L.d0)
     T* din = L.d0;
     T* dout = L.d1;
     for (int s = 1; s < kSmooth; ++s) {
-        k_mg_smooth_step<T><<<g, kThreads, 0, c.stream>>>(L.n, L.K, L.Di, din, dout, L.r, L.x,
-                                                         lam, s, stop);
-        T* t = din;
-        din = dout;
-        dout = t;
+        k_mg_step<T><<<g, kThreads, 0, c.stream>>>(L, s, s == 1 ? kStepFromZero : kStepRegular,
+                                                   din, dout, stop);
+        std::swap(din, dout);
     }
-    k_mg_residual<T><<<g, kThreads, 0, c.stream>>>(L.n, L.K, L.b, L.x, L.r, stop);
-    k_mg_restrict<T><<<grid_for(c, C.N), kThreads, 0, c.stream>>>(L.n, L.r, L.mask, C.n, C.b,
-                                                                 C.mask, stop);
-    c.launches += kSmooth + 2;
-    vcycle_level<T>(c, mg, l + 1, stop);
-    k_mg_prolong<T><<<g, kThreads, 0, c.stream>>>(L.n, L.x, L.mask, C.n, C.x, C.mask, stop);
+    k_mg_residual<T><<<g, kThreads, 0, c.stream>>>(L, stop);
+    k_mg_restrict<T><<<grid_for(c, C.N), kThreads, 0, c.stream>>>(L, C, stop);
+    c.launches += kSmooth + 1;
+    vcycle_level<T>(c, mg, l + 1, stop, false);
+    k_mg_prolong<T><<<g, kThreads, 0, c.stream>>>(L, C, stop);
     // post-smoothing from the corrected x
-    k_mg_residual<T><<<g, kThreads, 0, c.stream>>>(L.n, L.K, L.b, L.x, L.r, stop);
-    k_mg_smooth_first<T><<<g, kThreads, 0, c.stream>>>(L.n, L.K, L.Di, L.b, L.x, L.r, L.d0, lam,
-                                                      1, stop);
+    k_mg_resid_first<T><<<g, kThreads, 0, c.stream>>>(L, stop);
+    c.launches += 2;
     din = L.d0;
     dout = L.d1;
     for (int s = 1; s < kSmooth; ++s) {
-        k_mg_smooth_step<T><<<g, kThreads, 0, c.stream>>>(L.n, L.K, L.Di, din, dout, L.r, L.x,
-                                                         lam, s, stop);
-        T* t = din;
-        din = dout;
-        dout = t;
+        if (skip_final && s == kSmooth - 1) break;
+        k_mg_step<T><<<g, kThreads, 0, c.stream>>>(L, s, s == 1 ? kStepAfterFirst : kStepRegular,
+                                                   din, dout, stop);
+        std::swap(din, dout);
+        c.launches += 1;
     }
-    c.launches += kSmooth + 2;
 }
 
 template <typename T>
-void mg_vcycle(Ctx& c, MG<T>& mg, const int* stop) {
-    vcycle_level<T>(c, mg, 0, stop);
+void mg_vcycle(Ctx& c, MG<T>& mg, const int* stop, bool skip_final) {
+    vcycle_level<T>(c, mg, 0, stop, skip_final);
     FTS_CUDA(cudaGetLastError());
 }
 
 template <typename T>
 void mg_free(MG<T>& mg) {
-    for (auto& L : mg.L)
+    for (auto& L : mg.L) {
+        if (L.Kh && (void*)L.Kh != (void*)L.K) cudaFree(L.Kh);
         for (void* p : {(void*)L.K, (void*)L.Di, (void*)L.b, (void*)L.x, (void*)L.r, (void*)L.d0,
                         (void*)L.d1, (void*)L.mask})
             if (p) cudaFree(p);
-    if (mg.lam) cudaFree(mg.lam);
-    if (mg.coef) cudaFree(mg.coef);
-    mg.coef = nullptr;
-    mg.L.clear();
+    }
+    for (void* p : {(void*)mg.lam, (void*)mg.coef, (void*)mg.scale, (void*)mg.maxbits,
+                    (void*)mg.bar})
+        if (p) cudaFree(p);
+    mg.bar = nullptr;
+    mg.tail_level = -1;
     mg.lam = nullptr;
+    mg.coef = nullptr;
+    mg.scale = nullptr;
+    mg.maxbits = nullptr;
+    mg.L.clear();
     mg.built = false;
 }
 
+template <typename T>
+bool mg_barrier_failed(Ctx& c, MG<T>& mg) {
+    if (!mg.bar) return false;
+    BarrierState b;
+    FTS_CUDA(cudaMemcpyAsync(&b, mg.bar, sizeof(b), cudaMemcpyDeviceToHost, c.stream));
+    FTS_CUDA(cudaStreamSynchronize(c.stream));
+    return b.error != 0;
+}
+
+template bool mg_barrier_failed<double>(Ctx&, MG<double>&);
+template bool mg_barrier_failed<float>(Ctx&, MG<float>&);
 template void mg_setup<double>(Ctx&, MG<double>&);
 template void mg_setup<float>(Ctx&, MG<float>&);
-template void mg_vcycle<double>(Ctx&, MG<double>&, const int*);
-template void mg_vcycle<float>(Ctx&, MG<float>&, const int*);
+template void mg_vcycle<double>(Ctx&, MG<double>&, const int*, bool);
+template void mg_vcycle<float>(Ctx&, MG<float>&, const int*, bool);
 template void mg_free<double>(MG<double>&);
 template void mg_free<float>(MG<float>&);
 

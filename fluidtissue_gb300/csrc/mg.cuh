@@ -1,23 +1,45 @@
 // Geometric multigrid hierarchy on Kuhn lattices (internal).
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include <cstdint>
 #include <vector>
 
 namespace fts {
 
 struct Ctx;
+struct BarrierState;
 
 constexpr int kSmooth = 2;        // Chebyshev degree of each pre / post smoothing
 constexpr int kCoarse = 20;       // Chebyshev degree of the coarsest-level solve
 constexpr int kPowerIters = 12;   // power iterations for lambda_max(D^-1 K)
 constexpr double kLamSafety = 1.1;
+constexpr int kCoefStride = 64;   // per level: 1/theta, then (ca_s, cb_s) for s >= 1
+constexpr int kMaxMGLevels = 10;  // levels of one hierarchy (n <= 513)
+constexpr int64_t kTailNodes = 40000;  // levels this small run in one persistent launch
+
+// Storage of the smoothing operator: the FP32 hierarchy keeps its stencils in
+// FP16 (scaled per level by max|K| / 16384; arithmetic stays FP32), the FP64
+// hierarchy in FP64.
+template <typename T>
+struct MGStore;
+template <>
+struct MGStore<float> {
+    using type = __half;
+};
+template <>
+struct MGStore<double> {
+    using type = double;
+};
 
 template <typename T>
 struct MGLevel {
+    using KS = typename MGStore<T>::type;
     int n = 0;
     int64_t N = 0;
-    T* K = nullptr;      // [15 directions][9 entries][N]
+    T* K = nullptr;      // half stencil in T (Galerkin construction), tiles of 32 nodes x 72
+    KS* Kh = nullptr;    // the stencil the V-cycle reads (== K when KS is T)
     T* Di = nullptr;     // [6][N] inverse 3x3 node blocks (xx xy xz yy yz zz)
     T* b = nullptr;      // [3][N] right-hand side
     T* x = nullptr;      // [3][N] solution
@@ -32,18 +54,42 @@ struct MG {
     std::vector<MGLevel<T>> L;
     double* lam = nullptr;           // device: lambda_max per level (with safety factor)
     double* coef = nullptr;          // device: Chebyshev coefficients per level
+    double* scale = nullptr;         // device: stencil scale per level (Kh * scale = K)
+    unsigned* maxbits = nullptr;     // device: max |K| per level (float bits)
     std::vector<double> lam_host;
     bool built = false;
+    // levels tail_level.. of every V-cycle run in one cooperative launch of
+    // tail_blocks blocks (grid barriers between phases); -1: none
+    int tail_level = -1;
+    int tail_blocks = 0;
+    BarrierState* bar = nullptr;
 };
 
 // Nodes per axis of the next coarser lattice.
 inline int mg_coarse_n(int n) { return n % 2 ? (n + 1) / 2 : n / 2 + 1; }
 
+// Nodes per axis of every level, finest first (coarsening stops below 5).
+inline std::vector<int> mg_chain(int n) {
+    std::vector<int> out;
+    while (true) {
+        out.push_back(n);
+        if (n < 5) break;
+        n = mg_coarse_n(n);
+    }
+    return out;
+}
+
 template <typename T>
 void mg_setup(Ctx& c, MG<T>& mg);
+// V-cycle on mg.L[0].b, whose first Chebyshev direction L[0].d0 the caller has
+// written.  skip_final leaves out the last post-smoothing step of the finest
+// level, which the caller then runs fused with its own epilogue.
 template <typename T>
-void mg_vcycle(Ctx& c, MG<T>& mg, const int* stop);
+void mg_vcycle(Ctx& c, MG<T>& mg, const int* stop, bool skip_final);
 template <typename T>
 void mg_free(MG<T>& mg);
+// True when a grid barrier of the persistent coarse-level launch timed out.
+template <typename T>
+bool mg_barrier_failed(Ctx& c, MG<T>& mg);
 
 }  // namespace fts

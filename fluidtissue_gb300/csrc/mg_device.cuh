@@ -1,0 +1,297 @@
+// Per-node bodies of the multigrid V-cycle (internal), shared by the
+// single-solve kernels (mg.cu, krylov.cu) and the batched persistent kernel
+// (batch.cu).  Lattice offsets are compile-time functions.
+//
+// Chebyshev smoothing of degree kSmooth on [lambda/10, lambda] of D^-1 K:
+//   d_0 = D^-1 r_0 / theta;  r_s = r_{s-1} - K d_{s-1};
+//   d_s = ca_s d_{s-1} + cb_s D^-1 r_s;  x_s = x_{s-1} + d_s.
+// The first direction d_0 is pointwise, so it is produced together with the
+// level's right-hand side (by the restriction, or by the preconditioner stage
+// that writes the finest b) or with the post-smoothing residual; the x update
+// of d_0 is deferred to the next step so that no kernel writes x while
+// another thread of it reads x at a neighbour.
+#pragma once
+
+#include "fts_device.cuh"
+
+namespace fts {
+
+// The 15 Kuhn directions: 0 = self, 1..7 = (1,0,0) (0,1,0) (0,0,1) (1,1,0)
+// (1,0,1) (0,1,1) (1,1,1), 8..14 = their negatives.
+__host__ __device__ __forceinline__ constexpr int off_x(int d) {
+    return (d == 1 || d == 4 || d == 5 || d == 7) ? 1
+                                                   : ((d == 8 || d == 11 || d == 12 || d == 14) ? -1 : 0);
+}
+__host__ __device__ __forceinline__ constexpr int off_y(int d) {
+    return (d == 2 || d == 4 || d == 6 || d == 7) ? 1
+                                                   : ((d == 9 || d == 11 || d == 13 || d == 14) ? -1 : 0);
+}
+__host__ __device__ __forceinline__ constexpr int off_z(int d) {
+    return (d == 3 || d == 5 || d == 6 || d == 7) ? 1
+                                                   : ((d == 10 || d == 12 || d == 13 || d == 14) ? -1 : 0);
+}
+
+// Tiled stencil layout: 32 consecutive nodes share one tile of kStored x 32
+// values (entry q = 9 d + 3 r + c, d = 0..7), so the loads of a warp stay
+// inside one contiguous region.
+constexpr int kStored = 72;
+__host__ __device__ __forceinline__ int64_t kidx(int q, int64_t v) {
+    return ((v >> 5) * kStored + q) * 32 + (v & 31);
+}
+
+__device__ __forceinline__ int nbr(int i, int j, int k, int d, int n) {
+    const int a = i + off_x(d), b = j + off_y(d), c = k + off_z(d);
+    if (a < 0 || b < 0 || c < 0 || a >= n || b >= n || c >= n) return -1;
+    return a + n * (b + n * c);
+}
+
+template <typename T>
+__device__ __forceinline__ T ldk(const T* p) {
+    return *p;
+}
+template <typename T>
+__device__ __forceinline__ T ldk(const __half* p) {
+    return (T)__half2float(*p);
+}
+
+// One level of a hierarchy as the kernels see it.
+template <typename T>
+struct LevelView {
+    using KS = typename MGStore<T>::type;
+    int n;
+    int64_t N;
+    const KS* K;
+    const double* ks;    // stencil scale
+    const T* Di;
+    T* b;
+    T* x;
+    T* r;
+    T* d0;
+    T* d1;
+    const uint8_t* mask;
+    const double* coef;  // 1/theta, (ca_s, cb_s) for s >= 1
+};
+
+template <typename T>
+inline LevelView<T> level_view(const MG<T>& mg, size_t l) {
+    const MGLevel<T>& L = mg.L[l];
+    return LevelView<T>{L.n, L.N, L.Kh, mg.scale + l, L.Di, L.b, L.x, L.r, L.d0, L.d1, L.mask,
+                        mg.coef + l * kCoefStride};
+}
+
+// y = K x at node v (3 components, without the level's scale); x SoA [3][N].
+// 32-bit lattice coordinates; interior nodes take the neighbour offsets
+// without range checks.
+template <typename T, typename KS>
+__device__ __forceinline__ void stencil_apply(int n, int64_t N, int64_t v64,
+                                              const KS* __restrict__ K,
+                                              const T* __restrict__ x, T y[3]) {
+    const int v = (int)v64;
+    const int nn = n * n;
+    const int k = v / nn;
+    const int rem = v - k * nn;
+    const int j = rem / n;
+    const int i = rem - j * n;
+    const bool inner = i > 0 && j > 0 && k > 0 && i < n - 1 && j < n - 1 && k < n - 1;
+    T a0 = T(0), a1 = T(0), a2 = T(0);
+#pragma unroll
+    for (int d = 0; d < 8; ++d) {  // self and positive directions: own blocks
+        const int w = inner ? v + off_x(d) + n * off_y(d) + nn * off_z(d) : nbr(i, j, k, d, n);
+        if (w < 0) continue;
+        const T x0 = x[w], x1 = x[N + w], x2 = x[2 * N + w];
+        const KS* kb = K + kidx(d * 9, v64);
+        a0 = fma(ldk<T>(kb), x0, fma(ldk<T>(kb + 32), x1, fma(ldk<T>(kb + 64), x2, a0)));
+        a1 = fma(ldk<T>(kb + 96), x0, fma(ldk<T>(kb + 128), x1, fma(ldk<T>(kb + 160), x2, a1)));
+        a2 = fma(ldk<T>(kb + 192), x0, fma(ldk<T>(kb + 224), x1, fma(ldk<T>(kb + 256), x2, a2)));
+    }
+#pragma unroll
+    for (int d = 1; d < 8; ++d) {  // negative directions: neighbour's block, transposed
+        const int w = inner ? v - off_x(d) - n * off_y(d) - nn * off_z(d) : nbr(i, j, k, d + 7, n);
+        if (w < 0) continue;
+        const T x0 = x[w], x1 = x[N + w], x2 = x[2 * N + w];
+        const KS* kb = K + kidx(d * 9, (int64_t)w);
+        a0 = fma(ldk<T>(kb), x0, fma(ldk<T>(kb + 96), x1, fma(ldk<T>(kb + 192), x2, a0)));
+        a1 = fma(ldk<T>(kb + 32), x0, fma(ldk<T>(kb + 128), x1, fma(ldk<T>(kb + 224), x2, a1)));
+        a2 = fma(ldk<T>(kb + 64), x0, fma(ldk<T>(kb + 160), x1, fma(ldk<T>(kb + 256), x2, a2)));
+    }
+    y[0] = a0;
+    y[1] = a1;
+    y[2] = a2;
+}
+
+template <typename T>
+__device__ __forceinline__ void dinv_apply(int64_t N, int64_t v, const T* __restrict__ Di,
+                                           const T r[3], T z[3]) {
+    const T d0 = Di[v], d1 = Di[N + v], d2 = Di[2 * N + v], d3 = Di[3 * N + v],
+            d4 = Di[4 * N + v], d5 = Di[5 * N + v];
+    z[0] = d0 * r[0] + d1 * r[1] + d2 * r[2];
+    z[1] = d1 * r[0] + d3 * r[1] + d4 * r[2];
+    z[2] = d2 * r[0] + d4 * r[1] + d5 * r[2];
+}
+
+// d_0 = D^-1 b / theta at node v, from the right-hand side value bv.
+template <typename T>
+__device__ __forceinline__ void mg_first_dir(const LevelView<T>& L, int64_t v, const T bv[3]) {
+    const T ith = (T)L.coef[0];
+    T z[3];
+    dinv_apply<T>(L.N, v, L.Di, bv, z);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) L.d0[c * L.N + v] = z[c] * ith;
+}
+
+// Step modes: how r and x enter the step.
+enum : int {
+    kStepRegular = 0,  // r -= K d_in; x += d_out
+    kStepFromZero = 1, // x was 0 and d_in = d_0: r = b - K d_in; x = d_in + d_out
+    kStepAfterFirst = 2 // r holds b - K x and d_in = d_0 (x not yet updated):
+                        // r -= K d_in; x += d_in + d_out
+};
+
+// Chebyshev step s >= 1 at node v.  Returns the new x value (3 components),
+// written to L.x unless `out` is non-null (the fused caller writes it).
+template <typename T>
+__device__ __forceinline__ void mg_step_node(const LevelView<T>& L, int64_t v, int step, int mode,
+                                             const T* __restrict__ din, T* __restrict__ dout,
+                                             T xo[3], bool write_x, bool write_rd) {
+    const int64_t N = L.N;
+    const T A = (T)L.coef[2 * step - 1], B = (T)L.coef[2 * step];
+    const T ks = (T)*L.ks;
+    T y[3], rr[3], z[3];
+    stencil_apply<T>(L.n, N, v, L.K, din, y);
+    const T* rin = mode == kStepFromZero ? L.b : L.r;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) rr[c] = rin[c * N + v] - ks * y[c];
+    dinv_apply<T>(N, v, L.Di, rr, z);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const T di = din[c * N + v];
+        const T dd = A * di + B * z[c];
+        if (write_rd) {
+            L.r[c * N + v] = rr[c];
+            dout[c * N + v] = dd;
+        }
+        T xv;
+        if (mode == kStepFromZero) xv = di + dd;
+        else if (mode == kStepAfterFirst) xv = L.x[c * N + v] + di + dd;
+        else xv = L.x[c * N + v] + dd;
+        xo[c] = xv;
+        if (write_x) L.x[c * N + v] = xv;
+    }
+}
+
+// r = b - K x at node v.
+template <typename T>
+__device__ __forceinline__ void mg_resid_node(const LevelView<T>& L, int64_t v) {
+    const int64_t N = L.N;
+    const T ks = (T)*L.ks;
+    T y[3];
+    stencil_apply<T>(L.n, N, v, L.K, L.x, y);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) L.r[c * N + v] = L.b[c * N + v] - ks * y[c];
+}
+
+// r = b - K x and d_0 = D^-1 r / theta at node v (x is left for the next step).
+template <typename T>
+__device__ __forceinline__ void mg_resid_first_node(const LevelView<T>& L, int64_t v) {
+    const int64_t N = L.N;
+    const T ks = (T)*L.ks;
+    T y[3], rr[3];
+    stencil_apply<T>(L.n, N, v, L.K, L.x, y);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        rr[c] = L.b[c * N + v] - ks * y[c];
+        L.r[c * N + v] = rr[c];
+    }
+    mg_first_dir<T>(L, v, rr);
+}
+
+// b_c(I) = sum_a w_a r_f(2I + off[a])  (P^T r), zero on Dirichlet nodes; then
+// the coarse level's first direction.
+template <typename T>
+__device__ __forceinline__ void mg_restrict_node(const LevelView<T>& F, const LevelView<T>& C,
+                                                 int64_t I) {
+    const int nf = F.n, nc = C.n;
+    const int64_t Nf = F.N, Nc = C.N;
+    T a[3] = {T(0), T(0), T(0)};
+    if (!C.mask[I]) {
+        const int ci = (int)(I % nc), cj = (int)((I / nc) % nc), ck = (int)(I / ((int64_t)nc * nc));
+#pragma unroll
+        for (int d = 0; d < 15; ++d) {
+            const int f = nbr(2 * ci, 2 * cj, 2 * ck, d, nf);
+            if (f < 0 || F.mask[f]) continue;
+            const T w = d == 0 ? T(1) : T(0.5);
+            a[0] += w * F.r[f];
+            a[1] += w * F.r[Nf + f];
+            a[2] += w * F.r[2 * Nf + f];
+        }
+    }
+    C.b[I] = a[0];
+    C.b[Nc + I] = a[1];
+    C.b[2 * Nc + I] = a[2];
+    mg_first_dir<T>(C, I, a);
+}
+
+// x_f(f) += sum_{parents J} w x_c(J)  (P e).
+template <typename T>
+__device__ __forceinline__ void mg_prolong_node(const LevelView<T>& F, const LevelView<T>& C,
+                                                int64_t f) {
+    if (F.mask[f]) return;
+    const int nf = F.n, nc = C.n;
+    const int64_t Nf = F.N, Nc = C.N;
+    const int fi = (int)(f % nf), fj = (int)((f / nf) % nf), fk = (int)(f / ((int64_t)nf * nf));
+    const int Ai = fi >> 1, Aj = fj >> 1, Ak = fk >> 1;
+    const int oi = fi & 1, oj = fj & 1, ok = fk & 1;
+    T s0 = T(0), s1 = T(0), s2 = T(0);
+    const int64_t A = Ai + (int64_t)nc * (Aj + (int64_t)nc * Ak);
+    if ((oi | oj | ok) == 0) {
+        if (!C.mask[A]) {
+            s0 = C.x[A];
+            s1 = C.x[Nc + A];
+            s2 = C.x[2 * Nc + A];
+        }
+    } else {
+        const int64_t Bn = (Ai + oi) + (int64_t)nc * ((Aj + oj) + (int64_t)nc * (Ak + ok));
+        if (!C.mask[A]) {
+            s0 += T(0.5) * C.x[A];
+            s1 += T(0.5) * C.x[Nc + A];
+            s2 += T(0.5) * C.x[2 * Nc + A];
+        }
+        if (!C.mask[Bn]) {
+            s0 += T(0.5) * C.x[Bn];
+            s1 += T(0.5) * C.x[Nc + Bn];
+            s2 += T(0.5) * C.x[2 * Nc + Bn];
+        }
+    }
+    F.x[f] += s0;
+    F.x[Nf + f] += s1;
+    F.x[2 * Nf + f] += s2;
+}
+
+// Coarsest level: `steps` Chebyshev steps from zero on L.b by the calling CTA
+// alone (every thread of the block must call it).
+template <typename T>
+__device__ __forceinline__ void mg_coarse_block(const LevelView<T>& L, int steps) {
+    const int64_t N = L.N;
+    for (int64_t v = threadIdx.x; v < N; v += blockDim.x) {
+        const T bv[3] = {L.b[v], L.b[N + v], L.b[2 * N + v]};
+        mg_first_dir<T>(L, v, bv);
+    }
+    __syncthreads();
+    T xo[3];
+    if (steps == 1) {
+        for (int64_t v = threadIdx.x; v < N; v += blockDim.x)
+            for (int c = 0; c < 3; ++c) L.x[c * N + v] = L.d0[c * N + v];
+        __syncthreads();
+        return;
+    }
+    for (int s = 1; s < steps; ++s) {
+        const T* din = (s & 1) ? L.d0 : L.d1;
+        T* dout = (s & 1) ? L.d1 : L.d0;
+        const int mode = s == 1 ? kStepFromZero : kStepRegular;
+        for (int64_t v = threadIdx.x; v < N; v += blockDim.x)
+            mg_step_node<T>(L, v, s, mode, din, dout, xo, true, true);
+        __syncthreads();
+    }
+}
+
+}  // namespace fts

@@ -62,9 +62,13 @@ enum {
 
 /* Operator representation. */
 enum {
-    FTS_OP_AUTO = 0,       /* assembled BSR */
-    FTS_OP_ASSEMBLED = 1,  /* node-blocked 4x4 BSR, assembled every solve */
-    FTS_OP_MATFREE = 2     /* element-by-element operator for the FP32 inner solve */
+    FTS_OP_AUTO = 0,       /* FTS_OP_STENCIL on Kuhn lattices, else FTS_OP_ASSEMBLED */
+    FTS_OP_ASSEMBLED = 1,  /* node-blocked 4x4 BSR, assembled every solve; the FP32 inner
+                              solve reads a sliced-ELL copy */
+    FTS_OP_MATFREE = 2,    /* element-by-element operator for the FP32 inner solve */
+    FTS_OP_STENCIL = 3     /* assembled BSR; the FP32 inner solve reads a symmetric half
+                              stencil (self + 7 positive Kuhn directions, 8 blocks per
+                              node) of it.  Kuhn lattices only. */
 };
 
 /* Mesh3D (src/fem/TetraMesh.hpp:49-62).  The library copies what it needs

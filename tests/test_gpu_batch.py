@@ -13,8 +13,18 @@ def _instances(count=6, nmin=9, nmax=17):
     return [W.batch_instance(i, nmin, nmax) for i in range(count)]
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_batch_matches_oracle(precision):
+def _renumbered(inst, seed=1):
+    """The same instance with its nodes renumbered (no longer in lattice order:
+    the batch treats it as a general mesh, block Jacobi)."""
+    perm = np.random.default_rng(seed).permutation(inst.np).astype(np.int32)
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(inst.np, dtype=np.int32)
+    return perm, inv
+
+
+@pytest.mark.parametrize("precision,pc", [("fp64", "auto"), ("mixed", "auto"),
+                                          ("mixed", "jacobi")])
+def test_batch_matches_oracle(precision, pc):
     import oracle as O
     from fluidtissue_gb300.flow import Batch, Mesh
     insts = _instances()
@@ -24,7 +34,7 @@ def test_batch_matches_oracle(precision):
         par["Stokes tolerance"] = 1e-10
         pars.append(par)
     b = Batch([Mesh(i.xyz, i.tets) for i in insts], pars, precision=precision,
-              warm_start=False)
+              warm_start=False, preconditioner=pc)
     flows = [np.zeros(4 * i.np) for i in insts]
     rc = b.solve([i.phi for i in insts], [i.source for i in insts], flows,
                  mus=[i.mu for i in insts])
@@ -68,3 +78,41 @@ def test_batch_zero_load_instance_left_untouched():
     assert b.last_stats[1]["solved"] == 0 and np.all(flows[1] == 3.0)
     assert b.last_stats[0]["solved"] == 1 and not np.all(flows[0] == 3.0)
     b.close()
+
+
+def test_batch_multigrid_and_jacobi_instances_together():
+    """A batch whose instances mix lattice meshes (multigrid V-cycle inside the
+    persistent launch) and a renumbered mesh (block Jacobi): every instance
+    equals its own single solve, and multigrid instances need fewer iterations
+    than the same instance under Jacobi."""
+    from fluidtissue_gb300.flow import Batch, Flow, Mesh
+    insts = _instances(5, 9, 16)
+    meshes = [Mesh(i.xyz, i.tets) for i in insts]
+    perm, inv = _renumbered(insts[2])
+    meshes[2] = Mesh(insts[2].xyz[perm], inv[insts[2].tets])
+    phis = [i.phi for i in insts]
+    srcs = [i.source for i in insts]
+    phis[2], srcs[2] = insts[2].phi[perm], insts[2].source[perm]
+    pars = [dict(i.params, **{"Stokes tolerance": 1e-10}) for i in insts]
+    b = Batch(meshes, pars, precision="mixed", warm_start=False)
+    flows = [np.zeros(4 * i.np) for i in insts]
+    rc = b.solve(phis, srcs, flows, mus=[i.mu for i in insts])
+    assert rc == 0, b.last_error()
+    its_batch = [s["iterations"] for s in b.last_stats]
+    b.close()
+    for k, inst in enumerate(insts):
+        single = {}
+        for pc in ("auto", "jacobi"):
+            f = Flow()
+            assert f.init(meshes[k], pars[k], precision="mixed", warm_start=False,
+                          preconditioner=pc) == 0, f.last_error()
+            fl = np.zeros(4 * inst.np)
+            assert f.solve(phis[k], srcs[k], fl, mu=inst.mu) == 0, f.last_error()
+            single[pc] = (fl, f.last_stats["iterations"])
+            f.close()
+        ref = single["auto"][0]
+        npn = inst.np
+        ev = np.linalg.norm(flows[k][:3 * npn] - ref[:3 * npn]) / np.linalg.norm(ref[:3 * npn])
+        assert ev <= 1e-7, (k, ev)
+        if k != 2:
+            assert its_batch[k] < single["jacobi"][1], (k, its_batch[k], single["jacobi"][1])
