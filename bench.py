@@ -454,6 +454,108 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+# Fig. 5-6 growth parameters of the reference's parameter summary
+# (parameters/summary.txt): 32000 explicit Euler steps of 1/32 per RD call.
+RD_PAR = {"RD dt": 1.0 / 32.0, "RD iterations": 32000.0, "Act": 2.0, "Da": 5.0e-6,
+          "DegA": 0.01, "Inh": 1.0, "Di": 7.5e-5, "DegI": 0.02, "GF production": 40.0,
+          "GF diffusion": 1.25e-4, "GF degradation": 0.02, "GF inhibition": 200.0}
+
+
+def _rd_sources(inst, count=16):
+    """Interior nodes nearest `count` seeded points of the level set's interior
+    (stand-ins for the signalling centres' source nodes)."""
+    inside = np.where(inst.phi < 0)[0]
+    pick = np.linspace(0, len(inside) - 1, count).astype(int)
+    return inside[pick].astype(np.int32)
+
+
+def run_rd(args):
+    """Reaction-diffusion (RD::solve) on the ellipsoid129 mesh and level set:
+    value = RD calls/s, one call = 32000 FP64 explicit Euler steps of the
+    activator, inhibitor and growth factor on the interior submesh (all steps
+    in one persistent launch).  The state is copied in from and out to host
+    memory every call (the reference's RD keeps it on the host)."""
+    import torch
+    from fluidtissue_gb300 import workloads as W
+    from fluidtissue_gb300.flow import Mesh
+    from fluidtissue_gb300.rd import RD
+
+    ws, rank, local = _dist()
+    dist = _setup_dist(ws, local)
+    torch.cuda.set_device(local)
+    inst = W.ellipsoid129()
+    src = _rd_sources(inst)
+    rd = RD()
+    if rd.init(Mesh(inst.xyz, inst.tets), inst.phi, RD_PAR, device=local) != 0:
+        raise RuntimeError(f"fts_rd_create failed: {rd.last_error()}")
+    a0, i0, g0 = rd.activator.copy(), rd.inhibitor.copy(), rd.growth_factor.copy()
+
+    def step():
+        rd.set_state(a0, i0, g0)
+        rc = rd.solve(inst.phi, src)
+        if rc != 0:
+            raise RuntimeError(f"fts_rd_solve failed ({rc}): {rd.last_error()}")
+        return rd.last_stats
+
+    for _ in range(args.warmup):
+        step()
+    _barrier(dist)
+    clk = Clocks(local)
+    t0 = time.perf_counter()
+    stats = [step() for _ in range(args.steps)]
+    wall = (time.perf_counter() - t0) * 1e3
+    clocks = clk.stop()
+    ms = _max_over_ranks(wall, dist)
+    ms_dev = statistics.mean(s["ms_steps"] for s in stats)
+    st = stats[-1]
+    n_steps = int(RD_PAR["RD iterations"])
+    nint = st["interior_nodes"]
+    res = {"metric": "RD calls/s (32000 FP64 Euler steps, ellipsoid129 interior)",
+           "value": round(ws * args.steps / (ms / 1e3), 4), "unit": "calls/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (ellipsoid129 level set; activator ramp x + 1; 16 source nodes)",
+           "config": {"workload": f"rd129: {nint} interior nodes, "
+                                  f"{st['interior_elements']} interior tets, {n_steps} steps"},
+           "e2e": {"value": round(ws * args.steps / (ms / 1e3), 4), "unit": "calls/s",
+                   "h2d_bytes_per_step": 4 * 8 * inst.np + 4 * len(src),
+                   "d2h_bytes_per_step": 3 * 8 * inst.np},
+           "device_steps_per_s": round(n_steps / (ms_dev / 1e3), 1),
+           "ms_device_per_call": round(ms_dev, 3), "ms_setup": round(st["ms_setup"], 3),
+           "node_steps_per_s": round(nint * n_steps / (ms_dev / 1e3), 1),
+           "gpu_launches": int(st["kernel_launches"]), "clocks": clocks}
+    if rank == 0 and not args.no_cpu_baseline:
+        res["cpu_baseline"] = rd_cpu_baseline(inst, src, a0, i0, g0, n_steps)
+    if rank == 0:
+        print(json.dumps(res), flush=True)
+    rd.close()
+
+
+def rd_cpu_baseline(inst, src, a0, i0, g0, n_steps, sample_steps=200):
+    """The oracle's RD restatement (OpenMP, FP64) on this host: the Laplacian
+    assembly in full plus `sample_steps` Euler steps, scaled to n_steps."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    par = dict(RD_PAR)
+    a, i, g = a0.copy(), i0.copy(), g0.copy()
+    par["RD iterations"] = 1.0
+    t0 = time.perf_counter()
+    O.rd_solve(inst.xyz, inst.tets, inst.phi, src, par, a, i, g)
+    t_one = time.perf_counter() - t0
+    par["RD iterations"] = float(sample_steps + 1)
+    t0 = time.perf_counter()
+    O.rd_solve(inst.xyz, inst.tets, inst.phi, src, par, a, i, g)
+    t_more = time.perf_counter() - t0
+    t_step = max(t_more - t_one, 0.0) / sample_steps
+    t_setup = max(t_one - t_step, 0.0)
+    total = t_setup + n_steps * t_step
+    return {"value": 1.0 / total, "unit": "calls/s", "cores": O.num_threads(), "kind": "port",
+            "sample": (f"oracle RD on the same interior ({O.num_threads()} threads): set-up "
+                       f"{t_setup:.2f} s + {sample_steps} steps of {t_step * 1e3:.3f} ms, "
+                       f"scaled to {n_steps} steps"),
+            "t_setup_s": t_setup, "t_step_s": t_step}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -476,6 +578,8 @@ def main():
         run_reference(args)
     elif args.workload.startswith("batch"):
         run_batch(args)
+    elif args.workload == "rd129":
+        run_rd(args)
     else:
         run_ours(args)
 

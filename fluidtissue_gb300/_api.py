@@ -84,6 +84,36 @@ class FtsBatchConfig(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class FtsRdParams(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double),
+        ("iterations", C.c_int64),
+        ("act", C.c_double), ("da", C.c_double), ("dega", C.c_double),
+        ("inh", C.c_double), ("di", C.c_double), ("degi", C.c_double),
+        ("gf_production", C.c_double),
+        ("gf_diffusion", C.c_double),
+        ("gf_degradation", C.c_double),
+        ("gf_inhibition", C.c_double),
+    ]
+
+
+class FtsRdStats(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32),
+        ("alive", C.c_int32),
+        ("interior_nodes", C.c_int64),
+        ("interior_elements", C.c_int64),
+        ("steps", C.c_int64),
+        ("ms_setup", C.c_double),
+        ("ms_steps", C.c_double),
+        ("ms_total", C.c_double),
+        ("kernel_launches", C.c_int64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_MINRES, SOLVER_BICGSTAB = 0, 1
 PC_AUTO, PC_JACOBI, PC_MULTIGRID = 0, 1, 2
@@ -121,6 +151,11 @@ SIGNATURES = {
     "fts_batch_set_stream": (C.c_int, [_vp, _vp]),
     "fts_batch_last_error": (C.c_char_p, [_vp]),
     "fts_batch_destroy": (None, [_vp]),
+    "fts_rd_create": (C.c_int, [_P(FtsMesh), C.c_int32, _P(_vp)]),
+    "fts_rd_solve": (C.c_int, [_vp, _P(FtsRdParams), _dp, _P(C.c_int32), C.c_int32, _dp, _dp,
+                               _dp, _P(FtsRdStats)]),
+    "fts_rd_destroy": (None, [_vp]),
+    "fts_rd_last_error": (C.c_char_p, [_vp]),
 }
 
 NOALLOC_MAX_NODES = 1048576

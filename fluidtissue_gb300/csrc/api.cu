@@ -635,6 +635,9 @@ static int solve_common(fts_ctx* ctx, const double* phi, const double* source, c
         if (c.matfree)  // tets + node->element map + 64 B record per element; map offsets,
                         // flags, x, r1, q per node
             st.spmv_bytes = (double)c.nt * (16.0 + 16.0 + 64.0) + n * (4.0 + 1.0 + 3.0 * 16.0);
+        if (c.matfree && c.topo.kuhn_elements)  // lattice form: coordinates, flags, x, r1, q
+                                                // per node, FP32 mu per element
+            st.spmv_bytes = (double)c.nt * 4.0 + n * (12.0 + 1.0 + 3.0 * 16.0);
         st.spmv_bytes_fp64 = nb * (16.0 * 8.0 + 4.0) + 4.0 * (n + 1.0) + 3.0 * 4.0 * n * 8.0;
     }
     if (stats) *stats = st;

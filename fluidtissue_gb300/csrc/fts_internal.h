@@ -24,6 +24,8 @@ struct HostTopology {
     int32_t max_p2t = 0;           // most tetrahedra around one node
     int32_t lattice_n = 0;         // n if the mesh is the Kuhn lattice of n^3 nodes (index
                                    // i + n j + n^2 k, Kuhn node graph), else 0
+    bool kuhn_elements = false;    // lattice with element 6c + t = the monotone path of axis
+                                   // permutation t in cube c (the lattice generator's order)
     int64_t n_interior = 0;        // nI
 };
 
@@ -41,6 +43,7 @@ void boundary_from_faces(const fts_mesh& m, const HostTopology& T, std::vector<u
 struct RefConstants {
     double wq[4];
     double mref[4][4];
+    double phi[4][4];  // the float-rounded basis table phi[a][q]
 };
 RefConstants ref_constants();
 

@@ -676,8 +676,6 @@ long long minres_inner(Ctx& c, double rtol, long long maxit, double* achieved, i
         c.spmv_runs += ran;
         if (c.ms_host->stop) break;
     }
-    if (use_mg && mg_barrier_failed<T>(c, mg_of<T>(c)))
-        throw CudaError(cudaErrorLaunchTimeout, "multigrid grid barrier", __FILE__, __LINE__);
     const MinresScalars& S = *c.ms_host;
     *achieved = S.beta1 > 0.0 ? S.phibar / S.beta1 : 0.0;
     *status = S.status;

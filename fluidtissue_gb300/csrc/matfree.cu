@@ -13,9 +13,11 @@
 // :135-203, symmetric sign convention).  Dirichlet velocity rows are identity
 // and Dirichlet velocity values are read as zero.
 //
-// FP32 inner operator: a 64-byte FP32 record per element (gradients, volume,
-// h^2, mu) built from the FP64 geometry; each record is read by the element's
-// 4 nodes (L2 reuse).  FP64 outer residual: the stored FP64 ElemGeom.
+// FP32 inner operator: on meshes in the lattice generator's element order the
+// geometry is recomputed per node from the coordinates (k_mf_lat_minres_A);
+// otherwise a 64-byte FP32 record per element (gradients, volume, h^2, mu)
+// built from the FP64 geometry, each read by the element's 4 nodes (L2 reuse).
+// FP64 outer residual: the stored FP64 ElemGeom.
 #include <cfloat>
 
 #include "fts_device.cuh"
@@ -159,6 +161,157 @@ k_mf_minres_A(int64_t np, const int32_t* __restrict__ p2t_ptr, const uint32_t* _
     }
 }
 
+// ---------------------------------------------------------------------------
+// Kuhn-lattice form (elements in the order of the lattice generator: element
+// 6c + t of cube c is the monotone path 0 -> e_p0 -> e_p0 + e_p1 -> (1,1,1) of
+// axis permutation t).  A node's 24 elements follow from its lattice position,
+// and their geometry is recomputed in FP32 from the node coordinates (edge
+// vectors of nearby float coordinates are exact or nearly so), so one
+// application reads 12 B of coordinates, 24 B of viscosity and the vectors per
+// node — no element records, connectivity or node-element map.
+// ---------------------------------------------------------------------------
+// First two axes of the path of permutation t: {0,1,2} {0,2,1} {1,0,2}
+// {1,2,0} {2,0,1} {2,1,0} (the lattice generator's order).
+__device__ __forceinline__ void lat_path(int t, int& p0, int& p1) {
+    switch (t) {
+        case 0: p0 = 0; p1 = 1; break;
+        case 1: p0 = 0; p1 = 2; break;
+        case 2: p0 = 1; p1 = 0; break;
+        case 3: p0 = 1; p1 = 2; break;
+        case 4: p0 = 2; p1 = 0; break;
+        default: p0 = 2; p1 = 1; break;
+    }
+}
+
+// FP32 geometry of a tetrahedron from its 4 vertices (the same formulas as the
+// FP64 element geometry: B = [p1-p0, p2-p0, p3-p0], g = invB^T ghat, V = |det|/6,
+// h = cbrt|det|, h^2 in float).
+__device__ __forceinline__ void tet_geom_f32(const float p[4][3], float g[4][3], float& vol,
+                                             float& hh) {
+    float B[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        B[a][0] = p[1][a] - p[0][a];
+        B[a][1] = p[2][a] - p[0][a];
+        B[a][2] = p[3][a] - p[0][a];
+    }
+    const float c00 = B[1][1] * B[2][2] - B[1][2] * B[2][1];
+    const float c01 = B[1][2] * B[2][0] - B[1][0] * B[2][2];
+    const float c02 = B[1][0] * B[2][1] - B[1][1] * B[2][0];
+    const float det = B[0][0] * c00 + B[0][1] * c01 + B[0][2] * c02;
+    float cof[3][3];
+    cof[0][0] = c00;
+    cof[0][1] = c01;
+    cof[0][2] = c02;
+    cof[1][0] = B[0][2] * B[2][1] - B[0][1] * B[2][2];
+    cof[1][1] = B[0][0] * B[2][2] - B[0][2] * B[2][0];
+    cof[1][2] = B[0][1] * B[2][0] - B[0][0] * B[2][1];
+    cof[2][0] = B[0][1] * B[1][2] - B[0][2] * B[1][1];
+    cof[2][1] = B[0][2] * B[1][0] - B[0][0] * B[1][2];
+    cof[2][2] = B[0][0] * B[1][1] - B[0][1] * B[1][0];
+    const float id = 1.f / det;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float it0 = cof[r][0] * id, it1 = cof[r][1] * id, it2 = cof[r][2] * id;
+        g[0][r] = -it0 - it1 - it2;
+        g[1][r] = it0;
+        g[2][r] = it1;
+        g[3][r] = it2;
+    }
+    const float adet = fabsf(det);
+    vol = adet * (1.f / 6.f);
+    const float h = cbrtf(adet);
+    hh = h * h;
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_mf_lat_minres_A(int n, int64_t np, const float* __restrict__ xyz, const float* __restrict__ muf,
+                  const uint8_t* __restrict__ bnd, const V4<float>* __restrict__ Y, int ybuf,
+                  const V4<float>* __restrict__ R1, V4<float>* __restrict__ q, float alpha,
+                  float eps, MfConst K, Reduction red, MinresScalars* s) {
+    if (s->stop) return;
+    const float tinv = (float)(1.0 / s->beta);
+    const float wadd = (float)s->ycorr[ybuf];
+    const int m = n - 1;
+    const int nn = n * n;
+    double acc[2] = {0.0, 0.0};
+    for (int64_t v64 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v64 < np;
+         v64 += (int64_t)gridDim.x * blockDim.x) {
+        const int v = (int)v64;
+        const int k = v / nn;
+        const int rem = v - k * nn;
+        const int j = rem / n;
+        const int i = rem - j * n;
+        float y[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+        for (int corner = 0; corner < 8; ++corner) {
+            const int dx = corner & 1, dy = (corner >> 1) & 1, dz = corner >> 2;
+            const int ci = i - dx, cj = j - dy, ck = k - dz;
+            if (ci < 0 || cj < 0 || ck < 0 || ci >= m || cj >= m || ck >= m) continue;
+            const int a = dx + dy + dz;  // the node's place on every path through it
+            const int o = ci + n * (cj + n * ck);
+            const int64_t cube = ci + (int64_t)m * (cj + (int64_t)m * ck);
+            // axis of the single 1 (a == 1) or of the single 0 (a == 2)
+            const int ax = a == 1 ? (dx ? 0 : (dy ? 1 : 2)) : (!dx ? 0 : (!dy ? 1 : 2));
+#pragma unroll 1
+            for (int t = 0; t < 6; ++t) {
+                int p0, p1;
+                lat_path(t, p0, p1);
+                const int p2 = 3 - p0 - p1;
+                if ((a == 1 && p0 != ax) || (a == 2 && p2 != ax)) continue;
+                const int s0 = p0 == 0 ? 1 : (p0 == 1 ? n : nn);
+                const int s1 = p1 == 0 ? 1 : (p1 == 1 ? n : nn);
+                const int ids[4] = {o, o + s0, o + s0 + s1, o + 1 + n + nn};
+                float p[4][3], u[4][4];
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const float* xp = xyz + 3 * (int64_t)ids[b];
+                    p[b][0] = __ldg(xp);
+                    p[b][1] = __ldg(xp + 1);
+                    p[b][2] = __ldg(xp + 2);
+                    const V4<float> xv = Y[ids[b]];
+                    const bool d = __ldg(bnd + ids[b]) != 0;
+                    u[b][0] = d ? 0.f : xv.x;
+                    u[b][1] = d ? 0.f : xv.y;
+                    u[b][2] = d ? 0.f : xv.z;
+                    u[b][3] = xv.w + wadd;
+                }
+                float g[4][3], vol, hh;
+                tet_geom_f32(p, g, vol, hh);
+                elem_row<float>(g, vol, hh, __ldg(muf + 6 * cube + t), a, u, alpha, eps, K.wq,
+                                K.mref, y);
+            }
+        }
+        const V4<float> yv = Y[v];
+        if (bnd[v]) {
+            y[0] = yv.x;
+            y[1] = yv.y;
+            y[2] = yv.z;
+        }
+        V4<float> o4;
+        o4.x = y[0] * tinv;
+        o4.y = y[1] * tinv;
+        o4.z = y[2] * tinv;
+        o4.w = y[3] * tinv;
+        q[v] = o4;
+        const V4<float> r1 = R1[v];
+        const float v0 = yv.x * tinv, v1 = yv.y * tinv, v2 = yv.z * tinv, v3 = (yv.w + wadd) * tinv;
+        acc[0] += (double)(v0 * o4.x) + (double)(v1 * o4.y) + (double)(v2 * o4.z) + (double)(v3 * o4.w);
+        acc[1] += (double)(v0 * r1.x) + (double)(v1 * r1.y) + (double)(v2 * r1.z) + (double)(v3 * r1.w);
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
+        const double c1 = s->iters >= 1 ? s->beta / s->oldb : 0.0;
+        s->alfa = tot[0] - c1 * tot[1];
+    }
+}
+
+__global__ void k_mu_f32(int64_t nt, const double* __restrict__ mu, float* __restrict__ muf) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nt;
+         k += (int64_t)gridDim.x * blockDim.x)
+        muf[k] = (float)mu[k];
+}
+
 // FP64 outer residual r = b - S x (stored FP64 geometry), ||r||^2, ||b||^2.
 __global__ void __launch_bounds__(kThreads)
 k_mf_residual64(int64_t np, const int32_t* __restrict__ p2t_ptr, const uint32_t* __restrict__ p2t,
@@ -251,6 +404,13 @@ __global__ void k_mf_pc(int64_t np, const int32_t* __restrict__ p2t_ptr,
 
 void launch_mf_minres_A(Ctx& c, const V4<float>* Y, int ybuf, const V4<float>* R1, V4<float>* q) {
     static const MfConst K = mf_const();
+    if (c.topo.kuhn_elements) {
+        k_mf_lat_minres_A<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
+            c.topo.lattice_n, c.np, c.xyz, c.mf_rec, c.bnd, Y, ybuf, R1, q, (float)c.par.alpha,
+            (float)c.par.eps, K, c.red, c.ms);
+        c.launches += 1;
+        return;
+    }
     k_mf_minres_A<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
         c.np, c.p2t_ptr, c.p2t, c.tets, reinterpret_cast<const ElemF32*>(c.mf_rec), c.bnd, Y,
         ybuf, R1, q, (float)c.par.alpha, (float)c.par.eps, K, c.red, c.ms);
@@ -269,9 +429,14 @@ void launch_mf_residual64(Ctx& c) {
 void launch_mf_pc(Ctx& c) {
     static const MfConst K = mf_const();
     static_assert(sizeof(ElemF32) == 64, "64-byte element record");
-    if (!c.mf_rec) c.mf_rec = dev_alloc<float>(c, (size_t)c.nt * 16);
-    k_mf_records<<<grid_for(c, c.nt), kThreads, 0, c.stream>>>(
-        c.nt, c.geom, c.mu, reinterpret_cast<ElemF32*>(c.mf_rec));
+    if (c.topo.kuhn_elements) {  // lattice form: FP32 viscosity only
+        if (!c.mf_rec) c.mf_rec = dev_alloc<float>(c, (size_t)c.nt);
+        k_mu_f32<<<grid_for(c, c.nt), kThreads, 0, c.stream>>>(c.nt, c.mu, c.mf_rec);
+    } else {
+        if (!c.mf_rec) c.mf_rec = dev_alloc<float>(c, (size_t)c.nt * 16);
+        k_mf_records<<<grid_for(c, c.nt), kThreads, 0, c.stream>>>(
+            c.nt, c.geom, c.mu, reinterpret_cast<ElemF32*>(c.mf_rec));
+    }
     c.launches += 1;
     k_mf_pc<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(c.np, c.p2t_ptr, c.p2t, c.geom, c.mu,
                                                          c.par.alpha, c.par.eps, K, c.pc32);

@@ -33,8 +33,9 @@
 #include <utility>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "fts_device.cuh"
-#include "grid_sync.cuh"
 #include "mg.cuh"
 #include "mg_device.cuh"
 #include "reduce.cuh"
@@ -308,17 +309,29 @@ __global__ void k_mg_absmax(int64_t n, const float* __restrict__ K, unsigned* __
     if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(out, __float_as_uint(m));
 }
 
-// FP16 copy of a level's stencil, scaled so that max |K| maps to 16384.
-__global__ void k_mg_to_half(int64_t n, const float* __restrict__ K,
-                             const unsigned* __restrict__ maxbits, __half* __restrict__ Kh,
+// FP16 copy of a level's stencil (layout of hidx), scaled so that max |K|
+// maps to 16384.  Thread per (node, group): group g < 8 takes entries 0..7 of
+// direction g, group 8 entry 8 of every direction.
+__global__ void k_mg_to_half(int64_t nodes, const float* __restrict__ K,
+                             const unsigned* __restrict__ maxbits, uint4* __restrict__ Kh,
                              double* __restrict__ scale) {
     const float mx = __uint_as_float(*maxbits);
     const float sc = mx > 0.f ? mx / 16384.f : 1.f;
     const float inv = 1.f / sc;
     if (blockIdx.x == 0 && threadIdx.x == 0) *scale = (double)sc;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x)
-        Kh[i] = __float2half_rn(K[i] * inv);
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nodes * 9;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t tile = t / (9 * 32);
+        const int g = (int)((t / 32) % 9);
+        const int64_t v = tile * 32 + (t & 31);
+        __align__(16) __half h[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int q = g < 8 ? 9 * g + k : 9 * k + 8;
+            h[k] = __float2half_rn(K[kidx(q, v)] * inv);
+        }
+        Kh[hidx(g, v)] = *reinterpret_cast<const uint4*>(h);
+    }
 }
 
 __global__ void k_mg_unit_scale(int levels, double* __restrict__ scale) {
@@ -401,11 +414,16 @@ k_mg_coarse_solve(LevelView<T> L, int steps, const int* __restrict__ stop) {
     mg_coarse_block<T>(L, steps);
 }
 
-// The levels l0.. of one V-cycle in one cooperative launch: the small levels
-// are latency bound as separate launches, so their phases are separated by
-// grid barriers instead.  Level l0's right-hand side and first direction are
-// ready; its corrected x is the result.  skip_final (l0 == 0) leaves the last
+// The levels l0.. of one V-cycle in one launch of a single thread-block
+// cluster (16 CTAs of 512 threads where the device allows it, else 8): the
+// small levels are latency bound as separate launches, so their phases are
+// separated by hardware cluster barriers instead (barrier.cluster: release /
+// acquire at cluster scope, covering the global-memory vectors the CTAs
+// exchange).  Level l0's right-hand side and first direction are ready; its
+// corrected x is the result.  skip_final (l0 == 0) leaves the last
 // post-smoothing step of the finest level to the caller.
+constexpr int kTailThreads = 512;
+
 template <typename T>
 struct MGTailArgs {
     LevelView<T> lv[kMaxMGLevels];
@@ -413,12 +431,13 @@ struct MGTailArgs {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
-k_mg_tail(const __grid_constant__ MGTailArgs<T> a, BarrierState* bar,
-          const int* __restrict__ stop) {
+__global__ void __launch_bounds__(kTailThreads, 1)
+k_mg_tail(const __grid_constant__ MGTailArgs<T> a, const int* __restrict__ stop) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
     if (stop && *stop) return;  // uniform: nothing writes the flag during the V-cycle
-    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)cl.block_rank() * blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)cl.num_blocks() * blockDim.x;
     T xo[3];
     for (int l = a.l0; l + 1 < a.nlev; ++l) {
         const LevelView<T> L = a.lv[l];
@@ -427,34 +446,60 @@ k_mg_tail(const __grid_constant__ MGTailArgs<T> a, BarrierState* bar,
             for (int64_t v = tid; v < L.N; v += nth)
                 mg_step_node<T>(L, v, s, mode, (s & 1) ? L.d0 : L.d1, (s & 1) ? L.d1 : L.d0, xo,
                                 true, true);
-            if (!grid_barrier(bar)) return;
+            cl.sync();
         }
         for (int64_t v = tid; v < L.N; v += nth) mg_resid_node<T>(L, v);
-        if (!grid_barrier(bar)) return;
+        cl.sync();
         const LevelView<T> C = a.lv[l + 1];
         for (int64_t v = tid; v < C.N; v += nth) mg_restrict_node<T>(L, C, v);
-        if (!grid_barrier(bar)) return;
+        cl.sync();
     }
-    if (blockIdx.x == 0) {
+    if (cl.block_rank() == 0) {
         const LevelView<T> L = a.lv[a.nlev - 1];
         mg_coarse_block<T>(L, L.n == 3 ? 1 : kCoarse);
     }
-    if (!grid_barrier(bar)) return;
+    cl.sync();
     for (int l = a.nlev - 2; l >= a.l0; --l) {
         const LevelView<T> L = a.lv[l], C = a.lv[l + 1];
         for (int64_t v = tid; v < L.N; v += nth) mg_prolong_node<T>(L, C, v);
-        if (!grid_barrier(bar)) return;
+        cl.sync();
         for (int64_t v = tid; v < L.N; v += nth) mg_resid_first_node<T>(L, v);
-        if (!grid_barrier(bar)) return;
+        cl.sync();
         const int last = (l == 0 && a.skip_final) ? kSmooth - 2 : kSmooth - 1;
         for (int s = 1; s <= last; ++s) {
             const int mode = s == 1 ? kStepAfterFirst : kStepRegular;
             for (int64_t v = tid; v < L.N; v += nth)
                 mg_step_node<T>(L, v, s, mode, (s & 1) ? L.d0 : L.d1, (s & 1) ? L.d1 : L.d0, xo,
                                 true, true);
-            if (!grid_barrier(bar)) return;
+            cl.sync();
         }
     }
+}
+
+// Cluster size for the tail launch: 16 where the device and the kernel's
+// resources allow it, else 8 (the portable maximum); 0 if neither fits.
+template <typename T>
+static int tail_cluster_size(Ctx& c) {
+    FTS_CUDA(cudaFuncSetAttribute(k_mg_tail<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    for (int cs : {16, 8}) {
+        cudaLaunchConfig_t lc = {};
+        lc.gridDim = dim3((unsigned)cs);
+        lc.blockDim = dim3((unsigned)kTailThreads);
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)cs;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        lc.attrs = attr;
+        lc.numAttrs = 1;
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, k_mg_tail<T>, &lc) == cudaSuccess &&
+            clusters > 0)
+            return cs;
+        (void)cudaGetLastError();
+    }
+    (void)c;
+    return 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -470,6 +515,8 @@ void mg_build(Ctx& c, MG<T>& mg) {
         L.N = (int64_t)n * n * n;
         const size_t stored = (size_t)((L.N + 31) / 32) * 32 * kStored;
         L.K = dev_alloc<T>(c, stored);
+        // the set-up kernels write nodes < N only; the tile padding stays zero
+        FTS_CUDA(cudaMemsetAsync(L.K, 0, stored * sizeof(T), c.stream));
         if (sizeof(typename MGStore<T>::type) == sizeof(T))
             L.Kh = reinterpret_cast<typename MGStore<T>::type*>(L.K);
         else
@@ -488,21 +535,16 @@ void mg_build(Ctx& c, MG<T>& mg) {
         throw (int)FTS_ERR_UNSUPPORTED;
     }
     // persistent launch for the small levels: the first level (below the
-    // finest, unless the whole hierarchy is small) with at most kTailNodes nodes
+    // finest, unless the whole hierarchy is small) with at most tail_nodes<T>() nodes
     mg.tail_level = -1;
     for (size_t l = 0; l + 1 < mg.L.size(); ++l)
-        if (mg.L[l].N <= kTailNodes) {
+        if (mg.L[l].N <= tail_nodes<T>()) {
             mg.tail_level = (int)l;
             break;
         }
     if (mg.tail_level >= 0) {
-        int per_sm = 0;
-        FTS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mg_tail<T>, kThreads, 0));
-        const int64_t want = (mg.L[mg.tail_level].N + kThreads - 1) / kThreads;
-        mg.tail_blocks = (int)std::min<int64_t>(want, (int64_t)std::max(per_sm, 0) * c.num_sms);
-        if (mg.tail_blocks < 1) mg.tail_level = -1;
-        mg.bar = dev_alloc<BarrierState>(c, 1);
-        FTS_CUDA(cudaMemsetAsync(mg.bar, 0, sizeof(BarrierState), c.stream));
+        mg.tail_blocks = tail_cluster_size<T>(c);
+        if (mg.tail_blocks == 0) mg.tail_level = -1;
     }
     FTS_CUDA(cudaMemcpyAsync(mg.L[0].mask, c.bnd, (size_t)mg.L[0].N, cudaMemcpyDeviceToDevice,
                              c.stream));
@@ -521,8 +563,9 @@ static void mg_store(Ctx& c, MG<float>& mg, size_t l) {
     const int64_t stored = ((L.N + 31) / 32) * 32 * kStored;
     FTS_CUDA(cudaMemsetAsync(mg.maxbits + l, 0, sizeof(unsigned), c.stream));
     k_mg_absmax<<<grid_for(c, stored), kThreads, 0, c.stream>>>(stored, L.K, mg.maxbits + l);
-    k_mg_to_half<<<grid_for(c, stored), kThreads, 0, c.stream>>>(stored, L.K, mg.maxbits + l,
-                                                                  L.Kh, mg.scale + l);
+    const int64_t nodes = ((L.N + 31) / 32) * 32;
+    k_mg_to_half<<<grid_for(c, nodes * 9), kThreads, 0, c.stream>>>(
+        nodes, L.K, mg.maxbits + l, reinterpret_cast<uint4*>(L.Kh), mg.scale + l);
     c.launches += 2;
 }
 static void mg_store(Ctx& c, MG<double>& mg, size_t l) {
@@ -602,14 +645,16 @@ static void vcycle_level(Ctx& c, MG<T>& mg, size_t l, const int* stop, bool skip
         a.skip_final = skip_final ? 1 : 0;
         cudaLaunchConfig_t lc = {};
         lc.gridDim = dim3((unsigned)mg.tail_blocks);
-        lc.blockDim = dim3((unsigned)kThreads);
+        lc.blockDim = dim3((unsigned)kTailThreads);
         lc.stream = c.stream;
         cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeCooperative;
-        attr[0].val.cooperative = 1;
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)mg.tail_blocks;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
         lc.attrs = attr;
         lc.numAttrs = 1;
-        FTS_CUDA(cudaLaunchKernelEx(&lc, k_mg_tail<T>, a, mg.bar, stop));
+        FTS_CUDA(cudaLaunchKernelEx(&lc, k_mg_tail<T>, a, stop));
         c.launches += 1;
         return;
     }
@@ -660,10 +705,8 @@ void mg_free(MG<T>& mg) {
                         (void*)L.d1, (void*)L.mask})
             if (p) cudaFree(p);
     }
-    for (void* p : {(void*)mg.lam, (void*)mg.coef, (void*)mg.scale, (void*)mg.maxbits,
-                    (void*)mg.bar})
+    for (void* p : {(void*)mg.lam, (void*)mg.coef, (void*)mg.scale, (void*)mg.maxbits})
         if (p) cudaFree(p);
-    mg.bar = nullptr;
     mg.tail_level = -1;
     mg.lam = nullptr;
     mg.coef = nullptr;
@@ -673,17 +716,6 @@ void mg_free(MG<T>& mg) {
     mg.built = false;
 }
 
-template <typename T>
-bool mg_barrier_failed(Ctx& c, MG<T>& mg) {
-    if (!mg.bar) return false;
-    BarrierState b;
-    FTS_CUDA(cudaMemcpyAsync(&b, mg.bar, sizeof(b), cudaMemcpyDeviceToHost, c.stream));
-    FTS_CUDA(cudaStreamSynchronize(c.stream));
-    return b.error != 0;
-}
-
-template bool mg_barrier_failed<double>(Ctx&, MG<double>&);
-template bool mg_barrier_failed<float>(Ctx&, MG<float>&);
 template void mg_setup<double>(Ctx&, MG<double>&);
 template void mg_setup<float>(Ctx&, MG<float>&);
 template void mg_vcycle<double>(Ctx&, MG<double>&, const int*, bool);

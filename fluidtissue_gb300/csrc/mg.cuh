@@ -9,7 +9,6 @@
 namespace fts {
 
 struct Ctx;
-struct BarrierState;
 
 constexpr int kSmooth = 2;        // Chebyshev degree of each pre / post smoothing
 constexpr int kCoarse = 20;       // Chebyshev degree of the coarsest-level solve
@@ -17,7 +16,10 @@ constexpr int kPowerIters = 12;   // power iterations for lambda_max(D^-1 K)
 constexpr double kLamSafety = 1.1;
 constexpr int kCoefStride = 64;   // per level: 1/theta, then (ca_s, cb_s) for s >= 1
 constexpr int kMaxMGLevels = 10;  // levels of one hierarchy (n <= 513)
-constexpr int64_t kTailNodes = 40000;  // levels this small run in one persistent launch
+// Levels with at most this many nodes run in one cluster launch (FP32 / FP64:
+// a cluster has a tenth of the GPU's SMs, which the FP64 FMA rate feels first).
+template <typename T>
+constexpr int64_t tail_nodes() { return sizeof(T) == 4 ? 5000 : 1000; }
 
 // Storage of the smoothing operator: the FP32 hierarchy keeps its stencils in
 // FP16 (scaled per level by max|K| / 16384; arithmetic stays FP32), the FP64
@@ -58,11 +60,10 @@ struct MG {
     unsigned* maxbits = nullptr;     // device: max |K| per level (float bits)
     std::vector<double> lam_host;
     bool built = false;
-    // levels tail_level.. of every V-cycle run in one cooperative launch of
-    // tail_blocks blocks (grid barriers between phases); -1: none
+    // levels tail_level.. of every V-cycle run in one launch of a single
+    // cluster of tail_blocks CTAs (cluster barriers between phases); -1: none
     int tail_level = -1;
     int tail_blocks = 0;
-    BarrierState* bar = nullptr;
 };
 
 // Nodes per axis of the next coarser lattice.
@@ -88,8 +89,5 @@ template <typename T>
 void mg_vcycle(Ctx& c, MG<T>& mg, const int* stop, bool skip_final);
 template <typename T>
 void mg_free(MG<T>& mg);
-// True when a grid barrier of the persistent coarse-level launch timed out.
-template <typename T>
-bool mg_barrier_failed(Ctx& c, MG<T>& mg);
 
 }  // namespace fts

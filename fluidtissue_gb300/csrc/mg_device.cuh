@@ -12,6 +12,8 @@
 // another thread of it reads x at a neighbour.
 #pragma once
 
+#include <type_traits>
+
 #include "fts_device.cuh"
 
 namespace fts {
@@ -79,6 +81,82 @@ inline LevelView<T> level_view(const MG<T>& mg, size_t l) {
                         mg.coef + l * kCoefStride};
 }
 
+// FP16 stencil layout: per node 9 groups of 8 halfs (16 B each), in tiles of
+// 32 nodes: group d < 8 holds entries 0..7 (3r + c) of the block towards
+// direction d, group 8 holds entry 8 of the 8 blocks.  A warp's load of one
+// group is 512 contiguous bytes; a node's own blocks are 9 loads, a
+// neighbour's block 2.  Index in 16-byte units.
+__host__ __device__ __forceinline__ int64_t hidx(int g, int64_t v) {
+    return ((v >> 5) * 9 + g) * 32 + (v & 31);
+}
+
+__device__ __forceinline__ void unpack8(const uint4& u, float f[8]) {
+    const __half2* h = reinterpret_cast<const __half2*>(&u);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float2 a = __half22float2(h[k]);
+        f[2 * k] = a.x;
+        f[2 * k + 1] = a.y;
+    }
+}
+__device__ __forceinline__ float half_at(const uint4& u, int k) {
+    return __half2float(reinterpret_cast<const __half*>(&u)[k]);
+}
+
+// y = K x at node v from the FP16 layout (without the level's scale).
+// INNER: all 14 neighbours exist (no range checks, so the compiler can issue
+// every load of the node before the first use).
+template <bool INNER>
+__device__ __forceinline__ void stencil_h_body(int n, int64_t N, int v, int i, int j, int k,
+                                               const uint4* __restrict__ K,
+                                               const float* __restrict__ x, float y[3]) {
+    const int nn = n * n;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    const uint4 e8 = __ldg(K + hidx(8, v));
+#pragma unroll
+    for (int d = 0; d < 8; ++d) {  // self and positive directions: own blocks
+        const int w = INNER ? v + off_x(d) + n * off_y(d) + nn * off_z(d) : nbr(i, j, k, d, n);
+        if (!INNER && w < 0) continue;
+        const float x0 = x[w], x1 = x[N + w], x2 = x[2 * N + w];
+        float f[8];
+        unpack8(__ldg(K + hidx(d, v)), f);
+        const float f8 = half_at(e8, d);
+        a0 = fmaf(f[0], x0, fmaf(f[1], x1, fmaf(f[2], x2, a0)));
+        a1 = fmaf(f[3], x0, fmaf(f[4], x1, fmaf(f[5], x2, a1)));
+        a2 = fmaf(f[6], x0, fmaf(f[7], x1, fmaf(f8, x2, a2)));
+    }
+#pragma unroll
+    for (int d = 1; d < 8; ++d) {  // negative directions: neighbour's block, transposed
+        const int w = INNER ? v - off_x(d) - n * off_y(d) - nn * off_z(d) : nbr(i, j, k, d + 7, n);
+        if (!INNER && w < 0) continue;
+        const float x0 = x[w], x1 = x[N + w], x2 = x[2 * N + w];
+        float f[8];
+        unpack8(__ldg(K + hidx(d, (int64_t)w)), f);
+        const float f8 = half_at(__ldg(K + hidx(8, (int64_t)w)), d);
+        a0 = fmaf(f[0], x0, fmaf(f[3], x1, fmaf(f[6], x2, a0)));
+        a1 = fmaf(f[1], x0, fmaf(f[4], x1, fmaf(f[7], x2, a1)));
+        a2 = fmaf(f[2], x0, fmaf(f[5], x1, fmaf(f8, x2, a2)));
+    }
+    y[0] = a0;
+    y[1] = a1;
+    y[2] = a2;
+}
+
+__device__ __forceinline__ void stencil_apply_h(int n, int64_t N, int64_t v64,
+                                                const uint4* __restrict__ K,
+                                                const float* __restrict__ x, float y[3]) {
+    const int v = (int)v64;
+    const int nn = n * n;
+    const int k = v / nn;
+    const int rem = v - k * nn;
+    const int j = rem / n;
+    const int i = rem - j * n;
+    if (i > 0 && j > 0 && k > 0 && i < n - 1 && j < n - 1 && k < n - 1)
+        stencil_h_body<true>(n, N, v, i, j, k, K, x, y);
+    else
+        stencil_h_body<false>(n, N, v, i, j, k, K, x, y);
+}
+
 // y = K x at node v (3 components, without the level's scale); x SoA [3][N].
 // 32-bit lattice coordinates; interior nodes take the neighbour offsets
 // without range checks.
@@ -86,6 +164,10 @@ template <typename T, typename KS>
 __device__ __forceinline__ void stencil_apply(int n, int64_t N, int64_t v64,
                                               const KS* __restrict__ K,
                                               const T* __restrict__ x, T y[3]) {
+    if constexpr (std::is_same<KS, __half>::value) {
+        stencil_apply_h(n, N, v64, reinterpret_cast<const uint4*>(K), x, y);
+        return;
+    }
     const int v = (int)v64;
     const int nn = n * n;
     const int k = v / nn;

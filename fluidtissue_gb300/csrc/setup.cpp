@@ -30,6 +30,7 @@ RefConstants ref_constants() {
         phi[2][q] = (double)y;
         phi[3][q] = (double)z;
     }
+    std::memcpy(R.phi, phi, sizeof(phi));
     for (int i = 0; i < 4; ++i) {
         double s = 0.0;
         for (int q = 0; q < 4; ++q) s += 0.25 * phi[i][q];
@@ -97,6 +98,27 @@ static int32_t detect_lattice(const HostTopology& T) {
         }
     }
     return ok ? (int32_t)n : 0;
+}
+
+// Whether element 6c + t of cube c = (ci, cj, ck) is the path origin,
+// origin + e_p0, origin + e_p0 + e_p1, origin + (1,1,1) of axis permutation t
+// ({0,1,2} {0,2,1} {1,0,2} {1,2,0} {2,0,1} {2,1,0}), nodes in that order.
+static bool kuhn_element_order(const fts_mesh& m, int32_t n) {
+    static const int perm[6][2] = {{0, 1}, {0, 2}, {1, 0}, {1, 2}, {2, 0}, {2, 1}};
+    const int64_t nn = n, cm = n - 1;
+    const int64_t step[3] = {1, nn, nn * nn};
+    bool ok = true;
+#pragma omp parallel for schedule(static) reduction(&& : ok)
+    for (int64_t c = 0; c < cm * cm * cm; ++c) {
+        const int64_t ci = c % cm, cj = (c / cm) % cm, ck = c / (cm * cm);
+        const int64_t o = ci + nn * (cj + nn * ck);
+        for (int t = 0; t < 6; ++t) {
+            const int32_t* e = m.tets + 4 * (6 * c + t);
+            const int64_t a = o + step[perm[t][0]], b = a + step[perm[t][1]];
+            ok = ok && e[0] == o && e[1] == a && e[2] == b && e[3] == o + 1 + nn + nn * nn;
+        }
+    }
+    return ok;
 }
 
 int build_topology(const fts_mesh& m, HostTopology& T, std::string& err) {
@@ -193,6 +215,7 @@ int build_topology(const fts_mesh& m, HostTopology& T, std::string& err) {
     for (int64_t i = 0; i < np; ++i) nI += T.bnd[i] ? 0 : 1;
     T.n_interior = nI;
     T.lattice_n = detect_lattice(T);
+    T.kuhn_elements = T.lattice_n > 0 && kuhn_element_order(m, T.lattice_n);
     return FTS_OK;
 }
 

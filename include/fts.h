@@ -269,6 +269,58 @@ int fts_bsr_residual_noalloc(int64_t np, const int32_t* rowptr, const int32_t* c
                              const double* vals, const double* x, const double* b, double* r,
                              double* norms, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Reaction-diffusion: activator / inhibitor patterning and the growth factor,
+ * replacing RD::solve (src/growth/RD.hpp:16-56, RD.cpp:27-108).  The system
+ * lives on the interior submesh (nodes with phi < 0, elements with four such
+ * nodes; LevelSet.cpp:180-211) with the lumped-mass Laplacian
+ * L = diag(1 / rowsum M) K (RD.cpp:116-172, Assembler.cpp:75-84) and is
+ * advanced by `iterations` explicit Euler steps of length dt (RD.cpp:74-92):
+ *   u' = u + dt (-Da L u + Act u^2 / (1 + Inh v + GFinh g) - DegA u)
+ *   v' = v + dt (-Di L v + u^2 - DegI v)       (only while u or v is non-zero)
+ *   g' = g + dt (-GFdiff L g - GFdeg g),  g' = GF production on source nodes
+ * All arithmetic FP64; all steps run in one persistent launch.
+ * ------------------------------------------------------------------------ */
+typedef struct fts_rd_params {
+    double dt;                /* "RD dt" */
+    int64_t iterations;       /* "RD iterations" */
+    double act, da, dega;     /* "Act", "Da", "DegA" */
+    double inh, di, degi;     /* "Inh", "Di", "DegI" */
+    double gf_production;     /* "GF production" */
+    double gf_diffusion;      /* "GF diffusion" */
+    double gf_degradation;    /* "GF degradation" */
+    double gf_inhibition;     /* "GF inhibition" */
+} fts_rd_params;
+
+typedef struct fts_rd_stats {
+    int32_t status;
+    int32_t alive;            /* activator / inhibitor were advanced (RD.cpp:60-62) */
+    int64_t interior_nodes;
+    int64_t interior_elements;
+    int64_t steps;
+    double ms_setup;          /* interior sets, Laplacian assembly, uploads */
+    double ms_steps;          /* the Euler steps (device time) */
+    double ms_total;          /* wall time of the call */
+    int64_t kernel_launches;
+} fts_rd_stats;
+
+typedef struct fts_rd fts_rd;
+
+/* RD's mesh (Mesh3D of the level set, RD.cpp:123-147) on `device`.  Returns
+ * FTS_ERR_DEGENERATE_ELEMENT for a flat tetrahedron. */
+int fts_rd_create(const fts_mesh* mesh, int32_t device, fts_rd** out);
+/* RD::solve: activator, inhibitor, growth_factor [np] are the state (in/out,
+ * host memory), phi [np] the level set, source_nodes the growth-factor
+ * sources (Knots::getSourceNodes, global node indices; every one must be an
+ * interior node, else FTS_ERR_BAD_INPUT).  iterations == 0 or dt < FLT_MIN
+ * returns at once with the state untouched (RD.cpp:31-33); otherwise every
+ * non-interior node of the three fields is zero on return (RD.cpp:94-102). */
+int fts_rd_solve(fts_rd* rd, const fts_rd_params* params, const double* phi,
+                 const int32_t* source_nodes, int32_t n_sources, double* activator,
+                 double* inhibitor, double* growth_factor, fts_rd_stats* stats);
+void fts_rd_destroy(fts_rd* rd);
+const char* fts_rd_last_error(const fts_rd* rd);
+
 #ifdef __cplusplus
 }
 #endif

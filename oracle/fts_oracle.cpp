@@ -28,6 +28,8 @@
 //  * un-preconditioned BiCGSTAB with ||r||/||b|| stop  src/growth/Flow.hpp:62, Flow.cpp:77-82, :266-285
 //      (Eigen's BiCGSTAB, external and not vendored; restated from van der Vorst 1992)
 //  * scatter to [ux(np), uy(np), uz(np), p(np)]        src/growth/Flow.cpp:290-300
+//  * reaction-diffusion: interior submesh, lumped-mass  src/growth/RD.cpp:27-108, :116-172;
+//    Laplacian, explicit Euler                         src/fem/Assembler.cpp:75-84
 #include <algorithm>
 #include <cfloat>
 #include <chrono>
@@ -791,6 +793,144 @@ double ora_minres_blockjacobi(int64_t N, int64_t nI, const int64_t* rp, const in
 int ora_scatter(int64_t np, int64_t N, const int32_t* sidx, const double* x, double* flow) {
     std::fill(flow, flow + 4 * np, 0.0);
     for (int64_t r = 0; r < N; ++r) flow[sidx[r]] = x[r];
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Reaction-diffusion (src/growth/RD.cpp:27-108, :116-172)
+// ---------------------------------------------------------------------------
+// Parameters, in this order: RD dt, Act, Da, DegA, Inh, Di, DegI,
+// GF production, GF diffusion, GF degradation, GF inhibition.
+//
+// Interior nodes: phi < 0 (LevelSet.cpp:200-211), local index = rank in
+// ascending global order; interior elements: all four nodes phi < 0
+// (LevelSet.cpp:180-196).  On that submesh (Neumann boundary):
+//   M(i,j) = int phi_i phi_j (float-rounded basis table), K(i,j) = int grad phi_i . grad phi_j
+//   (Assembler weak forms u.*v and ux.*vx + uy.*vy + uz.*vz, RD.cpp:150-160),
+//   L = diag(1 / rowsum M) K  (lump_mass, Assembler.cpp:75-84; RD.cpp:166-169);
+// a row with no interior element stays empty.  Explicit Euler, iters steps
+// (RD.cpp:74-92):
+//   alive (max |act|, |inh| over all nodes >= FLT_MIN):
+//     u2 = u.*u; de = 1 + Inh v + GFinh g
+//     u' = u + dt (-Da L u + Act u2./de - DegA u);  v' = v + dt (-Di L v + u2 - DegI v)
+//   g' = g + dt (-GFdiff L g - GFdeg g);  g'(sources) = GF production
+// with g(sources) = GF production before the first step.  Afterwards act,
+// inh, gf are zero on every non-interior node (RD.cpp:94-102).  Sources must be
+// interior nodes here (the reference's map lookup would send any other node
+// to its first interior node).  Returns 0, or -1 for a source outside the
+// interior or a degenerate element.
+int ora_rd_solve(int64_t np, int64_t nt, const float* xyz, const int32_t* tets,
+                 const double* phi, const int32_t* src, int32_t nsrc, const double* prm,
+                 int64_t iters, double* act, double* inh, double* gf) {
+    const double dt = prm[0];
+    if (iters == 0 || dt < FLT_MIN) return 0;
+    const double Act = prm[1], Da = prm[2], DegA = prm[3], Inh = prm[4], Di = prm[5],
+                 DegI = prm[6], GFprod = prm[7], GFdiff = prm[8], GFdeg = prm[9],
+                 GFinh = prm[10];
+    std::vector<int64_t> loc(np, -1);
+    std::vector<int64_t> nodes;
+    for (int64_t i = 0; i < np; ++i)
+        if (phi[i] < 0.0) {
+            loc[i] = (int64_t)nodes.size();
+            nodes.push_back(i);
+        }
+    const int64_t n = (int64_t)nodes.size();
+    for (int32_t s = 0; s < nsrc; ++s)
+        if (src[s] < 0 || src[s] >= np || loc[src[s]] < 0) return -1;
+    // node -> interior elements, rows of K and lumped M (row gather)
+    std::vector<std::vector<int64_t>> n2e(n);
+    for (int64_t k = 0; k < nt; ++k) {
+        const int32_t* t = tets + 4 * k;
+        if (phi[t[0]] < 0.0 && phi[t[1]] < 0.0 && phi[t[2]] < 0.0 && phi[t[3]] < 0.0)
+            for (int a = 0; a < 4; ++a) n2e[loc[t[a]]].push_back(k);
+    }
+    const RefTables& R = tables();
+    std::vector<std::vector<std::pair<int64_t, double>>> Lrow(n);
+    bool ok = true;
+#pragma omp parallel for schedule(dynamic, 256) reduction(&& : ok)
+    for (int64_t i = 0; i < n; ++i) {
+        std::vector<std::pair<int64_t, double>> row;  // (local col, K)
+        double msum = 0.0;
+        for (int64_t k : n2e[i]) {
+            const int32_t* t = tets + 4 * k;
+            Geom G;
+            if (!element_geom(xyz, t, G)) {
+                ok = false;
+                continue;
+            }
+            int a = 0;
+            while (t[a] != nodes[i]) ++a;
+            for (int b = 0; b < 4; ++b) {
+                double f[4];
+                const double gg = G.g[b][0] * G.g[a][0] + G.g[b][1] * G.g[a][1] +
+                                  G.g[b][2] * G.g[a][2];
+                for (int q = 0; q < 4; ++q) f[q] = gg;
+                const double kv = integ(f, R.qw, G.detB);
+                for (int q = 0; q < 4; ++q) f[q] = R.phi[b][q] * R.phi[a][q];
+                msum += integ(f, R.qw, G.detB);
+                const int64_t j = loc[t[b]];
+                bool found = false;
+                for (auto& e : row)
+                    if (e.first == j) {
+                        e.second += kv;
+                        found = true;
+                    }
+                if (!found) row.push_back({j, kv});
+            }
+        }
+        std::sort(row.begin(), row.end());
+        if (msum != 0.0)
+            for (auto& e : row) e.second = e.second / msum;
+        else
+            row.clear();
+        Lrow[i] = std::move(row);
+    }
+    if (!ok) return -1;
+    bool alive = false;
+    for (int64_t i = 0; i < np; ++i)
+        alive = alive || std::fabs(act[i]) >= FLT_MIN || std::fabs(inh[i]) >= FLT_MIN;
+    std::vector<double> u(n), v(n), g(n), un(n), vn(n), gn(n);
+    for (int64_t i = 0; i < n; ++i) {
+        u[i] = act[nodes[i]];
+        v[i] = inh[nodes[i]];
+        g[i] = gf[nodes[i]];
+    }
+    std::vector<char> is_src(n, 0);
+    for (int32_t s = 0; s < nsrc; ++s) is_src[loc[src[s]]] = 1;
+    for (int64_t i = 0; i < n; ++i)
+        if (is_src[i]) g[i] = GFprod;
+    for (int64_t it = 0; it < iters; ++it) {
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            double lu = 0.0, lv = 0.0, lg = 0.0;
+            for (const auto& e : Lrow[i]) {
+                lu += e.second * u[e.first];
+                lv += e.second * v[e.first];
+                lg += e.second * g[e.first];
+            }
+            if (alive) {
+                const double u2 = u[i] * u[i];
+                const double de = 1.0 + Inh * v[i] + GFinh * g[i];
+                un[i] = u[i] + dt * (-Da * lu + Act * (u2 / de) - DegA * u[i]);
+                vn[i] = v[i] + dt * (-Di * lv + u2 - DegI * v[i]);
+            } else {
+                un[i] = u[i];
+                vn[i] = v[i];
+            }
+            gn[i] = is_src[i] ? GFprod : g[i] + dt * (-GFdiff * lg - GFdeg * g[i]);
+        }
+        u.swap(un);
+        v.swap(vn);
+        g.swap(gn);
+    }
+    std::fill(act, act + np, 0.0);
+    std::fill(inh, inh + np, 0.0);
+    std::fill(gf, gf + np, 0.0);
+    for (int64_t i = 0; i < n; ++i) {
+        act[nodes[i]] = u[i];
+        inh[nodes[i]] = v[i];
+        gf[nodes[i]] = g[i];
+    }
     return 0;
 }
 

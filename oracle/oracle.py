@@ -68,6 +68,8 @@ def lib():
                                    _p(dbl), dbl, i64, C.c_int, _p(i64)]),
         "ora_minres_blockjacobi": (dbl, [i64, i64, _p(i64), _p(i32), _p(dbl), _p(dbl), _p(dbl),
                                          _p(dbl), dbl, _p(dbl), dbl, i64, _p(i64)]),
+        "ora_rd_solve": (C.c_int, [i64, i64, _p(f32), _p(i32), _p(dbl), _p(i32), i32, _p(dbl),
+                                   i64, _p(dbl), _p(dbl), _p(dbl)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -347,6 +349,26 @@ def flow_solve(xyz, tets, boundary, phi, c, mu, par, x_warm=None, flow=None):
     return 0, flow, x, info
 
 
+# Reaction-diffusion parameter keys (the reference's parameter files), in the
+# order ora_rd_solve takes them.
+RD_KEYS = ("RD dt", "Act", "Da", "DegA", "Inh", "Di", "DegI", "GF production",
+           "GF diffusion", "GF degradation", "GF inhibition")
+
+
+def rd_solve(xyz, tets, phi, src_nodes, par, act, inh, gf):
+    """RD::solve restated (src/growth/RD.cpp:27-108): advances (act, inh, gf)
+    in place by ``RD iterations`` explicit Euler steps; returns the status."""
+    prm = np.array([params_get(par, k) for k in RD_KEYS], np.float64)
+    iters = int(params_get(par, "RD iterations"))
+    src = np.ascontiguousarray(src_nodes, np.int32)
+    for a in (act, inh, gf):
+        assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return lib().ora_rd_solve(xyz.shape[0], tets.shape[0], _ptr(xyz, F32), _ptr(tets, I32),
+                              _ptr(np.ascontiguousarray(phi, np.float64), D), _ptr(src, I32),
+                              len(src), _ptr(prm, D), iters, _ptr(act, D), _ptr(inh, D),
+                              _ptr(gf, D))
+
+
 __all__ = ["build", "lib", "ref_tables", "boundary_nodes", "set_viscosity", "source",
            "assemble_blocks", "reduce", "spmv", "bicgstab", "true_residual", "scatter",
-           "system", "direct_solve", "solve_tight", "flow_solve"]
+           "system", "direct_solve", "solve_tight", "flow_solve", "rd_solve", "RD_KEYS"]

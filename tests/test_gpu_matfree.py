@@ -53,3 +53,27 @@ def test_matfree_refuses_fp64_and_inspection():
     with pytest.raises(Exception):
         f.system()
     f.close()
+
+
+def test_matfree_element_records_on_reordered_elements():
+    """Elements not in the lattice generator's order: the operator falls back
+    to per-element FP32 records over the node-element map; same answer."""
+    from fluidtissue_gb300.flow import Flow, Mesh
+    inst = workload("spheres257", 17)
+    par = dict(inst.params)
+    par["Stokes tolerance"] = 1e-10
+    perm = np.random.default_rng(3).permutation(inst.tets.shape[0])
+    flows = {}
+    for name, tets, mu in (("lattice", inst.tets, inst.mu),
+                           ("records", inst.tets[perm], inst.mu[perm])):
+        f = Flow()
+        assert f.init(Mesh(inst.xyz, tets), par, precision="mixed", operator="matfree",
+                      warm_start=False) == 0, f.last_error()
+        flow = np.zeros(4 * inst.np)
+        assert f.solve(inst.phi, inst.source, flow, mu=mu) == 0, f.last_error()
+        assert f.last_stats["rel_residual"] <= 1e-10
+        flows[name] = flow
+        f.close()
+    npn = inst.np
+    a, b = flows["records"][:3 * npn], flows["lattice"][:3 * npn]
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) <= 1e-7

@@ -194,3 +194,98 @@ def test_golden_fixture(fixture):
     ev = np.linalg.norm(flow[:3 * npn] - ref[:3 * npn]) / np.linalg.norm(ref[:3 * npn])
     ep = np.linalg.norm(flow[3 * npn:] - ref[3 * npn:]) / np.linalg.norm(ref[3 * npn:])
     assert ev <= 1e-10 and ep <= 1e-10
+
+
+# ---- reaction-diffusion (RD.cpp) restatement --------------------------------
+
+_RD0 = {"RD dt": 0.05, "RD iterations": 40.0, "Act": 0.0, "Da": 0.0, "DegA": 0.0, "Inh": 0.0,
+        "Di": 0.0, "DegI": 0.0, "GF production": 0.0, "GF diffusion": 0.0,
+        "GF degradation": 0.0, "GF inhibition": 0.0}
+
+
+def _lumped_mass(inst):
+    """Row sums of the P1 mass matrix over the interior elements, per node,
+    with the float-rounded basis table (local node a's row sum is
+    detB sum_b sum_q qw phi_b(q) phi_a(q), not exactly vol / 4)."""
+    tab, qw = O.ref_tables()
+    row = np.array([sum(qw * tab[b, q] * tab[a, q] for b in range(4) for q in range(4))
+                     for a in range(4)])
+    inside = inst.phi < 0
+    el = np.all(inside[inst.tets], axis=1)
+    m = np.zeros(inst.np)
+    detb = 6.0 * _volumes(inst)[el]
+    for a in range(4):
+        np.add.at(m, inst.tets[el, a], detb * row[a])
+    return m, inside
+
+
+def test_rd_constant_fields_only_decay():
+    """L 1 = 0 (K annihilates constants): uniform fields under diffusion keep
+    their value; pure degradation gives g_n = g_0 (1 - dt deg)^n exactly in
+    the limit of rounding."""
+    inst = workload("sphere65", 13)
+    par = dict(_RD0, **{"Da": 1e-3, "Di": 1e-3, "GF diffusion": 1e-3, "GF degradation": 0.1})
+    inside = inst.phi < 0
+    a = np.where(inside, 2.0, 0.0)
+    i = np.zeros(inst.np)
+    g = np.where(inside, 3.0, 0.0)
+    assert O.rd_solve(inst.xyz, inst.tets, inst.phi, [], par, a, i, g) == 0
+    m, _ = _lumped_mass(inst)
+    live = inside & (m > 0)
+    assert np.allclose(a[live], 2.0, rtol=0, atol=1e-12)
+    assert np.allclose(g[live], 3.0 * (1 - 0.05 * 0.1) ** 40, rtol=1e-12)
+    assert np.all(a[~inside] == 0) and np.all(g[~inside] == 0)
+
+
+def test_rd_diffusion_conserves_lumped_mass():
+    """sum_i m_i (L u)_i = sum_ij K_ij u_j = 0: pure diffusion conserves the
+    lumped-mass-weighted total."""
+    inst = workload("sphere65", 13)
+    par = dict(_RD0, **{"GF diffusion": 2e-3})
+    m, inside = _lumped_mass(inst)
+    rng = np.random.default_rng(2)
+    g = np.where(inside, rng.random(inst.np), 0.0)
+    total0 = float((m * g).sum())
+    a, i = np.zeros(inst.np), np.zeros(inst.np)
+    assert O.rd_solve(inst.xyz, inst.tets, inst.phi, [], par, a, i, g) == 0
+    assert abs(float((m * g).sum()) - total0) <= 1e-12 * total0
+    assert g[inside].std() < np.where(inside, rng.random(inst.np), 0.0)[inside].std()
+
+
+def test_rd_reaction_step_by_hand():
+    """One Euler step on a node with no interior element around it (L row
+    empty): the reaction terms alone, as in RD.cpp:79-84."""
+    inst = workload("sphere17", 9)
+    par = dict(_RD0, **{"RD iterations": 1.0, "Act": 2.0, "DegA": 0.01, "Inh": 1.0,
+                        "DegI": 0.02, "GF inhibition": 200.0, "GF degradation": 0.02})
+    m, inside = _lumped_mass(inst)
+    iso = np.where(inside & (m == 0))[0]
+    node = iso[0] if len(iso) else np.where(inside)[0][0]
+    a = np.where(inside, 0.7, 0.0)
+    i = np.where(inside, 0.3, 0.0)
+    g = np.where(inside, 0.01, 0.0)
+    a0, i0, g0 = a[node], i[node], g[node]
+    assert O.rd_solve(inst.xyz, inst.tets, inst.phi, [], par, a, i, g) == 0
+    if len(iso):
+        dt = 0.05
+        u2 = a0 * a0
+        de = 1.0 + 1.0 * i0 + 200.0 * g0
+        assert a[node] == a0 + dt * (-0.0 * 0.0 + 2.0 * (u2 / de) - 0.01 * a0)
+        assert i[node] == i0 + dt * (-0.0 * 0.0 + u2 - 0.02 * i0)
+        assert g[node] == g0 + dt * (-0.0 * 0.0 - 0.02 * g0)
+    # a uniform interior state changes by the reaction terms only (L 1 = 0)
+    live = np.where(inside & (m > 0))[0]
+    u2 = 0.49
+    want = 0.7 + 0.05 * (2.0 * (u2 / (1.0 + 0.3 + 200.0 * 0.01)) - 0.01 * 0.7)
+    assert np.allclose(a[live], want, rtol=1e-12)
+
+
+def test_rd_sources_and_refusal():
+    inst = workload("sphere17", 9)
+    par = dict(_RD0, **{"GF production": 5.0, "GF diffusion": 1e-3})
+    inside = np.where(inst.phi < 0)[0]
+    a, i, g = np.zeros(inst.np), np.zeros(inst.np), np.zeros(inst.np)
+    assert O.rd_solve(inst.xyz, inst.tets, inst.phi, inside[:2], par, a, i, g) == 0
+    assert np.all(g[inside[:2]] == 5.0) and g.max() == 5.0 and (g > 0).sum() > 2
+    outside = np.where(inst.phi >= 0)[0][:1]
+    assert O.rd_solve(inst.xyz, inst.tets, inst.phi, outside, par, a, i, g) == -1
