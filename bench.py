@@ -52,7 +52,8 @@ def _peaks():
 KERNELS = {
     "stencil": ("k_minres_A_lat", "FP32 lattice half-stencil 4x4-block SpMV + MINRES dots"),
     "assembled": ("k_minres_A_ell", "FP32 sliced-ELL 4x4-block SpMV + MINRES dots"),
-    "matfree": ("k_mf_minres_A", "FP32 matrix-free element operator + MINRES dots"),
+    "matfree": ("k_mf_lat_minres_A", "FP32 matrix-free lattice operator, geometry recomputed "
+                "per node, + MINRES dots; compute bound"),
 }
 
 
@@ -556,6 +557,79 @@ def rd_cpu_baseline(inst, src, a0, i0, g0, n_steps, sample_steps=200):
             "t_setup_s": t_setup, "t_step_s": t_step}
 
 
+def run_dist(args):
+    """Distance reset (EuclideanDistance::resetPhi) on the ellipsoid129 mesh
+    against its own interface points (the zero level set's edge crossings,
+    LevelSet.cpp:278-300): value = resets/s of the pruned search, through the
+    C ABI with host buffers (host sort, H2D, kernel, D2H).  Beside it the
+    reference's algorithm (every node against every point) on the same GPU, and
+    the oracle's host restatement on a sample of nodes."""
+    import torch
+    from fluidtissue_gb300 import workloads as W
+    from fluidtissue_gb300.distance import EuclideanDistance, interface_points
+
+    ws, rank, local = _dist()
+    dist = _setup_dist(ws, local)
+    torch.cuda.set_device(local)
+    inst = W.ellipsoid129()
+    ifp, _ = interface_points(inst.xyz, inst.tets, inst.phi)
+    d = EuclideanDistance()
+    if d.init(inst.xyz, device=local) != 0:
+        raise RuntimeError(f"fts_dist_create failed: {d.last_error()}")
+    out = {}
+    for method in ("pruned", "exhaustive"):
+        def step():
+            phi = inst.phi.copy()
+            rc = d.resetPhi(ifp, phi, method)
+            if rc != 0:
+                raise RuntimeError(f"fts_dist_reset failed ({rc}): {d.last_error()}")
+            return d.last_stats, phi
+        for _ in range(args.warmup):
+            step()
+        _barrier(dist)
+        clk = Clocks(local) if method == "pruned" else None
+        t0 = time.perf_counter()
+        res = [step() for _ in range(args.steps)]
+        wall = _max_over_ranks((time.perf_counter() - t0) * 1e3, dist)
+        out[method] = {"resets_per_s": round(ws * args.steps / (wall / 1e3), 3),
+                       "ms_per_reset": round(wall / args.steps, 3),
+                       "ms_kernel": round(statistics.mean(r[0]["ms_kernel"] for r in res), 3),
+                       "points_scanned": int(res[-1][0]["points_scanned"]),
+                       "clocks": clk.stop() if clk else None}
+        out[method]["phi"] = res[-1][1]
+    same = bool(np.array_equal(out["pruned"].pop("phi"), out["exhaustive"].pop("phi")))
+    pr = out["pruned"]
+    line = {"metric": "level-set distance resets/s (ellipsoid129 nodes x its interface points)",
+            "value": pr["resets_per_s"], "unit": "resets/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": pr["ms_per_reset"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (distances), f64 (phi)",
+            "data": "synthetic (ellipsoid129 mesh and level set; its edge crossings)",
+            "config": {"workload": f"dist129: {inst.np} nodes x {len(ifp)} interface points"},
+            "e2e": {"value": pr["resets_per_s"], "unit": "resets/s",
+                    "h2d_bytes_per_step": 12 * len(ifp) + 8 * inst.np,
+                    "d2h_bytes_per_step": 8 * inst.np},
+            "pruned": pr, "reference_algorithm_on_gpu": out["exhaustive"],
+            "pruned_equals_reference_algorithm": same,
+            "kernel_speedup": round(out["exhaustive"]["ms_kernel"] / max(pr["ms_kernel"], 1e-9), 1),
+            "gpu_launches": 1, "clocks": pr.pop("clocks")}
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle as O
+        k1 = min(inst.np, 20000)
+        phi = inst.phi.copy()
+        t0 = time.perf_counter()
+        O.dist_reset(inst.xyz, ifp, phi, 0, k1)
+        t = time.perf_counter() - t0
+        line["cpu_baseline"] = {
+            "value": 1.0 / (t * inst.np / k1), "unit": "resets/s", "cores": O.num_threads(),
+            "kind": "port",
+            "sample": (f"oracle host path on {k1} of {inst.np} nodes ({O.num_threads()} threads, "
+                       f"{t:.2f} s), scaled to all nodes")}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    d.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -580,6 +654,8 @@ def main():
         run_batch(args)
     elif args.workload == "rd129":
         run_rd(args)
+    elif args.workload == "dist129":
+        run_dist(args)
     else:
         run_ours(args)
 

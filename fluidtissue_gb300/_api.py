@@ -114,6 +114,48 @@ class FtsRdStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class FtsDistStats(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32),
+        ("blocks", C.c_int32),
+        ("points_scanned", C.c_int64),
+        ("ms_setup", C.c_double),
+        ("ms_kernel", C.c_double),
+        ("ms_total", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+DIST_PRUNED, DIST_EXHAUSTIVE = 0, 1
+
+
+class FtsLsParams(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double),
+        ("tol", C.c_double),
+        ("max_iter", C.c_int64),
+        ("reset", C.c_int32),
+    ]
+
+
+class FtsLsStats(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32),
+        ("iterations", C.c_int64),
+        ("error", C.c_double),
+        ("interface_points", C.c_int64),
+        ("ms_assembly", C.c_double),
+        ("ms_solve", C.c_double),
+        ("ms_reset", C.c_double),
+        ("ms_total", C.c_double),
+        ("kernel_launches", C.c_int64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
 PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_MINRES, SOLVER_BICGSTAB = 0, 1
 PC_AUTO, PC_JACOBI, PC_MULTIGRID = 0, 1, 2
@@ -156,6 +198,15 @@ SIGNATURES = {
                                _dp, _P(FtsRdStats)]),
     "fts_rd_destroy": (None, [_vp]),
     "fts_rd_last_error": (C.c_char_p, [_vp]),
+    "fts_dist_create": (C.c_int, [_P(C.c_float), C.c_int64, C.c_int32, _P(_vp)]),
+    "fts_dist_reset": (C.c_int, [_vp, _P(C.c_float), C.c_int32, _dp, C.c_int32,
+                                 _P(FtsDistStats)]),
+    "fts_dist_destroy": (None, [_vp]),
+    "fts_dist_last_error": (C.c_char_p, [_vp]),
+    "fts_ls_create": (C.c_int, [_P(FtsMesh), C.c_int32, _P(_vp)]),
+    "fts_ls_update": (C.c_int, [_vp, _P(FtsLsParams), _dp, _dp, _P(FtsLsStats)]),
+    "fts_ls_destroy": (None, [_vp]),
+    "fts_ls_last_error": (C.c_char_p, [_vp]),
 }
 
 NOALLOC_MAX_NODES = 1048576

@@ -1,0 +1,717 @@
+// Level-set update (LevelSet::update, src/fem/LevelSet.cpp:89-151, with the
+// distance reset resetPhi_, :429-455) on one GPU:
+//   1. Crank-Nicolson advection of phi by the nodal Stokes velocity:
+//        (M + dt/2 A) phi' = (M - dt/2 A) phi,
+//      M the P1 mass (assembled once), A(i,j) = int (V . grad phi_j) phi_i with
+//      V interpolated at the quadrature points from the nodal values
+//      (Assembler.hpp:179-190), both by the atomic-free node-row gather in
+//      FP64, then Jacobi-preconditioned BiCGSTAB (Eigen's algorithm and
+//      stopping rule, LevelSet.hpp:145) with device-side scalars;
+//   2. the distance reset: interface points on the edges whose end values
+//      differ in sign bit (LevelSet.cpp:278-300), the pruned exact distance
+//      search of dist.cu, the crossing edges' nodes keep the advected value, and
+//      phi = 0.75 phi_kept + 0.25 phi_reset (LevelSet.cpp:17-18, :147).
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "fts_device.cuh"
+#include "reduce.cuh"
+
+struct fts_dist;
+
+namespace fts {
+
+void dist_reset_device(fts_dist* D, const float* ifp, int32_t n_ifp, double* phi_dev,
+                       int32_t method, cudaStream_t s, fts_dist_stats* st);
+
+static std::string& g_ls_error() {
+    static thread_local std::string e;
+    return e;
+}
+
+constexpr int kLsThreads = 256;
+
+struct LsConst {
+    double phi[4][4];  // float-rounded basis table phi[a][q]
+    double qw;
+};
+
+static LsConst ls_const() {
+    const RefConstants R = ref_constants();
+    LsConst c;
+    std::memcpy(c.phi, R.phi, sizeof(c.phi));
+    c.qw = 0.25 / 6.0;
+    return c;
+}
+
+// Element geometry in FP64 from float coordinates (Assembler.hpp:430-462).
+__device__ __forceinline__ bool ls_geom(const float* __restrict__ xyz, const int ids[4],
+                                        double g[4][3], double& detB) {
+    double p[4][3];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) p[j][c] = (double)xyz[3 * (int64_t)ids[j] + c];
+    double B[3][3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        B[c][0] = p[1][c] - p[0][c];
+        B[c][1] = p[2][c] - p[0][c];
+        B[c][2] = p[3][c] - p[0][c];
+    }
+    const double c00 = B[1][1] * B[2][2] - B[1][2] * B[2][1];
+    const double c01 = B[1][2] * B[2][0] - B[1][0] * B[2][2];
+    const double c02 = B[1][0] * B[2][1] - B[1][1] * B[2][0];
+    const double det = B[0][0] * c00 + B[0][1] * c01 + B[0][2] * c02;
+    detB = fabs(det);
+    if (!(detB > 0.0)) return false;
+    double cof[3][3];
+    cof[0][0] = c00;
+    cof[0][1] = c01;
+    cof[0][2] = c02;
+    cof[1][0] = B[0][2] * B[2][1] - B[0][1] * B[2][2];
+    cof[1][1] = B[0][0] * B[2][2] - B[0][2] * B[2][0];
+    cof[1][2] = B[0][1] * B[2][0] - B[0][0] * B[2][1];
+    cof[2][0] = B[0][1] * B[1][2] - B[0][2] * B[1][1];
+    cof[2][1] = B[0][2] * B[1][0] - B[0][0] * B[1][2];
+    cof[2][2] = B[0][0] * B[1][1] - B[0][1] * B[1][0];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const double it0 = cof[r][0] / det, it1 = cof[r][1] / det, it2 = cof[r][2] / det;
+        g[0][r] = -it0 - it1 - it2;
+        g[1][r] = it0;
+        g[2][r] = it1;
+        g[3][r] = it2;
+    }
+    return true;
+}
+
+// feval . (qw) * detB with the reference's pairwise order.
+__device__ __forceinline__ double ls_integ(const double f[4], double qw, double detB) {
+    return ((f[0] * qw + f[2] * qw) + (f[1] * qw + f[3] * qw)) * detB;
+}
+
+// Row gather of M (mass == true) or A (nodal velocity `flow`), one thread per node.
+__global__ void k_ls_assemble(int64_t np, const int32_t* __restrict__ rowptr,
+                              const int32_t* __restrict__ cols,
+                              const int32_t* __restrict__ p2t_ptr,
+                              const uint32_t* __restrict__ p2t, const int32_t* __restrict__ tets,
+                              const float* __restrict__ xyz, const double* __restrict__ flow,
+                              LsConst K, double* __restrict__ out, int* __restrict__ bad) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t r0 = rowptr[i], r1 = rowptr[i + 1];
+        for (int32_t q = r0; q < r1; ++q) out[q] = 0.0;
+        for (int32_t e = p2t_ptr[i]; e < p2t_ptr[i + 1]; ++e) {
+            const uint32_t pe = p2t[e];
+            const int64_t k = pe >> 2;
+            const int a = pe & 3;
+            const int4 tt = reinterpret_cast<const int4*>(tets)[k];
+            const int ids[4] = {tt.x, tt.y, tt.z, tt.w};
+            double g[4][3], detB;
+            if (!ls_geom(xyz, ids, g, detB)) {
+                atomicOr(bad, 1);
+                continue;
+            }
+            double V[3][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
+            if (flow) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const double vj = flow[ids[j] + c * np];
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) V[c][q] += vj * K.phi[j][q];
+                    }
+            }
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                double f[4];
+                if (flow) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        f[q] = V[0][q] * (g[b][0] * K.phi[a][q]) + V[1][q] * (g[b][1] * K.phi[a][q]) +
+                               V[2][q] * (g[b][2] * K.phi[a][q]);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) f[q] = K.phi[b][q] * K.phi[a][q];
+                }
+                const double v = ls_integ(f, K.qw, detB);
+                int32_t slot = r0;
+                while (slot < r1 && cols[slot] != ids[b]) ++slot;
+                if (slot < r1) out[slot] += v;
+            }
+        }
+    }
+}
+
+// L = M + h A, b = (M - h A) phi, inv = 1 / diag(L) (1 where the diagonal is 0,
+// Eigen's DiagonalPreconditioner); x = phi (warm start).
+__global__ void k_ls_system(int64_t np, const int32_t* __restrict__ rowptr,
+                            const int32_t* __restrict__ cols, const double* __restrict__ M,
+                            const double* __restrict__ A, double h,
+                            const double* __restrict__ phi, double* __restrict__ L,
+                            double* __restrict__ b, double* __restrict__ inv,
+                            double* __restrict__ x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0, d = 0.0;
+        for (int32_t q = rowptr[i]; q < rowptr[i + 1]; ++q) {
+            const double l = M[q] + h * A[q];
+            L[q] = l;
+            acc += (M[q] - h * A[q]) * phi[cols[q]];
+            if (cols[q] == i) d = l;
+        }
+        b[i] = acc;
+        inv[i] = d != 0.0 ? 1.0 / d : 1.0;
+        x[i] = phi[i];
+    }
+}
+
+struct BjScalars {
+    double rho, rho_old, alpha, w, beta, r0n, rr, bb, tol2;
+    long long it, maxit;
+    int stop, restart, restarts;
+};
+
+__device__ __forceinline__ double csr_row(const int32_t* __restrict__ rowptr,
+                                          const int32_t* __restrict__ cols,
+                                          const double* __restrict__ L,
+                                          const double* __restrict__ v, int64_t i) {
+    double acc = 0.0;
+    for (int32_t q = rowptr[i]; q < rowptr[i + 1]; ++q) acc += L[q] * v[cols[q]];
+    return acc;
+}
+
+// r = b - L x, r0 = r (start, and Eigen's restart when rho collapses).
+// Start: p = vv = 0, rho = r0.r, stop if ||b|| = 0 or already converged.
+// Restart: rho = r0n = r.r, the iteration count resets on the first restart,
+// beta from the previous rho.
+__global__ void __launch_bounds__(kLsThreads)
+k_bj_residual(int64_t np, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ cols,
+              const double* __restrict__ L, const double* __restrict__ b,
+              const double* __restrict__ x, double* __restrict__ r, double* __restrict__ r0,
+              double* __restrict__ p, double* __restrict__ vv, int first, double tol,
+              Reduction red, BjScalars* S) {
+    double acc[2] = {0.0, 0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double ri = b[i] - csr_row(rowptr, cols, L, x, i);
+        r[i] = ri;
+        r0[i] = ri;
+        if (first) {
+            p[i] = 0.0;
+            vv[i] = 0.0;
+        }
+        acc[0] += ri * ri;
+        acc[1] += b[i] * b[i];
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
+        S->r0n = tot[0];
+        S->rr = tot[0];
+        S->restart = 0;
+        if (first) {
+            S->bb = tot[1];
+            S->tol2 = tol * tol * tot[1];
+            S->alpha = 1.0;
+            S->w = 1.0;
+            S->rho_old = 1.0;
+            S->rho = tot[0];
+            S->beta = tot[0];
+            S->it = 0;
+            S->restarts = 0;
+            S->stop = (tot[1] == 0.0 || tot[0] <= S->tol2 || S->maxit <= 0) ? 1 : 0;
+        } else {
+            S->rho = tot[0];
+            if (S->restarts++ == 0) S->it = 0;
+            S->beta = (S->rho / S->rho_old) * (S->alpha / S->w);
+            S->stop = 0;
+        }
+    }
+}
+
+// p = r + beta (p - w vv), y = inv p.
+__global__ void k_bj_p(int64_t np, const double* __restrict__ r, double* __restrict__ p,
+                       const double* __restrict__ vv, const double* __restrict__ inv,
+                       double* __restrict__ y, const BjScalars* __restrict__ S) {
+    if (S->stop) return;
+    const double beta = S->beta, w = S->w;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double pi = r[i] + beta * (p[i] - w * vv[i]);
+        p[i] = pi;
+        y[i] = inv[i] * pi;
+    }
+}
+
+// vv = L y; alpha = rho / (r0 . vv).
+__global__ void __launch_bounds__(kLsThreads)
+k_bj_spmv1(int64_t np, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ cols,
+           const double* __restrict__ L, const double* __restrict__ y,
+           const double* __restrict__ r0, double* __restrict__ vv, Reduction red, BjScalars* S) {
+    if (S->stop) return;
+    double acc[1] = {0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = csr_row(rowptr, cols, L, y, i);
+        vv[i] = v;
+        acc[0] += r0[i] * v;
+    }
+    double tot[1];
+    if (grid_sum<1>(acc, red, tot) && threadIdx.x == 0) S->alpha = S->rho / tot[0];
+}
+
+// s = r - alpha vv, z = inv s.
+__global__ void k_bj_s(int64_t np, const double* __restrict__ r, const double* __restrict__ vv,
+                       const double* __restrict__ inv, double* __restrict__ s,
+                       double* __restrict__ z, const BjScalars* __restrict__ S) {
+    if (S->stop) return;
+    const double alpha = S->alpha;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double si = r[i] - alpha * vv[i];
+        s[i] = si;
+        z[i] = inv[i] * si;
+    }
+}
+
+// t = L z; w = (t . s) / (t . t) (0 if t = 0).
+__global__ void __launch_bounds__(kLsThreads)
+k_bj_spmv2(int64_t np, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ cols,
+           const double* __restrict__ L, const double* __restrict__ z,
+           const double* __restrict__ s, double* __restrict__ t, Reduction red, BjScalars* S) {
+    if (S->stop) return;
+    double acc[2] = {0.0, 0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = csr_row(rowptr, cols, L, z, i);
+        t[i] = v;
+        acc[0] += v * v;
+        acc[1] += v * s[i];
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0)
+        S->w = tot[0] > 0.0 ? tot[1] / tot[0] : 0.0;
+}
+
+// x += alpha y + w z, r = s - w t; rr = r.r, rho_next = r0.r; the loop test
+// and the next beta (or a restart when rho collapses).
+__global__ void __launch_bounds__(kLsThreads)
+k_bj_update(int64_t np, double* __restrict__ x, const double* __restrict__ y,
+            const double* __restrict__ z, const double* __restrict__ s,
+            const double* __restrict__ t, double* __restrict__ r, const double* __restrict__ r0,
+            Reduction red, BjScalars* S) {
+    if (S->stop) return;
+    const double alpha = S->alpha, w = S->w;
+    double acc[2] = {0.0, 0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] += alpha * y[i] + w * z[i];
+        const double ri = s[i] - w * t[i];
+        r[i] = ri;
+        acc[0] += ri * ri;
+        acc[1] += r0[i] * ri;
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
+        S->rr = tot[0];
+        S->it += 1;
+        if (tot[0] <= S->tol2 || S->it >= S->maxit) {
+            S->stop = 1;
+            return;
+        }
+        S->rho_old = S->rho;
+        S->rho = tot[1];
+        const double eps2 = DBL_EPSILON * DBL_EPSILON;
+        if (fabs(S->rho) < eps2 * S->r0n) {
+            S->restart = 1;  // the host runs the restart residual
+            S->stop = 1;
+            return;
+        }
+        S->beta = (S->rho / S->rho_old) * (S->alpha / S->w);
+    }
+}
+
+// Interface points on the edges (i < j) whose end values differ in sign bit,
+// t = phi_i / (phi_i - phi_j) (0.5 if the difference is below FLT_MIN), the
+// point (1 - t) p_i + t p_j in double, stored as float; both nodes flagged.
+__global__ void k_ls_crossings(int64_t np, const int32_t* __restrict__ rowptr,
+                               const int32_t* __restrict__ cols, const double* __restrict__ x,
+                               const float* __restrict__ xyz, float* __restrict__ ifp,
+                               unsigned* __restrict__ count, uint8_t* __restrict__ keep,
+                               unsigned cap) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double xi = x[i];
+        for (int32_t q = rowptr[i]; q < rowptr[i + 1]; ++q) {
+            const int32_t j = cols[q];
+            if (j <= i) continue;
+            const double xj = x[j];
+            if (signbit(xi) == signbit(xj)) continue;
+            const double div = xi - xj;
+            const double t = fabs(div) > (double)FLT_MIN ? xi / div : 0.5;
+            const unsigned k = atomicAdd(count, 1u);
+            if (k < cap)
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                    ifp[3 * (int64_t)k + c] = (float)((1.0 - t) * (double)xyz[3 * i + c] +
+                                                      t * (double)xyz[3 * (int64_t)j + c]);
+            keep[i] = 1;
+            keep[j] = 1;
+        }
+    }
+}
+
+// phi = 0.75 (kept ? advected : reset) + 0.25 reset.
+__global__ void k_ls_mix(int64_t np, const double* __restrict__ adv, const double* __restrict__ ifn,
+                         const uint8_t* __restrict__ keep, double* __restrict__ phi) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double kept = keep[i] ? adv[i] : ifn[i];
+        phi[i] = 0.75 * kept + 0.25 * ifn[i];
+    }
+}
+
+__global__ void k_ls_check_velocity(int64_t n, const double* __restrict__ v,
+                                    int* __restrict__ nan_flag, Reduction red,
+                                    double* __restrict__ norm2) {
+    double acc[1] = {0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double vi = v[i];
+        if (isnan(vi) && i < 3 * (n / 4)) atomicOr(nan_flag, 1);
+        acc[0] += vi * vi;
+    }
+    double tot[1];
+    if (grid_sum<1>(acc, red, tot) && threadIdx.x == 0) *norm2 = tot[0];
+}
+
+}  // namespace fts
+
+using namespace fts;
+
+struct fts_ls {
+    int device = 0;
+    int num_sms = 148;
+    cudaStream_t stream = nullptr;
+    HostTopology topo;
+    int64_t np = 0, nt = 0, nnz = 0;
+    float* xyz = nullptr;
+    int32_t* tets = nullptr;
+    int32_t* rowptr = nullptr;
+    int32_t* cols = nullptr;
+    int32_t* p2t_ptr = nullptr;
+    uint32_t* p2t = nullptr;
+    double* M = nullptr;
+    double* A = nullptr;
+    double* L = nullptr;
+    double* flow = nullptr;
+    double* phi = nullptr;
+    double* vec[12] = {};  // x b r r0 p vv s t y z inv ifn
+    uint8_t* keep = nullptr;
+    float* ifp = nullptr;
+    unsigned ifp_cap = 0;
+    unsigned* count = nullptr;
+    int* flag = nullptr;
+    double* norm2 = nullptr;
+    BjScalars* S = nullptr;
+    BjScalars* S_host = nullptr;
+    Reduction red{nullptr, nullptr};
+    fts_dist* dist = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::string last_error;
+};
+
+namespace {
+
+template <typename T>
+T* ls_alloc(size_t n) {
+    void* p = nullptr;
+    FTS_CUDA(cudaMalloc(&p, n * sizeof(T) + 16));
+    return static_cast<T*>(p);
+}
+
+void ls_free(fts_ls& S) {
+    void* ptrs[] = {S.xyz, S.tets, S.rowptr, S.cols, S.p2t_ptr, S.p2t, S.M, S.A, S.L,
+                    S.flow, S.phi, S.keep, S.ifp, S.count, S.flag, S.norm2, S.S,
+                    S.red.partials, S.red.ticket};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (double* p : S.vec)
+        if (p) cudaFree(p);
+    if (S.S_host) cudaFreeHost(S.S_host);
+    if (S.dist) fts_dist_destroy(S.dist);
+    for (auto& e : S.ev)
+        if (e) cudaEventDestroy(e);
+    if (S.stream) cudaStreamDestroy(S.stream);
+}
+
+int grid_of(const fts_ls& S, int64_t work) {
+    const int64_t need = std::max<int64_t>(1, (work + kLsThreads - 1) / kLsThreads);
+    return (int)std::min<int64_t>(need, (int64_t)S.num_sms * 8);
+}
+
+}  // namespace
+
+extern "C" {
+
+int fts_ls_create(const fts_mesh* mesh, int32_t device, fts_ls** out) {
+    if (!mesh || !out) return FTS_ERR_BAD_INPUT;
+    *out = nullptr;
+    fts_ls* S = new (std::nothrow) fts_ls();
+    if (!S) return FTS_ERR_OOM;
+    S->device = device;
+    int rc = FTS_OK;
+    try {
+        std::string err;
+        rc = build_topology(*mesh, S->topo, err);
+        if (rc != FTS_OK) throw err;
+        FTS_CUDA(cudaSetDevice(device));
+        int sms = 0;
+        FTS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        S->num_sms = sms > 0 ? sms : 148;
+        FTS_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+        for (auto& e : S->ev) FTS_CUDA(cudaEventCreate(&e));
+        const HostTopology& T = S->topo;
+        S->np = T.np;
+        S->nt = T.nt;
+        S->nnz = T.rowptr[T.np];
+        S->xyz = ls_alloc<float>(3 * S->np);
+        S->tets = ls_alloc<int32_t>(4 * S->nt);
+        S->rowptr = ls_alloc<int32_t>(S->np + 1);
+        S->cols = ls_alloc<int32_t>(S->nnz);
+        S->p2t_ptr = ls_alloc<int32_t>(S->np + 1);
+        S->p2t = ls_alloc<uint32_t>(4 * S->nt);
+        S->M = ls_alloc<double>(S->nnz);
+        S->A = ls_alloc<double>(S->nnz);
+        S->L = ls_alloc<double>(S->nnz);
+        S->flow = ls_alloc<double>(4 * S->np);
+        S->phi = ls_alloc<double>(S->np);
+        for (auto& v : S->vec) v = ls_alloc<double>(S->np);
+        S->keep = ls_alloc<uint8_t>(S->np);
+        S->count = ls_alloc<unsigned>(1);
+        S->flag = ls_alloc<int>(1);
+        S->norm2 = ls_alloc<double>(1);
+        S->S = ls_alloc<BjScalars>(1);
+        FTS_CUDA(cudaMallocHost(&S->S_host, sizeof(BjScalars)));
+        S->red.partials = ls_alloc<double>(kMaxPartials * 4);
+        S->red.ticket = ls_alloc<unsigned>(1);
+        FTS_CUDA(cudaMemset(S->red.ticket, 0, sizeof(unsigned)));
+        FTS_CUDA(cudaMemcpy(S->xyz, mesh->xyz, 3 * S->np * sizeof(float), cudaMemcpyHostToDevice));
+        FTS_CUDA(cudaMemcpy(S->tets, mesh->tets, 4 * S->nt * sizeof(int32_t),
+                            cudaMemcpyHostToDevice));
+        FTS_CUDA(cudaMemcpy(S->rowptr, T.rowptr.data(), (S->np + 1) * sizeof(int32_t),
+                            cudaMemcpyHostToDevice));
+        FTS_CUDA(cudaMemcpy(S->cols, T.cols.data(), S->nnz * sizeof(int32_t),
+                            cudaMemcpyHostToDevice));
+        FTS_CUDA(cudaMemcpy(S->p2t_ptr, T.p2t_ptr.data(), (S->np + 1) * sizeof(int32_t),
+                            cudaMemcpyHostToDevice));
+        FTS_CUDA(cudaMemcpy(S->p2t, T.p2t.data(), 4 * S->nt * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice));
+        // the mass matrix, once per mesh (LevelSet.cpp:33-37)
+        static const LsConst K = ls_const();
+        FTS_CUDA(cudaMemset(S->flag, 0, sizeof(int)));
+        k_ls_assemble<<<grid_of(*S, S->np), kLsThreads, 0, S->stream>>>(
+            S->np, S->rowptr, S->cols, S->p2t_ptr, S->p2t, S->tets, S->xyz, nullptr, K, S->M,
+            S->flag);
+        int bad = 0;
+        FTS_CUDA(cudaMemcpyAsync(&bad, S->flag, sizeof(int), cudaMemcpyDeviceToHost, S->stream));
+        FTS_CUDA(cudaStreamSynchronize(S->stream));
+        if (bad) {
+            err = "degenerate tetrahedron (det B == 0)";
+            rc = FTS_ERR_DEGENERATE_ELEMENT;
+            throw err;
+        }
+        rc = fts_dist_create(mesh->xyz, S->np, device, &S->dist);
+        if (rc != FTS_OK) throw std::string(fts_dist_last_error(nullptr));
+    } catch (const std::string& e) {
+        g_ls_error() = e;
+        if (rc == FTS_OK) rc = FTS_ERR_BAD_INPUT;
+    } catch (const CudaError& e) {
+        g_ls_error() = e.what;
+        rc = e.code == cudaErrorMemoryAllocation ? FTS_ERR_OOM : FTS_ERR_CUDA;
+    } catch (const std::bad_alloc&) {
+        g_ls_error() = "host allocation failed";
+        rc = FTS_ERR_OOM;
+    }
+    if (rc != FTS_OK) {
+        ls_free(*S);
+        delete S;
+        return rc;
+    }
+    *out = S;
+    return FTS_OK;
+}
+
+int fts_ls_update(fts_ls* S, const fts_ls_params* P, const double* flow, double* phi,
+                  fts_ls_stats* stats) {
+    if (!S || !P || !flow || !phi) return FTS_ERR_BAD_INPUT;
+    const double t0 = wall_ms();
+    fts_ls_stats st;
+    std::memset(&st, 0, sizeof(st));
+    int rc = FTS_OK;
+    try {
+        FTS_CUDA(cudaSetDevice(S->device));
+        cudaStream_t s = S->stream;
+        const int64_t np = S->np;
+        const int g = grid_of(*S, np);
+        int launches = 0;
+        FTS_CUDA(cudaMemcpyAsync(S->flow, flow, 4 * np * sizeof(double), cudaMemcpyHostToDevice, s));
+        FTS_CUDA(cudaMemcpyAsync(S->phi, phi, np * sizeof(double), cudaMemcpyHostToDevice, s));
+        FTS_CUDA(cudaMemsetAsync(S->flag, 0, sizeof(int), s));
+        k_ls_check_velocity<<<g, kLsThreads, 0, s>>>(4 * np, S->flow, S->flag, S->red, S->norm2);
+        ++launches;
+        int nanv = 0;
+        double n2 = 0.0;
+        FTS_CUDA(cudaMemcpyAsync(&nanv, S->flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+        FTS_CUDA(cudaMemcpyAsync(&n2, S->norm2, sizeof(double), cudaMemcpyDeviceToHost, s));
+        FTS_CUDA(cudaStreamSynchronize(s));
+        // LevelSet.cpp:91-93: nothing to advect (a NaN norm is not below FLT_MIN)
+        if (P->dt < FLT_MIN || std::sqrt(n2) < FLT_MIN) {
+            st.ms_total = wall_ms() - t0;
+            if (stats) *stats = st;
+            return FTS_OK;
+        }
+        if (nanv) {  // LevelSet.cpp:111-114
+            S->last_error = "NaN in the velocity";
+            st.status = FTS_ERR_NAN;
+            st.ms_total = wall_ms() - t0;
+            if (stats) *stats = st;
+            return FTS_ERR_NAN;
+        }
+        static const LsConst K = ls_const();
+        double* x = S->vec[0];
+        double* b = S->vec[1];
+        double* r = S->vec[2];
+        double* r0 = S->vec[3];
+        double* p = S->vec[4];
+        double* vv = S->vec[5];
+        double* sv = S->vec[6];
+        double* t = S->vec[7];
+        double* y = S->vec[8];
+        double* z = S->vec[9];
+        double* inv = S->vec[10];
+        double* ifn = S->vec[11];
+        FTS_CUDA(cudaEventRecord(S->ev[0], s));
+        k_ls_assemble<<<g, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->p2t_ptr, S->p2t,
+                                               S->tets, S->xyz, S->flow, K, S->A, S->flag);
+        k_ls_system<<<g, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->M, S->A, 0.5 * P->dt,
+                                             S->phi, S->L, b, inv, x);
+        FTS_CUDA(cudaEventRecord(S->ev[1], s));
+        launches += 2;
+        // Jacobi BiCGSTAB, device scalars; the host polls every few iterations
+        BjScalars init{};
+        const long long maxit = P->max_iter > 0 ? P->max_iter : 2 * np;
+        init.maxit = maxit;
+        FTS_CUDA(cudaMemcpyAsync(S->S, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+        const double tol = P->tol > 0.0 ? P->tol : DBL_EPSILON;
+        k_bj_residual<<<g, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->L, b, x, r, r0, p, vv, 1,
+                                               tol, S->red, S->S);
+        ++launches;
+        const int poll = 8;
+        for (;;) {
+            for (int u = 0; u < poll; ++u) {
+                k_bj_p<<<g, kLsThreads, 0, s>>>(np, r, p, vv, inv, y, S->S);
+                k_bj_spmv1<<<g, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->L, y, r0, vv,
+                                                    S->red, S->S);
+                k_bj_s<<<g, kLsThreads, 0, s>>>(np, r, vv, inv, sv, z, S->S);
+                k_bj_spmv2<<<g, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->L, z, sv, t,
+                                                    S->red, S->S);
+                k_bj_update<<<g, kLsThreads, 0, s>>>(np, x, y, z, sv, t, r, r0, S->red, S->S);
+                launches += 5;
+            }
+            FTS_CUDA(cudaGetLastError());
+            FTS_CUDA(cudaMemcpyAsync(S->S_host, S->S, sizeof(BjScalars), cudaMemcpyDeviceToHost, s));
+            FTS_CUDA(cudaStreamSynchronize(s));
+            const BjScalars& H = *S->S_host;
+            if (!H.stop) continue;
+            if (H.restart) {
+                k_bj_residual<<<g, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->L, b, x, r, r0,
+                                                       p, vv, 0, tol, S->red, S->S);
+                ++launches;
+                continue;
+            }
+            break;
+        }
+        FTS_CUDA(cudaEventRecord(S->ev[2], s));
+        const BjScalars H = *S->S_host;
+        st.iterations = H.it;
+        st.error = H.bb > 0.0 ? std::sqrt(H.rr / H.bb) : 0.0;
+        if (!(H.rr <= H.tol2) && H.bb != 0.0) {  // LevelSet.cpp:135-139: phi untouched
+            S->last_error = "advection solve did not converge";
+            rc = FTS_ERR_NOT_CONVERGED;
+        } else if (!P->reset) {
+            FTS_CUDA(cudaMemcpyAsync(phi, x, np * sizeof(double), cudaMemcpyDeviceToHost, s));
+            FTS_CUDA(cudaStreamSynchronize(s));
+        } else {
+            // the distance reset (resetPhi_) of the advected phi
+            const unsigned cap = (unsigned)std::min<int64_t>((S->nnz - np) / 2 + 1, 0x7fffffff);
+            if (cap > S->ifp_cap) {
+                if (S->ifp) cudaFree(S->ifp);
+                S->ifp = nullptr;
+                S->ifp = ls_alloc<float>(3 * (size_t)cap);
+                S->ifp_cap = cap;
+            }
+            FTS_CUDA(cudaMemsetAsync(S->count, 0, sizeof(unsigned), s));
+            FTS_CUDA(cudaMemsetAsync(S->keep, 0, np, s));
+            k_ls_crossings<<<g, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, x, S->xyz, S->ifp,
+                                                    S->count, S->keep, S->ifp_cap);
+            ++launches;
+            unsigned nif = 0;
+            FTS_CUDA(cudaMemcpyAsync(&nif, S->count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+            FTS_CUDA(cudaStreamSynchronize(s));
+            nif = std::min(nif, S->ifp_cap);
+            std::vector<float> pts(3 * (size_t)nif);
+            if (nif > 0)
+                FTS_CUDA(cudaMemcpyAsync(pts.data(), S->ifp, pts.size() * sizeof(float),
+                                         cudaMemcpyDeviceToHost, s));
+            FTS_CUDA(cudaMemcpyAsync(ifn, x, np * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            FTS_CUDA(cudaStreamSynchronize(s));
+            dist_reset_device(S->dist, pts.data(), (int32_t)nif, ifn, FTS_DIST_PRUNED, s, nullptr);
+            k_ls_mix<<<g, kLsThreads, 0, s>>>(np, x, ifn, S->keep, S->phi);
+            launches += 2;
+            st.interface_points = nif;
+            FTS_CUDA(cudaMemcpyAsync(phi, S->phi, np * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
+        FTS_CUDA(cudaEventRecord(S->ev[3], s));
+        FTS_CUDA(cudaStreamSynchronize(s));
+        float ms = 0.f;
+        FTS_CUDA(cudaEventElapsedTime(&ms, S->ev[0], S->ev[1]));
+        st.ms_assembly = ms;
+        FTS_CUDA(cudaEventElapsedTime(&ms, S->ev[1], S->ev[2]));
+        st.ms_solve = ms;
+        FTS_CUDA(cudaEventElapsedTime(&ms, S->ev[2], S->ev[3]));
+        st.ms_reset = ms;
+        st.kernel_launches = launches;
+    } catch (const CudaError& e) {
+        S->last_error = e.what;
+        rc = e.code == cudaErrorMemoryAllocation ? FTS_ERR_OOM : FTS_ERR_CUDA;
+    } catch (const std::bad_alloc&) {
+        S->last_error = "host allocation failed";
+        rc = FTS_ERR_OOM;
+    }
+    st.status = rc;
+    st.ms_total = wall_ms() - t0;
+    if (stats) *stats = st;
+    return rc;
+}
+
+void fts_ls_destroy(fts_ls* S) {
+    if (!S) return;
+    cudaSetDevice(S->device);
+    if (S->stream) cudaStreamSynchronize(S->stream);
+    ls_free(*S);
+    delete S;
+}
+
+const char* fts_ls_last_error(const fts_ls* S) {
+    return S ? S->last_error.c_str() : g_ls_error().c_str();
+}
+
+}  // extern "C"

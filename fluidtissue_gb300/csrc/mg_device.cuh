@@ -142,6 +142,10 @@ __device__ __forceinline__ void stencil_h_body(int n, int64_t N, int v, int i, i
     y[2] = a2;
 }
 
+// SPLIT: a separate branch-free body for interior nodes (more registers; the
+// persistent batched kernel, which holds every phase in one function, keeps
+// the single checked body).
+template <bool SPLIT>
 __device__ __forceinline__ void stencil_apply_h(int n, int64_t N, int64_t v64,
                                                 const uint4* __restrict__ K,
                                                 const float* __restrict__ x, float y[3]) {
@@ -151,7 +155,7 @@ __device__ __forceinline__ void stencil_apply_h(int n, int64_t N, int64_t v64,
     const int rem = v - k * nn;
     const int j = rem / n;
     const int i = rem - j * n;
-    if (i > 0 && j > 0 && k > 0 && i < n - 1 && j < n - 1 && k < n - 1)
+    if (SPLIT && i > 0 && j > 0 && k > 0 && i < n - 1 && j < n - 1 && k < n - 1)
         stencil_h_body<true>(n, N, v, i, j, k, K, x, y);
     else
         stencil_h_body<false>(n, N, v, i, j, k, K, x, y);
@@ -160,12 +164,12 @@ __device__ __forceinline__ void stencil_apply_h(int n, int64_t N, int64_t v64,
 // y = K x at node v (3 components, without the level's scale); x SoA [3][N].
 // 32-bit lattice coordinates; interior nodes take the neighbour offsets
 // without range checks.
-template <typename T, typename KS>
+template <typename T, typename KS, bool SPLIT = true>
 __device__ __forceinline__ void stencil_apply(int n, int64_t N, int64_t v64,
                                               const KS* __restrict__ K,
                                               const T* __restrict__ x, T y[3]) {
     if constexpr (std::is_same<KS, __half>::value) {
-        stencil_apply_h(n, N, v64, reinterpret_cast<const uint4*>(K), x, y);
+        stencil_apply_h<SPLIT>(n, N, v64, reinterpret_cast<const uint4*>(K), x, y);
         return;
     }
     const int v = (int)v64;
@@ -231,7 +235,7 @@ enum : int {
 
 // Chebyshev step s >= 1 at node v.  Returns the new x value (3 components),
 // written to L.x unless `out` is non-null (the fused caller writes it).
-template <typename T>
+template <typename T, bool SPLIT = true>
 __device__ __forceinline__ void mg_step_node(const LevelView<T>& L, int64_t v, int step, int mode,
                                              const T* __restrict__ din, T* __restrict__ dout,
                                              T xo[3], bool write_x, bool write_rd) {
@@ -239,7 +243,7 @@ __device__ __forceinline__ void mg_step_node(const LevelView<T>& L, int64_t v, i
     const T A = (T)L.coef[2 * step - 1], B = (T)L.coef[2 * step];
     const T ks = (T)*L.ks;
     T y[3], rr[3], z[3];
-    stencil_apply<T>(L.n, N, v, L.K, din, y);
+    stencil_apply<T, typename MGStore<T>::type, SPLIT>(L.n, N, v, L.K, din, y);
     const T* rin = mode == kStepFromZero ? L.b : L.r;
 #pragma unroll
     for (int c = 0; c < 3; ++c) rr[c] = rin[c * N + v] - ks * y[c];
@@ -262,23 +266,23 @@ __device__ __forceinline__ void mg_step_node(const LevelView<T>& L, int64_t v, i
 }
 
 // r = b - K x at node v.
-template <typename T>
+template <typename T, bool SPLIT = true>
 __device__ __forceinline__ void mg_resid_node(const LevelView<T>& L, int64_t v) {
     const int64_t N = L.N;
     const T ks = (T)*L.ks;
     T y[3];
-    stencil_apply<T>(L.n, N, v, L.K, L.x, y);
+    stencil_apply<T, typename MGStore<T>::type, SPLIT>(L.n, N, v, L.K, L.x, y);
 #pragma unroll
     for (int c = 0; c < 3; ++c) L.r[c * N + v] = L.b[c * N + v] - ks * y[c];
 }
 
 // r = b - K x and d_0 = D^-1 r / theta at node v (x is left for the next step).
-template <typename T>
+template <typename T, bool SPLIT = true>
 __device__ __forceinline__ void mg_resid_first_node(const LevelView<T>& L, int64_t v) {
     const int64_t N = L.N;
     const T ks = (T)*L.ks;
     T y[3], rr[3];
-    stencil_apply<T>(L.n, N, v, L.K, L.x, y);
+    stencil_apply<T, typename MGStore<T>::type, SPLIT>(L.n, N, v, L.K, L.x, y);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         rr[c] = L.b[c * N + v] - ks * y[c];
@@ -351,7 +355,7 @@ __device__ __forceinline__ void mg_prolong_node(const LevelView<T>& F, const Lev
 
 // Coarsest level: `steps` Chebyshev steps from zero on L.b by the calling CTA
 // alone (every thread of the block must call it).
-template <typename T>
+template <typename T, bool SPLIT = true>
 __device__ __forceinline__ void mg_coarse_block(const LevelView<T>& L, int steps) {
     const int64_t N = L.N;
     for (int64_t v = threadIdx.x; v < N; v += blockDim.x) {
@@ -371,7 +375,7 @@ __device__ __forceinline__ void mg_coarse_block(const LevelView<T>& L, int steps
         T* dout = (s & 1) ? L.d1 : L.d0;
         const int mode = s == 1 ? kStepFromZero : kStepRegular;
         for (int64_t v = threadIdx.x; v < N; v += blockDim.x)
-            mg_step_node<T>(L, v, s, mode, din, dout, xo, true, true);
+            mg_step_node<T, SPLIT>(L, v, s, mode, din, dout, xo, true, true);
         __syncthreads();
     }
 }

@@ -321,6 +321,82 @@ int fts_rd_solve(fts_rd* rd, const fts_rd_params* params, const double* phi,
 void fts_rd_destroy(fts_rd* rd);
 const char* fts_rd_last_error(const fts_rd* rd);
 
+/* ------------------------------------------------------------------------
+ * Distance reset of the level set, replacing EuclideanDistance
+ * (src/fem/EuclideanDistance.hpp:13-51, EuclideanDistance.cu:45-118): for
+ * every mesh node p_k, phi_n[k] = min_j |ifp_j - p_k| over the interface
+ * points (float, each distance from norm3df as in the reference's kernel),
+ * negated where the old phi_n[k] < 0.  With no interface point the minimum is
+ * FLT_MAX, as in the reference.
+ *   FTS_DIST_PRUNED: the points sorted along a Morton curve into blocks of 32
+ *     with bounding boxes; each node scans only the blocks that can hold its
+ *     nearest point, and candidates within rounding of the minimum are
+ *     re-evaluated with norm3df, so the result equals the exhaustive minimum.
+ *   FTS_DIST_EXHAUSTIVE: the reference's algorithm (every node against every
+ *     point), for comparison.
+ * ------------------------------------------------------------------------ */
+enum { FTS_DIST_PRUNED = 0, FTS_DIST_EXHAUSTIVE = 1 };
+
+typedef struct fts_dist_stats {
+    int32_t status;
+    int32_t blocks;           /* point blocks */
+    int64_t points_scanned;   /* point distances evaluated (all nodes) */
+    double ms_setup;          /* host sort, uploads */
+    double ms_kernel;         /* device time of the distance kernel */
+    double ms_total;
+} fts_dist_stats;
+
+typedef struct fts_dist fts_dist;
+
+/* EuclideanDistance::init: node positions xyz[3 np] (float) on `device`. */
+int fts_dist_create(const float* xyz, int64_t np, int32_t device, fts_dist** out);
+/* EuclideanDistance::resetPhi: ifp[3 n_ifp] (float), phi_n[np] in/out (host). */
+int fts_dist_reset(fts_dist* d, const float* ifp, int32_t n_ifp, double* phi_n, int32_t method,
+                   fts_dist_stats* stats);
+void fts_dist_destroy(fts_dist* d);
+const char* fts_dist_last_error(const fts_dist* d);
+
+/* ------------------------------------------------------------------------
+ * Level-set update, replacing LevelSet::update (src/fem/LevelSet.cpp:89-151)
+ * with its distance reset resetPhi_ (:429-455; the interface triangulation
+ * and normals it also builds are not part of phi and are not computed):
+ *   Crank-Nicolson advection (M + dt/2 A) phi' = (M - dt/2 A) phi with the
+ *   nodal velocity of `flow` (A(i,j) = int (V . grad phi_j) phi_i), Jacobi-
+ *   preconditioned BiCGSTAB from phi to ||r|| <= tol ||b|| (Eigen's algorithm,
+ *   LevelSet.hpp:145), then (reset != 0) the distance reset to the edge
+ *   crossings of the advected zero level set, the crossing edges' nodes keeping
+ *   the advected value, and phi = 0.75 phi_kept + 0.25 phi_reset.
+ * dt < FLT_MIN or ||flow|| < FLT_MIN: returns at once, phi untouched.  A NaN
+ * velocity is FTS_ERR_NAN and an unconverged solve FTS_ERR_NOT_CONVERGED, phi
+ * untouched (LevelSet.cpp:111-114, :135-139).  All arithmetic FP64.
+ * ------------------------------------------------------------------------ */
+typedef struct fts_ls_params {
+    double dt;                /* "Advection dt" */
+    double tol;               /* "Advection tolerance" (<= 0: machine epsilon) */
+    int64_t max_iter;         /* "Max. CG iterations" (<= 0: 2 np) */
+    int32_t reset;            /* 1: distance reset after the advection (the reference) */
+} fts_ls_params;
+
+typedef struct fts_ls_stats {
+    int32_t status;
+    int64_t iterations;       /* BiCGSTAB iterations (Eigen's count) */
+    double error;             /* ||r|| / ||b|| at the stop */
+    int64_t interface_points;
+    double ms_assembly, ms_solve, ms_reset, ms_total;
+    int64_t kernel_launches;
+} fts_ls_stats;
+
+typedef struct fts_ls fts_ls;
+
+/* LevelSet's mesh on `device`; assembles the P1 mass matrix once
+ * (LevelSet.cpp:33-37).  FTS_ERR_DEGENERATE_ELEMENT for a flat tetrahedron. */
+int fts_ls_create(const fts_mesh* mesh, int32_t device, fts_ls** out);
+/* flow[4 np] = [ux, uy, uz, p] (Flow::solve's output), phi[np] in/out (host). */
+int fts_ls_update(fts_ls* ls, const fts_ls_params* params, const double* flow, double* phi,
+                  fts_ls_stats* stats);
+void fts_ls_destroy(fts_ls* ls);
+const char* fts_ls_last_error(const fts_ls* ls);
+
 #ifdef __cplusplus
 }
 #endif

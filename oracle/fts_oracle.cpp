@@ -30,6 +30,9 @@
 //  * scatter to [ux(np), uy(np), uz(np), p(np)]        src/growth/Flow.cpp:290-300
 //  * reaction-diffusion: interior submesh, lumped-mass  src/growth/RD.cpp:27-108, :116-172;
 //    Laplacian, explicit Euler                         src/fem/Assembler.cpp:75-84
+//  * distance reset of the level set (host path)       src/fem/EuclideanDistance.cu:16-38, :92-117
+//  * level-set update: Crank-Nicolson advection,        src/fem/LevelSet.cpp:89-151, :261-300,
+//    Jacobi-BiCGSTAB, distance reset and mixing          :429-455; Assembler.hpp:179-190
 #include <algorithm>
 #include <cfloat>
 #include <chrono>
@@ -930,6 +933,218 @@ int ora_rd_solve(int64_t np, int64_t nt, const float* xyz, const int32_t* tets,
         act[nodes[i]] = u[i];
         inh[nodes[i]] = v[i];
         gf[nodes[i]] = g[i];
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Distance reset (src/fem/EuclideanDistance.cu:16-38, :92-117, the host path):
+// phi_n[k] = min_j sqrt(dx*dx + dy*dy + dz*dz) in float with dx = ifp_j - p_k,
+// negated where the old phi_n[k] < 0; FLT_MAX when there is no point.  Nodes
+// k0 <= k < k1 only (the CPU baseline times a sample).
+// ---------------------------------------------------------------------------
+int ora_dist_reset(int64_t np, const float* xyz, const float* ifp, int32_t n_ifp, int64_t k0,
+                   int64_t k1, double* phi_n) {
+    if (k0 < 0 || k1 > np || k0 > k1) return -1;
+#pragma omp parallel for schedule(static)
+    for (int64_t k = k0; k < k1; ++k) {
+        const float p0 = xyz[3 * k], p1 = xyz[3 * k + 1], p2 = xyz[3 * k + 2];
+        float dmin = FLT_MAX;
+        for (int32_t j = 0; j < n_ifp; ++j) {
+            const float dx = ifp[3 * j] - p0;
+            const float dy = ifp[3 * j + 1] - p1;
+            const float dz = ifp[3 * j + 2] - p2;
+            const float d = std::sqrt(dx * dx + dy * dy + dz * dz);
+            if (d < dmin) dmin = d;
+        }
+        phi_n[k] = phi_n[k] < 0.0f ? -(double)dmin : (double)dmin;
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Level-set update (src/fem/LevelSet.cpp:89-151 with resetPhi_ :429-455)
+// ---------------------------------------------------------------------------
+// Crank-Nicolson advection of phi by the nodal velocity (flow[0..3np)):
+//   (M + dt/2 A) phi' = (M - dt/2 A) phi,
+//   M(i,j) = int phi_i phi_j,  A(i,j) = int (V . grad phi_j) phi_i with V
+//   interpolated at the quadrature points from the nodal values through the
+//   float-rounded table (Assembler.hpp:179-190; weak form LevelSet.cpp:106-108),
+// solved by Jacobi-preconditioned BiCGSTAB (Eigen's default preconditioner for
+// BiCGSTAB<SparseMatrix>, LevelSet.hpp:145) from phi, stop ||r|| <= tol ||b||,
+// at most maxit iterations (<= 0: 2N).  Then (reset != 0) the distance reset:
+// interface points on the edges whose end values differ in sign bit
+// (LevelSet.cpp:278-300), phi_ifn = +-distance to the nearest point
+// (EuclideanDistance host path), the crossing edges' nodes keep the advected
+// value, and phi = 0.75 phi_kept + 0.25 phi_ifn (LevelSet.cpp:17-18, :147).
+// Returns 0; 1 if the solver did not converge (phi untouched); 2 for a NaN
+// velocity (phi untouched); 3 for zero dt or zero flow (phi untouched, as the
+// reference's early return).
+namespace {
+
+// Eigen-style BiCGSTAB with a diagonal (Jacobi) preconditioner.
+int bicgstab_jacobi(int64_t N, const int64_t* rp, const int32_t* ci, const double* v,
+                    const double* b, double* x, double tol, int64_t maxit, int64_t* iters,
+                    double* err) {
+    std::vector<double> r(N), r0(N), p(N, 0.0), vv(N, 0.0), s(N), t(N), y(N), z(N), inv(N);
+    for (int64_t q = 0; q < N; ++q) {
+        double d = 0.0;
+        for (int64_t k = rp[q]; k < rp[q + 1]; ++k)
+            if (ci[k] == q) d = v[k];
+        inv[q] = d != 0.0 ? 1.0 / d : 1.0;
+    }
+    if (maxit <= 0) maxit = 2 * N;
+    spmv(N, rp, ci, v, x, r.data());
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < N; ++q) r[q] = b[q] - r[q];
+    const double bb = dot(N, b, b);
+    if (bb == 0.0) {
+        std::fill(x, x + N, 0.0);
+        if (iters) *iters = 0;
+        if (err) *err = 0.0;
+        return 0;
+    }
+    r0 = r;
+    double r0n = dot(N, r.data(), r.data());
+    double rr = r0n;
+    const double tol2 = tol * tol * bb;
+    const double eps2 = DBL_EPSILON * DBL_EPSILON;
+    double rho = 1.0, alpha = 1.0, w = 1.0;
+    int64_t it = 0;
+    int restarts = 0;
+    while (rr > tol2 && it < maxit) {
+        const double rho_old = rho;
+        rho = dot(N, r0.data(), r.data());
+        if (std::fabs(rho) < eps2 * r0n) {
+            spmv(N, rp, ci, v, x, r.data());
+#pragma omp parallel for schedule(static)
+            for (int64_t q = 0; q < N; ++q) r[q] = b[q] - r[q];
+            r0 = r;
+            rho = r0n = dot(N, r.data(), r.data());
+            if (restarts++ == 0) it = 0;
+        }
+        const double beta = (rho / rho_old) * (alpha / w);
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < N; ++q) {
+            p[q] = r[q] + beta * (p[q] - w * vv[q]);
+            y[q] = inv[q] * p[q];
+        }
+        spmv(N, rp, ci, v, y.data(), vv.data());
+        alpha = rho / dot(N, r0.data(), vv.data());
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < N; ++q) {
+            s[q] = r[q] - alpha * vv[q];
+            z[q] = inv[q] * s[q];
+        }
+        spmv(N, rp, ci, v, z.data(), t.data());
+        const double tt = dot(N, t.data(), t.data());
+        w = tt > 0.0 ? dot(N, t.data(), s.data()) / tt : 0.0;
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < N; ++q) {
+            x[q] += alpha * y[q] + w * z[q];
+            r[q] = s[q] - w * t[q];
+        }
+        rr = dot(N, r.data(), r.data());
+        ++it;
+    }
+    if (iters) *iters = it;
+    const double e = std::sqrt(rr / bb);
+    if (err) *err = e;
+    return rr <= tol2 ? 0 : 1;
+}
+
+}  // namespace
+
+int ora_ls_update(int64_t np, int64_t nt, const float* xyz, const int32_t* tets,
+                  const double* flow, double* phi, double dt, double tol, int64_t maxit,
+                  int reset, int64_t* iters, double* err, int64_t* n_ifp) {
+    if (iters) *iters = 0;
+    if (n_ifp) *n_ifp = 0;
+    double fn = 0.0;
+    for (int64_t q = 0; q < 4 * np; ++q) fn += flow[q] * flow[q];
+    if (dt < FLT_MIN || std::sqrt(fn) < FLT_MIN) return 3;
+    for (int64_t q = 0; q < 3 * np; ++q)
+        if (std::isnan(flow[q])) return 2;
+    Topology T;
+    build_topology(np, nt, tets, T);
+    const RefTables& R = tables();
+    const int64_t nnz = T.nb_ptr[np];
+    std::vector<double> Mv(nnz, 0.0), Av(nnz, 0.0);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < np; ++i) {
+        const int32_t* cols = T.nb.data() + T.nb_ptr[i];
+        const int ncol = (int)(T.nb_ptr[i + 1] - T.nb_ptr[i]);
+        for (int64_t q = T.p2t_ptr[i]; q < T.p2t_ptr[i + 1]; ++q) {
+            const int64_t k = T.p2t[q];
+            const int32_t* t = tets + 4 * k;
+            Geom G;
+            if (!element_geom(xyz, t, G)) continue;
+            int a = 0;
+            if (t[1] == i) a = 1;
+            else if (t[2] == i) a = 2;
+            else if (t[3] == i) a = 3;
+            double V[3][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
+            for (int j = 0; j < 4; ++j)
+                for (int c = 0; c < 3; ++c)
+                    for (int qq = 0; qq < 4; ++qq) V[c][qq] += flow[t[j] + c * np] * R.phi[j][qq];
+            for (int b = 0; b < 4; ++b) {
+                const int slot = find_col(cols, ncol, t[b]);
+                double f[4];
+                for (int qq = 0; qq < 4; ++qq) f[qq] = R.phi[b][qq] * R.phi[a][qq];
+                Mv[T.nb_ptr[i] + slot] += integ(f, R.qw, G.detB);
+                for (int qq = 0; qq < 4; ++qq)
+                    f[qq] = V[0][qq] * (G.g[b][0] * R.phi[a][qq]) +
+                            V[1][qq] * (G.g[b][1] * R.phi[a][qq]) +
+                            V[2][qq] * (G.g[b][2] * R.phi[a][qq]);
+                Av[T.nb_ptr[i] + slot] += integ(f, R.qw, G.detB);
+            }
+        }
+    }
+    const double h = 0.5 * dt;
+    std::vector<double> L(nnz), rhs(np), x(phi, phi + np);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < np; ++i) {
+        double sacc = 0.0;
+        for (int64_t k = T.nb_ptr[i]; k < T.nb_ptr[i + 1]; ++k) {
+            L[k] = Mv[k] + h * Av[k];
+            sacc += (Mv[k] - h * Av[k]) * phi[T.nb[k]];
+        }
+        rhs[i] = sacc;
+    }
+    std::vector<int64_t> rp(T.nb_ptr.begin(), T.nb_ptr.end());
+    int64_t it = 0;
+    double e = 0.0;
+    const int st = bicgstab_jacobi(np, rp.data(), T.nb.data(), L.data(), rhs.data(), x.data(),
+                                   tol > 0.0 ? tol : DBL_EPSILON, maxit, &it, &e);
+    if (iters) *iters = it;
+    if (err) *err = e;
+    if (st != 0) return 1;
+    if (!reset) {
+        std::copy(x.begin(), x.end(), phi);
+        return 0;
+    }
+    // interface points on the crossing edges (i < j)
+    std::vector<float> ifp;
+    std::vector<char> keep(np, 0);
+    for (int64_t i = 0; i < np; ++i)
+        for (int64_t k = T.nb_ptr[i]; k < T.nb_ptr[i + 1]; ++k) {
+            const int64_t j = T.nb[k];
+            if (j <= i || std::signbit(x[i]) == std::signbit(x[j])) continue;
+            double tt = 0.5;
+            const double div = x[i] - x[j];
+            if (std::fabs(div) > FLT_MIN) tt = x[i] / div;
+            for (int c = 0; c < 3; ++c)
+                ifp.push_back((float)((1.0 - tt) * (double)xyz[3 * i + c] +
+                                      tt * (double)xyz[3 * j + c]));
+            keep[i] = keep[j] = 1;
+        }
+    const int32_t nif = (int32_t)(ifp.size() / 3);
+    if (n_ifp) *n_ifp = nif;
+    std::vector<double> ifn(x);
+    ora_dist_reset(np, xyz, ifp.data(), nif, 0, np, ifn.data());
+    for (int64_t i = 0; i < np; ++i) {
+        const double kept = keep[i] ? x[i] : ifn[i];
+        phi[i] = 0.75 * kept + 0.25 * ifn[i];
     }
     return 0;
 }

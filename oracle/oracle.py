@@ -70,6 +70,9 @@ def lib():
                                          _p(dbl), dbl, _p(dbl), dbl, i64, _p(i64)]),
         "ora_rd_solve": (C.c_int, [i64, i64, _p(f32), _p(i32), _p(dbl), _p(i32), i32, _p(dbl),
                                    i64, _p(dbl), _p(dbl), _p(dbl)]),
+        "ora_dist_reset": (C.c_int, [i64, _p(f32), _p(f32), i32, i64, i64, _p(dbl)]),
+        "ora_ls_update": (C.c_int, [i64, i64, _p(f32), _p(i32), _p(dbl), _p(dbl), dbl, dbl, i64,
+                                    C.c_int, _p(i64), _p(dbl), _p(i64)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -369,6 +372,30 @@ def rd_solve(xyz, tets, phi, src_nodes, par, act, inh, gf):
                               _ptr(gf, D))
 
 
+def dist_reset(xyz, ifp, phi_n, k0=0, k1=None):
+    """EuclideanDistance::resetPhi restated (host path): phi_n updated in place
+    for nodes k0 <= k < k1; returns the status."""
+    xyz = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+    ifp = np.ascontiguousarray(ifp, np.float32).reshape(-1, 3)
+    assert phi_n.dtype == np.float64 and phi_n.flags["C_CONTIGUOUS"]
+    k1 = xyz.shape[0] if k1 is None else k1
+    return lib().ora_dist_reset(xyz.shape[0], _ptr(xyz, F32), _ptr(ifp, F32), ifp.shape[0], k0,
+                                k1, _ptr(phi_n, D))
+
+
+def ls_update(xyz, tets, flow, phi, dt, tol=1e-6, maxit=0, reset=True):
+    """LevelSet::update restated (advection + distance reset + mixing): phi
+    updated in place; returns (status, iterations, error, interface points)."""
+    assert phi.dtype == np.float64 and phi.flags["C_CONTIGUOUS"]
+    flow = np.ascontiguousarray(flow, np.float64)
+    it, err, nif = C.c_int64(), C.c_double(), C.c_int64()
+    st = lib().ora_ls_update(xyz.shape[0], tets.shape[0], _ptr(xyz, F32), _ptr(tets, I32),
+                             _ptr(flow, D), _ptr(phi, D), dt, tol, maxit, 1 if reset else 0,
+                             C.byref(it), C.byref(err), C.byref(nif))
+    return st, it.value, err.value, nif.value
+
+
 __all__ = ["build", "lib", "ref_tables", "boundary_nodes", "set_viscosity", "source",
            "assemble_blocks", "reduce", "spmv", "bicgstab", "true_residual", "scatter",
-           "system", "direct_solve", "solve_tight", "flow_solve", "rd_solve", "RD_KEYS"]
+           "system", "direct_solve", "solve_tight", "flow_solve", "rd_solve", "RD_KEYS",
+           "dist_reset", "ls_update"]

@@ -1,0 +1,61 @@
+"""Distance reset of the level set (fts_dist_*, the reference's
+EuclideanDistance): the pruned search returns exactly the reference
+algorithm's values (bit for bit, the same norm3df minimum), and both agree with
+the oracle's host restatement to float rounding."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import workload
+
+pytestmark = pytest.mark.gpu
+
+FLT_MAX = float(np.finfo(np.float32).max)
+
+
+def _reset(xyz, ifp, phi, method):
+    from fluidtissue_gb300.distance import EuclideanDistance
+    d = EuclideanDistance()
+    assert d.init(xyz) == 0, d.last_error()
+    out = np.ascontiguousarray(phi, np.float64).copy()
+    assert d.resetPhi(ifp, out, method) == 0, d.last_error()
+    st = d.last_stats
+    d.close()
+    return out, st
+
+
+def _point_sets(inst):
+    from fluidtissue_gb300.distance import interface_points
+    rng = np.random.default_rng(11)
+    ifp, _ = interface_points(inst.xyz, inst.tets, inst.phi)
+    cluster = (0.5 + 0.01 * rng.standard_normal((300, 3))).astype(np.float32)
+    return {"interface": ifp,
+            "uniform": rng.random((700, 3)).astype(np.float32),
+            "cluster+duplicates": np.concatenate([cluster, cluster[:50]]),
+            "single": np.array([[0.3, 0.7, 0.1]], np.float32),
+            "on_nodes": inst.xyz[rng.choice(inst.np, 40, replace=False)]}
+
+
+@pytest.mark.parametrize("name,n", [("ellipsoid129", 33), ("sphere65", 21)])
+def test_pruned_equals_reference_algorithm(name, n):
+    import oracle as O
+    inst = workload(name, n)
+    for label, ifp in _point_sets(inst).items():
+        ex, _ = _reset(inst.xyz, ifp, inst.phi, "exhaustive")
+        pr, st = _reset(inst.xyz, ifp, inst.phi, "pruned")
+        assert np.array_equal(pr, ex), (label, np.abs(pr - ex).max())
+        assert np.array_equal(np.signbit(pr), inst.phi < 0), label
+        ref = np.ascontiguousarray(inst.phi, np.float64).copy()
+        assert O.dist_reset(inst.xyz, ifp, ref) == 0
+        ulp = np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
+        assert np.all(np.abs(pr - ref) <= 4 * ulp), label
+        if label == "interface":
+            assert st["points_scanned"] < 0.5 * inst.np * len(ifp), st
+
+
+def test_no_interface_point_gives_flt_max():
+    inst = workload("sphere17", 9)
+    out, _ = _reset(inst.xyz, np.zeros((0, 3), np.float32), inst.phi, "pruned")
+    assert np.all(np.abs(out) == FLT_MAX)
+    assert np.array_equal(out < 0, inst.phi < 0)

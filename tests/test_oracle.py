@@ -289,3 +289,23 @@ def test_rd_sources_and_refusal():
     assert np.all(g[inside[:2]] == 5.0) and g.max() == 5.0 and (g > 0).sum() > 2
     outside = np.where(inst.phi >= 0)[0][:1]
     assert O.rd_solve(inst.xyz, inst.tets, inst.phi, outside, par, a, i, g) == -1
+
+
+# ---- distance reset (EuclideanDistance) restatement --------------------------
+
+def test_distance_reset_matches_numpy_float32():
+    """The host path in float: min_j sqrt(dx*dx + dy*dy + dz*dz), sign of the
+    old value; against the same sums in numpy float32."""
+    inst = workload("sphere17", 9)
+    rng = np.random.default_rng(4)
+    ifp = rng.random((257, 3)).astype(np.float32)
+    phi = np.ascontiguousarray(inst.phi, np.float64).copy()
+    assert O.dist_reset(inst.xyz, ifp, phi) == 0
+    d = ifp[None, :, :] - inst.xyz[:, None, :]
+    dd = np.sqrt(d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1] + d[..., 2] * d[..., 2]).min(axis=1)
+    want = np.where(inst.phi < 0, -dd.astype(np.float64), dd.astype(np.float64))
+    ulp = np.spacing(np.abs(want).astype(np.float32)).astype(np.float64)
+    assert np.all(np.abs(phi - want) <= ulp)
+    empty = np.ascontiguousarray(inst.phi, np.float64).copy()
+    assert O.dist_reset(inst.xyz, np.zeros((0, 3), np.float32), empty) == 0
+    assert np.all(np.abs(empty) == np.finfo(np.float32).max)
