@@ -639,8 +639,10 @@ int fts_ls_update(fts_ls* S, const fts_ls_params* P, const double* flow, double*
             }
             break;
         }
-        FTS_CUDA(cudaEventRecord(S->ev[2], s));
         const BjScalars H = *S->S_host;
+        if (H.bb == 0.0)  // Eigen: a zero right-hand side gives x = 0
+            FTS_CUDA(cudaMemsetAsync(x, 0, np * sizeof(double), s));
+        FTS_CUDA(cudaEventRecord(S->ev[2], s));
         st.iterations = H.it;
         st.error = H.bb > 0.0 ? std::sqrt(H.rr / H.bb) : 0.0;
         if (!(H.rr <= H.tol2) && H.bb != 0.0) {  // LevelSet.cpp:135-139: phi untouched

@@ -309,3 +309,44 @@ def test_distance_reset_matches_numpy_float32():
     empty = np.ascontiguousarray(inst.phi, np.float64).copy()
     assert O.dist_reset(inst.xyz, np.zeros((0, 3), np.float32), empty) == 0
     assert np.all(np.abs(empty) == np.finfo(np.float32).max)
+
+
+# ---- level-set update (LevelSet::update) restatement ---------------------------
+
+def test_levelset_zero_velocity_and_constant_phi():
+    """With no velocity the advection solve is M phi' = M phi, so phi' = phi;
+    a uniform velocity field translates nothing for a constant phi either."""
+    inst = workload("sphere65", 11)
+    phi = np.ascontiguousarray(inst.phi, np.float64).copy()
+    flow = np.zeros(4 * inst.np)
+    flow[3 * inst.np:] = 1.0  # pressure only: ||flow|| > 0, velocity 0
+    st, it, err, _ = O.ls_update(inst.xyz, inst.tets, flow, phi, 0.1, tol=1e-14, reset=False)
+    assert st == 0 and np.allclose(phi, inst.phi, rtol=0, atol=1e-13)
+    const = np.full(inst.np, 0.3)
+    flow[:3 * inst.np] = 0.2
+    st, *_ = O.ls_update(inst.xyz, inst.tets, flow, const, 0.1, tol=1e-14, reset=False)
+    assert st == 0 and np.allclose(const, 0.3, rtol=0, atol=1e-12)
+    # early return: zero dt
+    phi2 = np.ascontiguousarray(inst.phi, np.float64).copy()
+    assert O.ls_update(inst.xyz, inst.tets, flow, phi2, 0.0)[0] == 3
+    assert np.array_equal(phi2, inst.phi)
+
+
+def test_levelset_reset_is_distance_away_from_crossings():
+    """After the reset, nodes away from crossing edges hold 0.75 phi_ifn +
+    0.25 phi_ifn = the signed distance to the nearest interface point."""
+    import fluidtissue_gb300.distance as Dm
+    inst = workload("sphere65", 13)
+    flow = np.zeros(4 * inst.np)
+    flow[3 * inst.np:] = 1.0
+    phi = np.ascontiguousarray(inst.phi, np.float64).copy()
+    st, it, err, nif = O.ls_update(inst.xyz, inst.tets, flow, phi, 0.1, tol=1e-14, reset=True)
+    assert st == 0 and nif > 0
+    pts, edges = Dm.interface_points(inst.xyz, inst.tets, inst.phi)
+    assert len(pts) == nif
+    crossing = np.zeros(inst.np, bool)
+    crossing[edges.ravel()] = True
+    d = np.ascontiguousarray(inst.phi, np.float64).copy()
+    O.dist_reset(inst.xyz, pts, d)
+    far = ~crossing
+    assert np.allclose(phi[far], d[far], rtol=1e-6, atol=1e-7)
