@@ -5,7 +5,7 @@
 //      M the P1 mass (assembled once), A(i,j) = int (V . grad phi_j) phi_i with
 //      V interpolated at the quadrature points from the nodal values
 //      (Assembler.hpp:179-190), both by the atomic-free node-row gather in
-//      FP64, then Jacobi-preconditioned BiCGSTAB (Eigen's algorithm and
+//      FP64 from element geometry stored once per mesh, then Jacobi-preconditioned BiCGSTAB (Eigen's algorithm and
 //      stopping rule, LevelSet.hpp:145) with device-side scalars;
 //   2. the distance reset: interface points on the edges whose end values
 //      differ in sign bit (LevelSet.cpp:278-300), the pruned exact distance
@@ -91,18 +91,44 @@ __device__ __forceinline__ bool ls_geom(const float* __restrict__ xyz, const int
     return true;
 }
 
+// Per-element geometry, computed once per mesh (the coordinates never change):
+// gradients and |det B| (128 B).
+struct LsGeom {
+    double g[4][3];
+    double detB;
+    double pad[3];
+};
+
+__global__ void k_ls_geometry(int64_t nt, const int32_t* __restrict__ tets,
+                              const float* __restrict__ xyz, LsGeom* __restrict__ geom,
+                              int* __restrict__ bad) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nt;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int4 tt = reinterpret_cast<const int4*>(tets)[k];
+        const int ids[4] = {tt.x, tt.y, tt.z, tt.w};
+        LsGeom G;
+        if (!ls_geom(xyz, ids, G.g, G.detB)) {
+            atomicOr(bad, 1);
+            G.detB = 0.0;
+        }
+        G.pad[0] = G.pad[1] = G.pad[2] = 0.0;
+        geom[k] = G;
+    }
+}
+
 // feval . (qw) * detB with the reference's pairwise order.
 __device__ __forceinline__ double ls_integ(const double f[4], double qw, double detB) {
     return ((f[0] * qw + f[2] * qw) + (f[1] * qw + f[3] * qw)) * detB;
 }
 
-// Row gather of M (mass == true) or A (nodal velocity `flow`), one thread per node.
+// Row gather of M (flow == NULL) or A (nodal velocity `flow`), one thread per
+// node, from the stored element geometry.
 __global__ void k_ls_assemble(int64_t np, const int32_t* __restrict__ rowptr,
                               const int32_t* __restrict__ cols,
                               const int32_t* __restrict__ p2t_ptr,
                               const uint32_t* __restrict__ p2t, const int32_t* __restrict__ tets,
-                              const float* __restrict__ xyz, const double* __restrict__ flow,
-                              LsConst K, double* __restrict__ out, int* __restrict__ bad) {
+                              const LsGeom* __restrict__ geom, const double* __restrict__ flow,
+                              LsConst K, double* __restrict__ out) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t r0 = rowptr[i], r1 = rowptr[i + 1];
@@ -113,11 +139,13 @@ __global__ void k_ls_assemble(int64_t np, const int32_t* __restrict__ rowptr,
             const int a = pe & 3;
             const int4 tt = reinterpret_cast<const int4*>(tets)[k];
             const int ids[4] = {tt.x, tt.y, tt.z, tt.w};
-            double g[4][3], detB;
-            if (!ls_geom(xyz, ids, g, detB)) {
-                atomicOr(bad, 1);
-                continue;
-            }
+            const LsGeom& G = geom[k];
+            const double detB = G.detB;
+            double g[4][3];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) g[j][c] = G.g[j][c];
             double V[3][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
             if (flow) {
 #pragma unroll
@@ -408,6 +436,7 @@ struct fts_ls {
     int32_t* cols = nullptr;
     int32_t* p2t_ptr = nullptr;
     uint32_t* p2t = nullptr;
+    LsGeom* geom = nullptr;
     double* M = nullptr;
     double* A = nullptr;
     double* L = nullptr;
@@ -438,7 +467,7 @@ T* ls_alloc(size_t n) {
 }
 
 void ls_free(fts_ls& S) {
-    void* ptrs[] = {S.xyz, S.tets, S.rowptr, S.cols, S.p2t_ptr, S.p2t, S.M, S.A, S.L,
+    void* ptrs[] = {S.xyz, S.tets, S.rowptr, S.cols, S.p2t_ptr, S.p2t, S.geom, S.M, S.A, S.L,
                     S.flow, S.phi, S.keep, S.ifp, S.count, S.flag, S.norm2, S.S,
                     S.red.partials, S.red.ticket};
     for (void* p : ptrs)
@@ -488,6 +517,7 @@ int fts_ls_create(const fts_mesh* mesh, int32_t device, fts_ls** out) {
         S->cols = ls_alloc<int32_t>(S->nnz);
         S->p2t_ptr = ls_alloc<int32_t>(S->np + 1);
         S->p2t = ls_alloc<uint32_t>(4 * S->nt);
+        S->geom = ls_alloc<LsGeom>(S->nt);
         S->M = ls_alloc<double>(S->nnz);
         S->A = ls_alloc<double>(S->nnz);
         S->L = ls_alloc<double>(S->nnz);
@@ -517,9 +547,10 @@ int fts_ls_create(const fts_mesh* mesh, int32_t device, fts_ls** out) {
         // the mass matrix, once per mesh (LevelSet.cpp:33-37)
         static const LsConst K = ls_const();
         FTS_CUDA(cudaMemset(S->flag, 0, sizeof(int)));
+        k_ls_geometry<<<grid_of(*S, S->nt), kLsThreads, 0, S->stream>>>(S->nt, S->tets, S->xyz,
+                                                                         S->geom, S->flag);
         k_ls_assemble<<<grid_of(*S, S->np), kLsThreads, 0, S->stream>>>(
-            S->np, S->rowptr, S->cols, S->p2t_ptr, S->p2t, S->tets, S->xyz, nullptr, K, S->M,
-            S->flag);
+            S->np, S->rowptr, S->cols, S->p2t_ptr, S->p2t, S->tets, S->geom, nullptr, K, S->M);
         int bad = 0;
         FTS_CUDA(cudaMemcpyAsync(&bad, S->flag, sizeof(int), cudaMemcpyDeviceToHost, S->stream));
         FTS_CUDA(cudaStreamSynchronize(S->stream));
@@ -600,7 +631,7 @@ int fts_ls_update(fts_ls* S, const fts_ls_params* P, const double* flow, double*
         double* ifn = S->vec[11];
         FTS_CUDA(cudaEventRecord(S->ev[0], s));
         k_ls_assemble<<<g, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->p2t_ptr, S->p2t,
-                                               S->tets, S->xyz, S->flow, K, S->A, S->flag);
+                                               S->tets, S->geom, S->flow, K, S->A);
         k_ls_system<<<g, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->M, S->A, 0.5 * P->dt,
                                              S->phi, S->L, b, inv, x);
         FTS_CUDA(cudaEventRecord(S->ev[1], s));
