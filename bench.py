@@ -718,7 +718,8 @@ def main():
     ap.add_argument("--steps-fp64", type=int, default=2)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ellipsoid129")
-    ap.add_argument("--preconditioner", default="auto", choices=["auto", "jacobi", "multigrid"])
+    ap.add_argument("--preconditioner", default="auto",
+                    choices=["auto", "jacobi", "multigrid", "multigrid_diag"])
     ap.add_argument("--inner-tol", type=float, default=0.0)
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
     ap.add_argument("--batch-count", type=int, default=96)

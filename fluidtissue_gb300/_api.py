@@ -158,7 +158,7 @@ class FtsLsStats(C.Structure):
 
 PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_MINRES, SOLVER_BICGSTAB = 0, 1
-PC_AUTO, PC_JACOBI, PC_MULTIGRID = 0, 1, 2
+PC_AUTO, PC_JACOBI, PC_MULTIGRID, PC_MULTIGRID_DIAG = 0, 1, 2, 3
 OP_AUTO, OP_ASSEMBLED, OP_MATFREE, OP_STENCIL = 0, 1, 2, 3
 
 STATUS = {

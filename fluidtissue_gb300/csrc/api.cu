@@ -26,6 +26,11 @@ void free_all(Ctx& c) {
         if (p) cudaFree(p);
     mg_free(c.mg64);
     mg_free(c.mg32);
+    pmg_free(c.pmg64);
+    pmg_free(c.pmg32);
+    if (c.ev_fork) cudaEventDestroy(c.ev_fork);
+    if (c.ev_join) cudaEventDestroy(c.ev_join);
+    if (c.aux_stream) cudaStreamDestroy(c.aux_stream);
     if (c.ms_host) cudaFreeHost(c.ms_host);
     if (c.os_host) cudaFreeHost(c.os_host);
     for (auto& e : c.ev)
@@ -144,6 +149,10 @@ int validate_params(const fts_params& p, std::string& err) {
         err = "unknown operator kind";
         return FTS_ERR_BAD_INPUT;
     }
+    if (p.preconditioner < FTS_PC_AUTO || p.preconditioner > FTS_PC_MULTIGRID_DIAG) {
+        err = "unknown preconditioner";
+        return FTS_ERR_BAD_INPUT;
+    }
     if (p.solver != FTS_SOLVER_MINRES && p.solver != FTS_SOLVER_BICGSTAB) {
         err = "unknown solver";
         return FTS_ERR_BAD_INPUT;
@@ -176,12 +185,20 @@ static void configure_preconditioner(Ctx& c) {
     const int n = c.topo.lattice_n;
     const bool mg_ok = n > 0 && mg_levels(n) >= 3 &&
                        (n % 2 == 1 || last_layers_dirichlet(c.topo, n));
-    if (c.par.preconditioner == FTS_PC_MULTIGRID && !mg_ok) {
+    const bool want_mg = c.par.preconditioner == FTS_PC_MULTIGRID ||
+                         c.par.preconditioner == FTS_PC_MULTIGRID_DIAG;
+    if (want_mg && !mg_ok) {
         c.last_error = "multigrid needs a Kuhn lattice mesh with n >= 9 (even n: Dirichlet "
                        "nodes on the last layer of every axis)";
         throw (int)FTS_ERR_UNSUPPORTED;
     }
     c.use_mg = mg_ok && c.par.preconditioner != FTS_PC_JACOBI;
+    c.use_pmg = c.use_mg && !c.in_batch && c.par.preconditioner != FTS_PC_MULTIGRID_DIAG;
+    if (c.use_pmg && !c.aux_stream) {
+        FTS_CUDA(cudaStreamCreateWithFlags(&c.aux_stream, cudaStreamNonBlocking));
+        FTS_CUDA(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));
+        FTS_CUDA(cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming));
+    }
     if (c.par.operator_kind == FTS_OP_STENCIL && n == 0) {
         c.last_error = "the stencil operator needs a Kuhn lattice mesh";
         throw (int)FTS_ERR_UNSUPPORTED;

@@ -9,6 +9,7 @@
 #include "fts.h"
 #include "fts_internal.h"
 #include "mg.cuh"
+#include "pmg.cuh"
 
 struct fts_ctx;
 
@@ -172,6 +173,13 @@ struct Ctx {
     bool use_mg = false;
     MG<double> mg64;
     MG<float> mg32;
+    // pressure-block V-cycle (Kuhn lattices with the velocity multigrid): runs
+    // on aux_stream between the events ev_fork and ev_join of each application
+    bool use_pmg = false;
+    PMG<double> pmg64;
+    PMG<float> pmg32;
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double volume = 0.0;  // sum of element volumes
     double crank = 0.0;   // 1 / (eps * volume), 0 when eps = 0
 

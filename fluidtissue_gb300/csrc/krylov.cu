@@ -18,6 +18,7 @@
 #include "fts_device.cuh"
 #include "mg.cuh"
 #include "mg_device.cuh"
+#include "pmg_device.cuh"
 #include "reduce.cuh"
 
 namespace fts {
@@ -430,13 +431,14 @@ k_minres_A_lat(int n, int64_t np, const float4* __restrict__ L, const V4<float>*
 // Preconditioner stage 1.
 //   init: n = r0 (written to Rn)      else: n = q - c1 R1 - c2 R2 (written to Rn = R1)
 //   y.w = ip * n.w;  Jacobi: y.xyz = D3^-1 n.xyz;  multigrid: b0 = n.xyz (SoA)
+//   pressure multigrid (pmg): y.w = 0 here, pressure b0 = n.w (stage 2 sets y.w)
 // Jacobi finishes beta here; multigrid leaves sum(n.w) and n.w y.w for stage 2.
 template <typename T, bool MGV>
 __global__ void __launch_bounds__(kThreads)
 k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
              const V4<T>* __restrict__ R2, V4<T>* Rn, const T* __restrict__ pc,
-             V4<T>* __restrict__ Ynew, int ybuf, LevelView<T> L0, Reduction red,
-             MinresScalars* s) {
+             V4<T>* __restrict__ Ynew, int ybuf, LevelView<T> L0, PView<T> P0, int pmg,
+             Reduction red, MinresScalars* s) {
     if (s->stop) return;
     T c1 = T(0), c2 = T(0);
     if (!init) {
@@ -460,7 +462,13 @@ k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
         V4<T> z;
         if (MGV) {
             z.x = z.y = z.z = T(0);
-            z.w = pc[8 * i + 6] * n.w;
+            if (pmg) {
+                z.w = T(0);
+                P0.b[i] = n.w;
+                pmg_first_dir<T>(P0, i, n.w);
+            } else {
+                z.w = pc[8 * i + 6] * n.w;
+            }
             L0.b[i] = n.x;
             L0.b[np + i] = n.y;
             L0.b[2 * np + i] = n.z;
@@ -488,14 +496,16 @@ k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
 }
 
 // Multigrid stage 2, fused with the V-cycle's last post-smoothing step on the
-// finest level: y.xyz = the step's new x (not stored in the level); beta.
+// finest level: y.xyz = the step's new x (not stored in the level), and with
+// pmg y.w likewise from the pressure V-cycle; beta.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, int init,
-             const V4<T>* __restrict__ Rn, V4<T>* __restrict__ Ynew, int ybuf, Reduction red,
-             MinresScalars* s) {
+k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, PView<T> P0,
+             int pmg, int init, const V4<T>* __restrict__ Rn, V4<T>* __restrict__ Ynew,
+             int ybuf, Reduction red, MinresScalars* s) {
     if (s->stop) return;
     double acc[1] = {0.0};
+    const T* pdin = (step & 1) ? P0.d0 : P0.d1;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L0.N;
          i += (int64_t)gridDim.x * blockDim.x) {
         T xo[3];
@@ -505,6 +515,10 @@ k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, int
         z.x = xo[0];
         z.y = xo[1];
         z.z = xo[2];
+        if (pmg) {
+            z.w = pmg_step_node<T>(P0, i, step, mode, pdin, nullptr, false);
+            acc[0] += (double)(n.w * z.w);
+        }
         Ynew[i] = z;
         acc[0] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z);
     }
@@ -568,6 +582,12 @@ template <>
 MG<double>& mg_of<double>(Ctx& c) { return c.mg64; }
 template <>
 MG<float>& mg_of<float>(Ctx& c) { return c.mg32; }
+template <typename T>
+static PMG<T>& pmg_of(Ctx& c);
+template <>
+PMG<double>& pmg_of<double>(Ctx& c) { return c.pmg64; }
+template <>
+PMG<float>& pmg_of<float>(Ctx& c) { return c.pmg32; }
 
 // y = P^-1 n for the Lanczos vector in Rn (stage 1, V-cycle, stage 2).
 template <typename T>
@@ -579,18 +599,29 @@ static void launch_pc(Ctx& c, bool use_mg, int init, const V4<T>* q, V4<T>* R1, 
     if (use_mg) {
         MG<T>& mg = mg_of<T>(c);
         const LevelView<T> L0 = level_view(mg, 0);
+        const bool pmg = c.use_pmg;
+        const PView<T> P0 = pmg ? pview(pmg_of<T>(c), 0) : PView<T>{};
         k_minres_pc1<T, true><<<gn, kThreads, 0, c.stream>>>(c.np, init, q, R1, R2, Rn, pc, Ynew,
-                                                             ybuf, L0, c.red, c.ms);
+                                                             ybuf, L0, P0, pmg ? 1 : 0, c.red,
+                                                             c.ms);
+        if (pmg) {  // pressure V-cycle on the second stream, beside the velocity one
+            FTS_CUDA(cudaEventRecord(c.ev_fork, c.stream));
+            FTS_CUDA(cudaStreamWaitEvent(c.aux_stream, c.ev_fork, 0));
+            pmg_vcycle<T>(c, pmg_of<T>(c), c.aux_stream, &c.ms->stop, true);
+            FTS_CUDA(cudaEventRecord(c.ev_join, c.aux_stream));
+        }
         mg_vcycle<T>(c, mg, &c.ms->stop, true);
+        if (pmg) FTS_CUDA(cudaStreamWaitEvent(c.stream, c.ev_join, 0));
         // the last post-smoothing step: step kSmooth - 1 reads d0 when it is odd
         constexpr int s = kSmooth - 1;
         k_minres_pc2<T><<<gn, kThreads, 0, c.stream>>>(
-            L0, s, s == 1 ? kStepAfterFirst : kStepRegular, (s & 1) ? L0.d0 : L0.d1, init, Rn,
-            Ynew, ybuf, c.red, c.ms);
+            L0, s, s == 1 ? kStepAfterFirst : kStepRegular, (s & 1) ? L0.d0 : L0.d1, P0,
+            pmg ? 1 : 0, init, Rn, Ynew, ybuf, c.red, c.ms);
         c.launches += 2;
     } else {
         k_minres_pc1<T, false><<<gn, kThreads, 0, c.stream>>>(c.np, init, q, R1, R2, Rn, pc, Ynew,
-                                                              ybuf, LevelView<T>{}, c.red, c.ms);
+                                                              ybuf, LevelView<T>{}, PView<T>{}, 0,
+                                                              c.red, c.ms);
         c.launches += 1;
     }
     (void)w;
@@ -688,6 +719,7 @@ template long long minres_inner<float>(Ctx&, double, long long, double*, int*);
 template <typename T>
 void setup_preconditioner(Ctx& c) {
     if (c.use_mg) mg_setup<T>(c, mg_of<T>(c));
+    if (c.use_pmg) pmg_setup<T>(c, pmg_of<T>(c));
 }
 template void setup_preconditioner<double>(Ctx&);
 template void setup_preconditioner<float>(Ctx&);

@@ -58,12 +58,11 @@ static int dir_index(int dx, int dy, int dz) {
 
 // Galerkin term table: coarse block (I, I + off[dJ]) = sum over terms (a, e, w)
 // of w * K_f(f, dir e) with f = 2I + off[a], g = f + off[e] a child of I + off[dJ].
-static void init_tables(int device) {
-    static bool done[64] = {};
-    if (device < 64 && done[device]) return;
-    std::vector<int> start(16, 0);
-    std::vector<unsigned short> term;
-    std::vector<float> w;
+void galerkin_terms(std::vector<int>& start, std::vector<unsigned short>& term,
+                    std::vector<float>& w) {
+    start.assign(16, 0);
+    term.clear();
+    w.clear();
     for (int dJ = 0; dJ < 15; ++dJ) {
         start[dJ] = (int)term.size();
         for (int a = 0; a < 15; ++a) {
@@ -80,6 +79,15 @@ static void init_tables(int device) {
         }
     }
     start[15] = (int)term.size();
+}
+
+static void init_tables(int device) {
+    static bool done[64] = {};
+    if (device < 64 && done[device]) return;
+    std::vector<int> start;
+    std::vector<unsigned short> term;
+    std::vector<float> w;
+    galerkin_terms(start, term, w);
     FTS_CUDA(cudaMemcpyToSymbol(c_gal_start, start.data(), 16 * sizeof(int)));
     FTS_CUDA(cudaMemcpyToSymbol(c_gal_term, term.data(), term.size() * sizeof(unsigned short)));
     FTS_CUDA(cudaMemcpyToSymbol(c_gal_w, w.data(), w.size() * sizeof(float)));

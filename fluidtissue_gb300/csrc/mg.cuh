@@ -80,6 +80,12 @@ inline std::vector<int> mg_chain(int n) {
     return out;
 }
 
+// Term table of the Galerkin product P^T K P on Kuhn lattices: for coarse
+// direction dJ, terms start[dJ]..start[dJ+1]-1 of (a | e << 4, weight): the
+// fine node f = 2I + off[a] and its direction e.
+void galerkin_terms(std::vector<int>& start, std::vector<unsigned short>& term,
+                    std::vector<float>& w);
+
 template <typename T>
 void mg_setup(Ctx& c, MG<T>& mg);
 // V-cycle on mg.L[0].b, whose first Chebyshev direction L[0].d0 the caller has

@@ -22,7 +22,8 @@ from . import _api as A
 from . import _native as N
 
 PREC = {"fp64": A.PREC_FP64, "mixed": A.PREC_MIXED}
-PC = {"auto": A.PC_AUTO, "jacobi": A.PC_JACOBI, "multigrid": A.PC_MULTIGRID}
+PC = {"auto": A.PC_AUTO, "jacobi": A.PC_JACOBI, "multigrid": A.PC_MULTIGRID,
+      "multigrid_diag": A.PC_MULTIGRID_DIAG}
 SOLVER = {"minres": A.SOLVER_MINRES, "bicgstab": A.SOLVER_BICGSTAB}
 OP = {"auto": A.OP_AUTO, "assembled": A.OP_ASSEMBLED, "matfree": A.OP_MATFREE,
       "stencil": A.OP_STENCIL}

@@ -53,11 +53,18 @@ enum {
     FTS_SOLVER_BICGSTAB = 1  /* un-preconditioned BiCGSTAB on the reference's form, as Flow.hpp:62 */
 };
 
-/* Velocity-block preconditioner of MINRES. */
+/* Preconditioner of MINRES: blockdiag(velocity part, pressure part) plus the
+ * rank-one term of the constant pressure mode. */
 enum {
-    FTS_PC_AUTO = 0,      /* multigrid when the mesh is a Kuhn lattice with odd n, else Jacobi */
-    FTS_PC_JACOBI = 1,    /* node 3x3 block Jacobi (any mesh) */
-    FTS_PC_MULTIGRID = 2  /* geometric multigrid V-cycle (Kuhn lattices only) */
+    FTS_PC_AUTO = 0,           /* FTS_PC_MULTIGRID when the mesh is a Kuhn lattice that
+                                  allows it, else FTS_PC_JACOBI */
+    FTS_PC_JACOBI = 1,         /* velocity: node 3x3 block Jacobi; pressure: inverse of the
+                                  diagonal of (alpha D + eps M) + lumped 1/mu mass (any mesh) */
+    FTS_PC_MULTIGRID = 2,      /* velocity: geometric multigrid V-cycle; pressure: scalar
+                                  multigrid V-cycle of (alpha D + eps M) + lumped 1/mu mass,
+                                  run concurrently (Kuhn lattices only; batched solves use
+                                  the pressure diagonal) */
+    FTS_PC_MULTIGRID_DIAG = 3  /* velocity V-cycle, pressure diagonal as in FTS_PC_JACOBI */
 };
 
 /* Operator representation. */
