@@ -17,7 +17,7 @@ namespace fts {
 void free_all(Ctx& c) {
     void* ptrs[] = {c.xyz, c.tets, c.bnd, c.rowptr, c.cols, c.diag, c.p2t_ptr, c.p2t, c.geom,
                     c.phi, c.src, c.force, c.mu, c.s, c.flow, c.A64, c.A32, c.ell_val,
-                    c.ell_col, c.ell_ptr, c.lat_val, c.lat_src, c.pc64, c.pc32,
+                    c.ell_col, c.ell_ptr, c.lat_val, c.lat_src, c.lat64, c.pc64, c.pc32,
                     c.b, c.x, c.r, c.w64.q, c.w64.R[0], c.w64.R[1], c.w64.Y[0], c.w64.Y[1],
                     c.w64.W[0], c.w64.W[1], c.w64.X, c.w32.q, c.w32.R[0], c.w32.R[1],
                     c.w32.Y[0], c.w32.Y[1], c.w32.W[0], c.w32.W[1], c.w32.X, c.w32.r0, c.ms,
@@ -205,6 +205,8 @@ static void configure_preconditioner(Ctx& c) {
     }
     c.use_lat = !c.matfree && !c.in_batch && n > 0 &&
                 (c.par.operator_kind == FTS_OP_AUTO || c.par.operator_kind == FTS_OP_STENCIL);
+    c.use_lat64 = c.use_lat && c.par.precision == FTS_PREC_MIXED &&
+                  c.par.solver == FTS_SOLVER_MINRES;
     if (c.matfree && (!c.use_mg || c.par.precision != FTS_PREC_MIXED)) {
         c.last_error = "the matrix-free operator runs in mixed precision with the multigrid "
                        "preconditioner (Kuhn lattice, odd n >= 9)";
@@ -242,7 +244,10 @@ void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
     c.s = dev_alloc<double>(c, c.np);
     c.flow = dev_alloc<double>(c, 4 * c.np);
     c.matfree = p.operator_kind == FTS_OP_MATFREE;
-    if (!c.matfree) c.A64 = dev_alloc<double>(c, (size_t)c.nnzb * 16);
+    // Single solves allocate the FP64 BSR at its first assembly
+    // (launch_assemble); batched instances hand its address to the batch's
+    // device table when the batch is built, before any assembly.
+    if (!c.matfree && c.in_batch) c.A64 = dev_alloc<double>(c, (size_t)c.nnzb * 16);
     c.pc64 = dev_alloc<double>(c, (size_t)c.np * 8);
     c.b = dev_alloc<V4<double>>(c, c.np);
     c.x = dev_alloc<V4<double>>(c, c.np);
@@ -351,6 +356,14 @@ static int solve_device(Ctx& c, bool have_mu, bool have_force, double* flow_out,
         // no block matrix: pressure weights and the multigrid fine level come
         // straight from the elements
         launch_mf_pc(c);
+        setup_preconditioner<float>(c);
+    } else if (c.use_lat64) {
+        // Kuhn lattice, mixed precision: FP64 and FP32 half stencils straight
+        // from the elements (no BSR)
+        ensure_fp32(c);
+        launch_assemble_lat(c);
+        launch_preconditioner(c);
+        launch_to_f32(c);
         setup_preconditioner<float>(c);
     } else {
         launch_assemble(c);
@@ -736,6 +749,7 @@ int fts_get_system(const fts_ctx* ctx, int32_t* rowptr, int32_t* cols, double* v
     if (c.matfree) return FTS_ERR_UNSUPPORTED;
     try {
         FTS_CUDA(cudaSetDevice(c.device));
+        if (vals) ensure_bsr64(const_cast<Ctx&>(c));
         FTS_CUDA(cudaStreamSynchronize(c.stream));
         if (rowptr) std::memcpy(rowptr, c.topo.rowptr.data(), (c.np + 1) * sizeof(int32_t));
         if (cols) std::memcpy(cols, c.topo.cols.data(), c.nnzb * sizeof(int32_t));
@@ -759,6 +773,7 @@ int fts_apply(fts_ctx* ctx, int32_t precision, const double* x, double* y) {
             c.last_error = "no FP32 operator assembled";
             return FTS_ERR_BAD_INPUT;
         }
+        if (precision != FTS_PREC_MIXED) ensure_bsr64(c);
         FTS_CUDA(cudaMemcpyAsync(c.r, x, c.np * 4 * sizeof(double), cudaMemcpyHostToDevice,
                                  c.stream));
         V4<double>* out = reinterpret_cast<V4<double>*>(c.flow);  // 4*np doubles of scratch

@@ -16,6 +16,7 @@
 #include <cfloat>
 
 #include "fts_device.cuh"
+#include "mg_device.cuh"
 #include "reduce.cuh"
 
 namespace fts {
@@ -360,6 +361,7 @@ __global__ void k_assemble(int64_t np, const int32_t* __restrict__ rowptr,
 }
 
 void launch_assemble(Ctx& c) {
+    if (!c.A64) c.A64 = dev_alloc<double>(c, (size_t)c.nnzb * 16);
     int max_row = c.topo.max_row;
     size_t per_warp = (size_t)max_row * 16 * sizeof(double);
     int wpb = 8;
@@ -375,6 +377,102 @@ void launch_assemble(Ctx& c) {
                                                     c.par.eps, ref_args(), max_row, c.A64);
     FTS_CUDA(cudaGetLastError());
     c.launches += 1;
+    c.a64_valid = true;
+}
+
+void ensure_bsr64(Ctx& c) {
+    if (!c.a64_valid && !c.matfree) launch_assemble(c);
+}
+
+// ---------------------------------------------------------------------------
+// Lattice assembly (Kuhn lattices): one thread per (node v, stored direction
+// d = 0..7) computes the 4x4 block (v, v + off[d]) by walking the elements of
+// v and keeping those that also hold v + off[d] — the same terms, expressions
+// and element order as k_assemble's row gather, so the block is bit-identical
+// to the BSR's — with the same Dirichlet masking, and writes it to the FP64
+// half stencil (lat64_idx) and the FP32 one (lat_idx of the Krylov kernels).
+// The row gather's warp per row is latency bound on the element walk (66 ms at
+// 129^3); here each thread walks one node's elements with no search and no
+// shared-memory staging.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads)
+k_assemble_lat(int n, const int32_t* __restrict__ p2t_ptr, const uint32_t* __restrict__ p2t,
+               const int32_t* __restrict__ tets, const ElemGeom* __restrict__ geom,
+               const double* __restrict__ mu, const uint8_t* __restrict__ bnd, double alpha,
+               double eps, RefArgs R, double2* __restrict__ L64, float4* __restrict__ L32) {
+    const int64_t N = (int64_t)n * n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * 8;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int d = (int)(t / N);
+        const int64_t v = t - d * N;
+        const int i = (int)(v % n), j = (int)((v / n) % n), k = (int)(v / ((int64_t)n * n));
+        const int w = nbr(i, j, k, d, n);
+        double blk[16];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) blk[e] = 0.0;
+        if (w >= 0) {
+            for (int32_t q = p2t_ptr[v]; q < p2t_ptr[v + 1]; ++q) {
+                const uint32_t pk = p2t[q];
+                const int64_t el = pk >> 2;
+                const int a = pk & 3;
+                const int4 tt = reinterpret_cast<const int4*>(tets)[el];
+                const int b =
+                    tt.x == w ? 0 : (tt.y == w ? 1 : (tt.z == w ? 2 : (tt.w == w ? 3 : -1)));
+                if (b < 0) continue;
+                const ElemGeom* G = geom + el;
+                const double ga[3] = {G->g[a][0], G->g[a][1], G->g[a][2]};
+                const double gb[3] = {G->g[b][0], G->g[b][1], G->g[b][2]};
+                const double vol = G->vol;
+                const double gg = ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2];
+                const double mv = mu[el] * vol;
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int cc = 0; cc < 3; ++cc)
+                        blk[4 * r + cc] += mv * ((r == cc ? gg : 0.0) + ga[cc] * gb[r]);
+#pragma unroll
+                for (int r = 0; r < 3; ++r) blk[4 * r + 3] += -(ga[r] * R.wq[b] * vol);
+#pragma unroll
+                for (int cc = 0; cc < 3; ++cc) blk[12 + cc] += -(gb[cc] * R.wq[a] * vol);
+                blk[15] += -(alpha * (G->hh * vol * gg) + eps * (vol * R.mref[a][b]));
+            }
+            const bool bi = bnd[v] != 0, bw = bnd[w] != 0;
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const int r = e >> 2, cc = e & 3;
+                if (bi && r < 3) blk[e] = (d == 0 && r == cc) ? 1.0 : 0.0;
+                else if (cc < 3 && bw) blk[e] = 0.0;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            L64[lat64_idx(d, r, 0, v)] = make_double2(blk[4 * r], blk[4 * r + 1]);
+            L64[lat64_idx(d, r, 1, v)] = make_double2(blk[4 * r + 2], blk[4 * r + 3]);
+            L32[((v >> 5) * 32 + d * 4 + r) * 32 + (v & 31)] =
+                make_float4((float)blk[4 * r], (float)blk[4 * r + 1], (float)blk[4 * r + 2],
+                            (float)blk[4 * r + 3]);
+        }
+    }
+}
+
+void launch_assemble_lat(Ctx& c) {
+    const int n = c.topo.lattice_n;
+    if (n <= 0 || !c.lat_val)
+        throw CudaError(cudaErrorInvalidValue, "lattice assembly without a lattice operator",
+                        __FILE__, __LINE__);
+    const int64_t tiles = (c.np + 31) / 32;
+    if (!c.lat64) {
+        c.lat64 = dev_alloc<double2>(c, (size_t)tiles * 64 * 32);
+        // tile padding past the last node stays zero
+        FTS_CUDA(cudaMemsetAsync(c.lat64, 0, (size_t)tiles * 64 * 32 * sizeof(double2),
+                                 c.stream));
+    }
+    k_assemble_lat<<<grid_for(c, c.np * 8), kThreads, 0, c.stream>>>(
+        n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.bnd, c.par.alpha, c.par.eps, ref_args(),
+        c.lat64, reinterpret_cast<float4*>(c.lat_val));
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+    c.a64_valid = false;
 }
 
 // ---------------------------------------------------------------------------
@@ -384,15 +482,39 @@ void launch_assemble(Ctx& c) {
 // mass, a Schur-complement estimate).  pc[8 i + 0..5] = xx xy xz yy yz zz,
 // pc[8 i + 6] = pressure weight.
 // ---------------------------------------------------------------------------
-__global__ void k_preconditioner(int64_t np, const int32_t* __restrict__ diag,
-                                 const int32_t* __restrict__ p2t_ptr,
+// Diagonal block (i, i) of the BSR and of the FP64 lattice half stencil.
+struct BsrDiag {
+    const double* A;
+    const int32_t* diag;
+    __device__ __forceinline__ void load(int64_t i, double D[16]) const {
+        const double* p = A + (int64_t)diag[i] * 16;
+#pragma unroll
+        for (int e = 0; e < 16; ++e) D[e] = p[e];
+    }
+};
+struct LatDiag {
+    const double2* L;
+    __device__ __forceinline__ void load(int64_t i, double D[16]) const {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const double2 u = L[lat64_idx(0, r, 0, i)], w = L[lat64_idx(0, r, 1, i)];
+            D[4 * r] = u.x;
+            D[4 * r + 1] = u.y;
+            D[4 * r + 2] = w.x;
+            D[4 * r + 3] = w.y;
+        }
+    }
+};
+
+template <typename Diag>
+__global__ void k_preconditioner(int64_t np, Diag dg, const int32_t* __restrict__ p2t_ptr,
                                  const uint32_t* __restrict__ p2t,
                                  const ElemGeom* __restrict__ geom, const double* __restrict__ mu,
-                                 const uint8_t* __restrict__ bnd, const double* __restrict__ A,
-                                 double* __restrict__ pc) {
+                                 const uint8_t* __restrict__ bnd, double* __restrict__ pc) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
          i += (int64_t)gridDim.x * blockDim.x) {
-        const double* D = A + (int64_t)diag[i] * 16;
+        double D[16];
+        dg.load(i, D);
         double o[8];
         if (bnd[i]) {
             o[0] = 1.0; o[1] = 0.0; o[2] = 0.0; o[3] = 1.0; o[4] = 0.0; o[5] = 1.0;
@@ -423,8 +545,12 @@ __global__ void k_preconditioner(int64_t np, const int32_t* __restrict__ diag,
 }
 
 void launch_preconditioner(Ctx& c) {
-    k_preconditioner<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
-        c.np, c.diag, c.p2t_ptr, c.p2t, c.geom, c.mu, c.bnd, c.A64, c.pc64);
+    if (c.use_lat64)
+        k_preconditioner<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
+            c.np, LatDiag{c.lat64}, c.p2t_ptr, c.p2t, c.geom, c.mu, c.bnd, c.pc64);
+    else
+        k_preconditioner<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
+            c.np, BsrDiag{c.A64, c.diag}, c.p2t_ptr, c.p2t, c.geom, c.mu, c.bnd, c.pc64);
     FTS_CUDA(cudaGetLastError());
     c.launches += 1;
 }
@@ -496,6 +622,13 @@ void launch_to_f32(Ctx& c) {
         (!c.use_lat && !c.use_ell && !c.A32) || !c.pc32)
         throw CudaError(cudaErrorInvalidValue, "FP32 operator copy used before allocation",
                         __FILE__, __LINE__);
+    if (c.use_lat64) {
+        // lat_val was written by the lattice assembly
+        k_to_f32<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(c.np * 8, c.pc64, c.pc32);
+        FTS_CUDA(cudaGetLastError());
+        c.launches += 1;
+        return;
+    }
     if (c.use_lat) {
         const int64_t tiles = (c.np + 31) / 32;
         k_to_lat<<<grid_for(c, tiles * 256), kThreads, 0, c.stream>>>(

@@ -54,6 +54,14 @@ struct alignas(128) ElemGeom {
     double pad[2];
 };
 
+// FP64 lattice half stencil (Kuhn lattices, mixed precision): entries
+// (r, 2h) and (r, 2h + 1) of node v's 4x4 block towards direction d (0 = self,
+// 1..7 positive Kuhn directions) as one double2; tiles of 32 nodes, so a
+// warp's access to one (d, r, h) is 512 contiguous bytes; 1 KB per node.
+__host__ __device__ __forceinline__ int64_t lat64_idx(int d, int r, int h, int64_t v) {
+    return ((v >> 5) * 64 + d * 8 + r * 2 + h) * 32 + (v & 31);
+}
+
 // Scalar state of one MINRES run (Paige & Saunders 1975), kept on the device
 // so that the iteration never waits on the host.
 struct MinresScalars {
@@ -145,6 +153,12 @@ struct Ctx {
     float* lat_val = nullptr;   // [ceil(np / 32) * 128 * 32]
     int32_t* lat_src = nullptr; // [ceil(np / 32) * 32 * 8] BSR block of (v, v + d) or -1
     bool use_lat = false;
+    // FP64 half stencil of the same layout family (lat64_idx), assembled
+    // straight from the elements in mixed precision on Kuhn lattices; the BSR
+    // A64 is then assembled only when a caller asks for it (a64_valid)
+    double2* lat64 = nullptr;
+    bool use_lat64 = false;
+    bool a64_valid = false;
     bool in_batch = false;
     double* pc64 = nullptr;   // 8 per node: inverse of the 3x3 velocity block (xx,xy,xz,yy,yz,zz),
     float* pc32 = nullptr;    // inverse pressure weight, pad
@@ -215,7 +229,9 @@ void launch_viscosity_profile(Ctx& c);
 void launch_mu_minmax(Ctx& c);
 void launch_source(Ctx& c);
 void launch_rhs(Ctx& c, bool have_force);
-void launch_assemble(Ctx& c);
+void launch_assemble(Ctx& c);       // FP64 BSR (allocated on first use)
+void launch_assemble_lat(Ctx& c);   // FP64 + FP32 lattice half stencils
+void ensure_bsr64(Ctx& c);          // BSR of the current system for callers that read it
 void launch_preconditioner(Ctx& c);
 void launch_to_f32(Ctx& c);
 void launch_scatter_flow(Ctx& c, double* flow_out);

@@ -206,9 +206,72 @@ __global__ void k_residual64(int64_t np, const int32_t* __restrict__ rowptr,
     }
 }
 
+// The same from the FP64 lattice half stencil, one thread per node.
+__global__ void __launch_bounds__(kThreads)
+k_residual64_lat(int n, int64_t np, const double2* __restrict__ L,
+                 const V4<double>* __restrict__ x, const V4<double>* __restrict__ b,
+                 V4<double>* __restrict__ r, Reduction red, OuterScalars* os) {
+    double acc[2] = {0.0, 0.0};
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < np;
+         v += (int64_t)gridDim.x * blockDim.x) {
+        const int vi = (int)v;
+        const int k = vi / (n * n), j = (vi / n) % n, i = vi % n;
+        double a[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {  // own blocks: row r . x_w
+            const int w = nbr(i, j, k, d, n);
+            if (w < 0) continue;
+            const V4<double> xw = x[w];
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) {
+                const double2 u = L[lat64_idx(d, rr, 0, v)], s2 = L[lat64_idx(d, rr, 1, v)];
+                a[rr] += u.x * xw.x + u.y * xw.y + s2.x * xw.z + s2.y * xw.w;
+            }
+        }
+#pragma unroll
+        for (int d = 1; d < 8; ++d) {  // the neighbour's block towards v, transposed
+            const int w = nbr(i, j, k, d + 7, n);
+            if (w < 0) continue;
+            const V4<double> xw = x[w];
+            const double xr[4] = {xw.x, xw.y, xw.z, xw.w};
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) {
+                const double2 u = L[lat64_idx(d, rr, 0, w)], s2 = L[lat64_idx(d, rr, 1, w)];
+                a[0] += u.x * xr[rr];
+                a[1] += u.y * xr[rr];
+                a[2] += s2.x * xr[rr];
+                a[3] += s2.y * xr[rr];
+            }
+        }
+        const V4<double> bv = b[v];
+        V4<double> o;
+        o.x = bv.x - a[0];
+        o.y = bv.y - a[1];
+        o.z = bv.z - a[2];
+        o.w = bv.w - a[3];
+        r[v] = o;
+        acc[0] += o.x * o.x + o.y * o.y + o.z * o.z + o.w * o.w;
+        acc[1] += bv.x * bv.x + bv.y * bv.y + bv.z * bv.z + bv.w * bv.w;
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
+        os->rr = tot[0];
+        os->bb = tot[1];
+        os->scale = tot[0] > 0.0 ? 1.0 / sqrt(tot[0]) : 0.0;
+        os->nonfinite = isfinite(tot[0]) ? 0 : 1;
+    }
+}
+
 void launch_residual64(Ctx& c) {
     if (c.matfree) {
         launch_mf_residual64(c);
+        return;
+    }
+    if (c.use_lat64) {
+        k_residual64_lat<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
+            c.topo.lattice_n, c.np, c.lat64, c.x, c.b, c.r, c.red, c.os);
+        FTS_CUDA(cudaGetLastError());
+        c.launches += 1;
         return;
     }
     k_residual64<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(

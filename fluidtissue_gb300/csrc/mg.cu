@@ -140,6 +140,25 @@ __global__ void k_mg_extract(int n, const int32_t* __restrict__ rowptr,
     }
 }
 
+// Fine level from the FP64 lattice half stencil: the velocity 3x3 part of the
+// same 8 blocks per node.
+template <typename T>
+__global__ void k_mg_extract_lat(int n, const double2* __restrict__ L, T* __restrict__ K) {
+    const int64_t N = (int64_t)n * n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * 8;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int d = (int)(t / N);
+        const int64_t v = t - d * N;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const double2 u = L[lat64_idx(d, r, 0, v)], w = L[lat64_idx(d, r, 1, v)];
+            K[kidx(d * 9 + 3 * r, v)] = (T)u.x;
+            K[kidx(d * 9 + 3 * r + 1, v)] = (T)u.y;
+            K[kidx(d * 9 + 3 * r + 2, v)] = (T)w.x;
+        }
+    }
+}
+
 // Fine level straight from the elements (matrix-free mode: no block matrix
 // exists).  One thread per (node v, stored direction d): the 3x3 block
 // K(v, v + off[d]) = sum over elements holding both nodes of
@@ -592,6 +611,8 @@ void mg_setup(Ctx& c, MG<T>& mg) {
     if (c.matfree)
         k_mg_from_elements<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
             F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.bnd, F.K);
+    else if (c.use_lat64)
+        k_mg_extract_lat<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(F.n, c.lat64, F.K);
     else
         k_mg_extract<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(F.n, c.rowptr, c.cols,
                                                                            c.A64, F.K);

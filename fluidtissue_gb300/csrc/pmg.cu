@@ -88,6 +88,24 @@ __global__ void k_pmg_extract(int n, const int32_t* __restrict__ rowptr,
     }
 }
 
+// Fine level from the FP64 lattice half stencil: entry (3,3) of the 8 blocks.
+template <typename T>
+__global__ void k_pmg_extract_lat(int n, const double2* __restrict__ L,
+                                  const int32_t* __restrict__ p2t_ptr,
+                                  const uint32_t* __restrict__ p2t,
+                                  const ElemGeom* __restrict__ geom,
+                                  const double* __restrict__ mu, T* __restrict__ K) {
+    const int64_t N = (int64_t)n * n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * 8;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int d = (int)(t / N);
+        const int64_t v = t - d * N;
+        double val = -L[lat64_idx(d, 3, 1, v)].y;
+        if (d == 0) val += lumped_inv_mu(v, p2t_ptr, p2t, geom, mu);
+        K[d * N + v] = (T)val;
+    }
+}
+
 struct PRef {
     double mref[4][4];
 };
@@ -382,6 +400,9 @@ void pmg_setup(Ctx& c, PMG<T>& pm) {
             for (int b = 0; b < 4; ++b) pr.mref[a][b] = R.mref[a][b];
         k_pmg_from_elements<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
             F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.par.alpha, c.par.eps, pr, F.K);
+    } else if (c.use_lat64) {
+        k_pmg_extract_lat<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
+            F.n, c.lat64, c.p2t_ptr, c.p2t, c.geom, c.mu, F.K);
     } else {
         k_pmg_extract<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
             F.n, c.rowptr, c.cols, c.A64, c.p2t_ptr, c.p2t, c.geom, c.mu, F.K);

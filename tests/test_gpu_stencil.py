@@ -77,3 +77,25 @@ def test_stencil_refused_off_lattice():
     rc = f.init(Mesh(inst.xyz[perm], inv[tets]), inst.params, precision="mixed",
                 operator="stencil")
     assert rc == 6, rc
+
+
+@pytest.mark.parametrize("name,n", [("sphere65", 17), ("ellipsoid129", 24)])
+def test_lattice_fp64_residual_matches_bsr(name, n):
+    """Mixed precision on a lattice assembles only the FP64 / FP32 half
+    stencils; the outer residual it reports (from the FP64 half stencil) equals
+    ||b - A x|| / ||b|| recomputed on the host from the BSR the context then
+    assembles on request, for the returned solution."""
+    inst = workload(name, n)
+    par = dict(inst.params)
+    f, flow = _flow(inst, par, precision="mixed", operator="stencil")
+    rp, ci, vals, rhs = f.system()
+    npn = inst.np
+    x = flow.reshape(4, npn).T.copy()  # (ux, uy, uz, p) per node
+    rows = np.repeat(np.arange(npn), np.diff(rp))
+    ax = np.zeros((npn, 4))
+    np.add.at(ax, rows, np.einsum("brc,bc->br", vals, x[ci]))
+    rel = np.linalg.norm(rhs - ax) / np.linalg.norm(rhs)
+    st = f.last_stats
+    assert st["rel_residual"] <= par["Stokes tolerance"]
+    assert abs(rel - st["rel_residual"]) <= 1e-3 * st["rel_residual"] + 1e-14, (rel, st)
+    f.close()
