@@ -630,6 +630,72 @@ def run_dist(args):
     d.close()
 
 
+def run_st(args):
+    """Surface-tension load (Flow::surfaceTension_ with LevelSet's normals,
+    curvature and interface patches) on the ellipsoid129 mesh, phi = the
+    workload's level set, phi_reset = its distance reset computed once on the
+    GPU; "Surface tension" 1, "Node density" 1: value = loads/s through the C
+    ABI with host buffers (phi and phi_reset in, the 3 np load out)."""
+    import torch
+    from fluidtissue_gb300 import workloads as W
+    from fluidtissue_gb300.flow import Mesh
+    from fluidtissue_gb300.levelset import LevelSet
+
+    ws, rank, local = _dist()
+    dist = _setup_dist(ws, local)
+    torch.cuda.set_device(local)
+    inst = W.ellipsoid129()
+    ls = LevelSet()
+    if ls.init(Mesh(inst.xyz, inst.tets), device=local) != 0:
+        raise RuntimeError(ls.last_error())
+    # the reset values: one update with a zero velocity (advection is the identity)
+    flow = np.zeros(4 * inst.np)
+    flow[3 * inst.np:] = 1.0
+    phi = np.ascontiguousarray(inst.phi, np.float64).copy()
+    if ls.update(flow, phi, {"Advection dt": 1.0 / 32.0, "Advection tolerance": 1e-10,
+                             "Max. CG iterations": 0.0}) != 0:
+        raise RuntimeError(ls.last_error())
+    ifn = ls.reset_values()
+    par = {"Surface tension": 1.0, "Node density": 1.0}
+
+    def step():
+        ls.surface_tension(phi, par, phi_reset=ifn)
+        return ls.last_st_stats
+
+    for _ in range(args.warmup):
+        step()
+    _barrier(dist)
+    clk = Clocks(local)
+    t0 = time.perf_counter()
+    stats = [step() for _ in range(args.steps)]
+    wall = _max_over_ranks((time.perf_counter() - t0) * 1e3, dist)
+    st = stats[-1]
+    dev_ms = float(np.mean([s["ms_kernels"] for s in stats]))
+    line = {"metric": "surface-tension loads/s (ellipsoid129: normals, curvature, patches)",
+            "value": round(ws * 1e3 / dev_ms, 3), "unit": "loads/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(dev_ms, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 / f32",
+            "data": "synthetic (ellipsoid129 level set and its distance reset)",
+            "config": {"workload": f"st129: {inst.np} nodes, {inst.nt} tets"},
+            "e2e": {"value": round(ws * args.steps / (wall / 1e3), 3), "unit": "loads/s",
+                    "h2d_bytes_per_step": 2 * 8 * inst.np, "d2h_bytes_per_step": 3 * 8 * inst.np},
+            "interface_points": st["interface_points"], "area": st["area"],
+            "gpu_launches": int(st["kernel_launches"]), "clocks": clk.stop()}
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle as O
+        t0 = time.perf_counter()
+        O.surface_tension(inst.xyz, inst.tets, phi, ifn, 1.0, 1)
+        t_cpu = time.perf_counter() - t0
+        line["cpu_baseline"] = {
+            "value": 1.0 / t_cpu, "unit": "loads/s", "cores": O.num_threads(), "kind": "port",
+            "sample": f"oracle, the same load in full ({O.num_threads()} threads, {t_cpu:.2f} s)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ls.close()
+
+
 def run_ls(args):
     """Level-set update (LevelSet::update: Crank-Nicolson advection with
     Jacobi-BiCGSTAB, distance reset, mixing) on the ellipsoid129 mesh, advected
@@ -739,6 +805,8 @@ def main():
         run_dist(args)
     elif args.workload == "ls129":
         run_ls(args)
+    elif args.workload == "st129":
+        run_st(args)
     else:
         run_ours(args)
 

@@ -156,6 +156,20 @@ class FtsLsStats(C.Structure):
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
 
+
+class FtsStStats(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32),
+        ("interface_points", C.c_int64),
+        ("area", C.c_double),
+        ("ms_kernels", C.c_double),
+        ("ms_total", C.c_double),
+        ("kernel_launches", C.c_int64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
 PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_MINRES, SOLVER_BICGSTAB = 0, 1
 PC_AUTO, PC_JACOBI, PC_MULTIGRID, PC_MULTIGRID_DIAG = 0, 1, 2, 3
@@ -207,6 +221,9 @@ SIGNATURES = {
     "fts_ls_update": (C.c_int, [_vp, _P(FtsLsParams), _dp, _dp, _P(FtsLsStats)]),
     "fts_ls_destroy": (None, [_vp]),
     "fts_ls_last_error": (C.c_char_p, [_vp]),
+    "fts_ls_reset_values": (C.c_int, [_vp, _dp]),
+    "fts_ls_surface_tension": (C.c_int, [_vp, _dp, _dp, C.c_double, C.c_int32, _dp,
+                                         _P(FtsStStats)]),
 }
 
 NOALLOC_MAX_NODES = 1048576

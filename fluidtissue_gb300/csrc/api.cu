@@ -137,10 +137,6 @@ int validate_params(const fts_params& p, std::string& err) {
         err = "only the P1-P1 stabilised element (velocity degree 1) is on this path";
         return FTS_ERR_UNSUPPORTED;
     }
-    if (p.surface_tension > 0.0) {
-        err = "surface tension is not on this path";
-        return FTS_ERR_UNSUPPORTED;
-    }
     if (p.precision != FTS_PREC_FP64 && p.precision != FTS_PREC_MIXED) {
         err = "unknown precision";
         return FTS_ERR_BAD_INPUT;
@@ -328,6 +324,13 @@ static int solve_device(Ctx& c, bool have_mu, bool have_force, double* flow_out,
     const fts_params& P = c.par;
     const double flt_min = FLT_MIN;
     st.solved = 0;
+    if (P.surface_tension > 0.0 && !have_force) {
+        // the load needs the level set's interface (normals, curvature,
+        // patches): fts_ls_surface_tension computes it
+        c.last_error = "\"Surface tension\" > 0 needs its nodal load in `force` "
+                       "(fts_ls_surface_tension)";
+        return FTS_ERR_UNSUPPORTED;
+    }
     // Early exits of Flow::Stokes_ (Flow.cpp:223-228)
     if (P.mu_interior - P.mu_exterior > flt_min && P.rd_iterations > 0.0) {
         // max |source| <= FLT_MIN: nothing to solve

@@ -401,6 +401,8 @@ k_assemble_lat(int n, const int32_t* __restrict__ p2t_ptr, const uint32_t* __res
                const double* __restrict__ mu, const uint8_t* __restrict__ bnd, double alpha,
                double eps, RefArgs R, double2* __restrict__ L64, float4* __restrict__ L32) {
     const int64_t N = (int64_t)n * n * n;
+    // direction-major: a warp's threads share d, so they walk alike (the self
+    // block keeps all of a node's elements, the others about a quarter)
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * 8;
          t += (int64_t)gridDim.x * blockDim.x) {
         const int d = (int)(t / N);

@@ -420,6 +420,207 @@ __global__ void k_ls_check_velocity(int64_t n, const double* __restrict__ v,
     if (grid_sum<1>(acc, red, tot) && threadIdx.x == 0) *norm2 = tot[0];
 }
 
+// ---------------------------------------------------------------------------
+// Surface tension (Flow::surfaceTension_, src/growth/Flow.cpp:307-341) and
+// the LevelSet quantities it reads, from phi (current) and phi_reset (the last
+// full distance reset, LevelSet::phi_ifn_, LevelSet.cpp:440):
+//   normals = grad_nodes(phi_reset)                   LevelSet.cpp:453
+//   k = div(normals / |normals|) by grad_nodes of each normalised component,
+//       interpolated along the crossing edge          LevelSet.cpp:215-253
+//   interface points on sign-bit crossing edges       LevelSet.cpp:261-300
+//   patch areas: per mixed element, its crossing edges in the local order
+//       01 02 03 12 13 23 make one triangle (3) or two (4: e0 e2 e3, e0 e1 e3),
+//       0.5 |e1 x e2| added to each of the triangle's points, elements in
+//       index order                                    LevelSet.cpp:326-420
+//   grad / grad_nodes                                  Assembler.cpp:11-69
+// Edges are (i, j) with i < j; the force is symmetric in the orientation.
+// ---------------------------------------------------------------------------
+
+// Element gradient of the nodal field u (Assembler::grad): FP64, stored float.
+// comp >= 0: only component comp of the gradient of u_comp (u = [3][np] float
+// fields), for the divergence.
+__global__ void k_st_elem_grad(int64_t nt, const int32_t* __restrict__ tets,
+                               const LsGeom* __restrict__ geom, const double* __restrict__ u,
+                               float* __restrict__ out) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nt;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int4 tt = reinterpret_cast<const int4*>(tets)[k];
+        const LsGeom& G = geom[k];
+        const double u0 = u[tt.x], u1 = u[tt.y], u2 = u[tt.z], u3 = u[tt.w];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            out[3 * k + c] = (float)(__dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(u0, G.g[0][c]),
+                                                                  __dmul_rn(u1, G.g[1][c])),
+                                                        __dmul_rn(u2, G.g[2][c])),
+                                               __dmul_rn(u3, G.g[3][c])));
+    }
+}
+
+__global__ void k_st_elem_div(int64_t nt, const int32_t* __restrict__ tets,
+                              const LsGeom* __restrict__ geom, const float* __restrict__ gn,
+                              int64_t np, float* __restrict__ out) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nt;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int4 tt = reinterpret_cast<const int4*>(tets)[k];
+        const LsGeom& G = geom[k];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float* u = gn + c * np;
+            const double u0 = u[tt.x], u1 = u[tt.y], u2 = u[tt.z], u3 = u[tt.w];
+            out[3 * k + c] = (float)(__dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(u0, G.g[0][c]),
+                                                                  __dmul_rn(u1, G.g[1][c])),
+                                                        __dmul_rn(u2, G.g[2][c])),
+                                               __dmul_rn(u3, G.g[3][c])));
+        }
+    }
+}
+
+__device__ __forceinline__ float st_norm3(float x, float y, float z) {
+    return sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+}
+
+// Nodal average of element vectors (grad_nodes): float sums over the node's
+// elements in index order / (float) count.  mode 0: normals (and their
+// normalised components into gn[3][np]); mode 1: k = sum of the diagonal.
+__global__ void k_st_node_avg(int64_t np, const int32_t* __restrict__ p2t_ptr,
+                              const uint32_t* __restrict__ p2t, const float* __restrict__ ge,
+                              int mode, float* __restrict__ nrm, float* __restrict__ gn,
+                              float* __restrict__ kmesh) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        for (int32_t q = p2t_ptr[i]; q < p2t_ptr[i + 1]; ++q) {
+            const int64_t k = p2t[q] >> 2;
+            sx = __fadd_rn(sx, ge[3 * k]);
+            sy = __fadd_rn(sy, ge[3 * k + 1]);
+            sz = __fadd_rn(sz, ge[3 * k + 2]);
+        }
+        const float cnt = (float)(p2t_ptr[i + 1] - p2t_ptr[i]);
+        const float ax = __fdiv_rn(sx, cnt), ay = __fdiv_rn(sy, cnt), az = __fdiv_rn(sz, cnt);
+        if (mode == 0) {
+            nrm[3 * i] = ax;
+            nrm[3 * i + 1] = ay;
+            nrm[3 * i + 2] = az;
+            const float nn = st_norm3(ax, ay, az);
+            gn[i] = __fdiv_rn(ax, nn);
+            gn[np + i] = __fdiv_rn(ay, nn);
+            gn[2 * np + i] = __fdiv_rn(az, nn);
+        } else {
+            kmesh[i] = __fadd_rn(__fadd_rn(ax, ay), az);
+        }
+    }
+}
+
+__device__ __forceinline__ void st_point(const float* __restrict__ xyz, const double* __restrict__ phi,
+                                         int a, int b, float p[3]) {
+    double t = 0.5;
+    const double div = phi[a] - phi[b];
+    if (fabs(div) > (double)FLT_MIN) t = phi[a] / div;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        p[c] = (float)__dadd_rn(__dmul_rn(1.0 - t, (double)xyz[3 * (int64_t)a + c]),
+                                __dmul_rn(t, (double)xyz[3 * (int64_t)b + c]));
+}
+
+__constant__ int c_st_edge[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+
+// Patch area of each crossing edge (i, j), i < j: the edge's thread walks the
+// elements of i in index order, keeps those holding j, rebuilds their
+// triangles and adds those that contain the edge's point.  nif counts the
+// crossing edges, atot sums the areas (each triangle three times).
+__global__ void k_st_areas(int64_t np, const int32_t* __restrict__ rowptr,
+                           const int32_t* __restrict__ cols, const int32_t* __restrict__ p2t_ptr,
+                           const uint32_t* __restrict__ p2t, const int32_t* __restrict__ tets,
+                           const float* __restrict__ xyz, const double* __restrict__ phi,
+                           float* __restrict__ area, unsigned* __restrict__ nif,
+                           double* __restrict__ atot, int* __restrict__ bad) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const bool si = signbit(phi[i]);
+        for (int32_t q = rowptr[i]; q < rowptr[i + 1]; ++q) {
+            const int32_t j = cols[q];
+            if (j <= i || signbit(phi[j]) == si) continue;
+            float A = 0.f;
+            for (int32_t e = p2t_ptr[i]; e < p2t_ptr[i + 1]; ++e) {
+                const int64_t k = p2t[e] >> 2;
+                const int4 tt = reinterpret_cast<const int4*>(tets)[k];
+                const int ids[4] = {tt.x, tt.y, tt.z, tt.w};
+                if (ids[0] != j && ids[1] != j && ids[2] != j && ids[3] != j) continue;
+                float pts[4][3];
+                int mine = -1, ne = 0;
+                for (int m = 0; m < 6; ++m) {
+                    const int a = ids[c_st_edge[m][0]], b = ids[c_st_edge[m][1]];
+                    if (signbit(phi[a]) == signbit(phi[b])) continue;
+                    if (ne == 4) {
+                        atomicOr(bad, 1);
+                        break;
+                    }
+                    const int lo = min(a, b), hi = max(a, b);
+                    if (lo == i && hi == j) mine = ne;
+                    st_point(xyz, phi, lo, hi, pts[ne]);
+                    ++ne;
+                }
+                if (ne != 3 && ne != 4) {
+                    atomicOr(bad, 1);
+                    continue;
+                }
+                const int tri[2][3] = {{0, ne == 3 ? 1 : 2, ne == 3 ? 2 : 3}, {0, 1, 3}};
+                for (int tr = 0; tr < (ne == 3 ? 1 : 2); ++tr) {
+                    if (tri[tr][0] != mine && tri[tr][1] != mine && tri[tr][2] != mine) continue;
+                    const float* p0 = pts[tri[tr][0]];
+                    const float* p1 = pts[tri[tr][1]];
+                    const float* p2 = pts[tri[tr][2]];
+                    const float e1x = __fsub_rn(p1[0], p0[0]), e1y = __fsub_rn(p1[1], p0[1]),
+                                e1z = __fsub_rn(p1[2], p0[2]);
+                    const float e2x = __fsub_rn(p2[0], p0[0]), e2y = __fsub_rn(p2[1], p0[1]),
+                                e2z = __fsub_rn(p2[2], p0[2]);
+                    const float cx = __fsub_rn(__fmul_rn(e1y, e2z), __fmul_rn(e1z, e2y));
+                    const float cy = __fsub_rn(__fmul_rn(e1z, e2x), __fmul_rn(e1x, e2z));
+                    const float cz = __fsub_rn(__fmul_rn(e1x, e2y), __fmul_rn(e1y, e2x));
+                    A = (float)((double)A + 0.5 * (double)st_norm3(cx, cy, cz));
+                }
+            }
+            area[q] = A;
+            atomicAdd(nif, 1u);
+            atomicAdd(atot, (double)A);
+        }
+    }
+}
+
+// Nodal force of each crossing edge (Flow.cpp:326-339), added to both ends.
+__global__ void k_st_force(int64_t np, const int32_t* __restrict__ rowptr,
+                           const int32_t* __restrict__ cols, const double* __restrict__ phi,
+                           const float* __restrict__ area, const float* __restrict__ kmesh,
+                           const float* __restrict__ nrm, float st, int rho,
+                           double* __restrict__ force) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double pi = phi[i];
+        for (int32_t q = rowptr[i]; q < rowptr[i + 1]; ++q) {
+            const int32_t j = cols[q];
+            if (j <= i || signbit(phi[j]) == signbit(pi)) continue;
+            const float t = (float)(pi / (pi - phi[j]));
+            const float kif = (float)__dadd_rn(__dmul_rn(1.0 - (double)t, (double)kmesh[i]),
+                                               (double)__fmul_rn(t, kmesh[j]));
+            const double A = (double)area[q];
+            const int64_t ends[2] = {i, j};
+#pragma unroll
+            for (int m = 0; m < 2; ++m) {
+                const int64_t v = ends[m];
+                const float nx = nrm[3 * v], ny = nrm[3 * v + 1], nz = nrm[3 * v + 2];
+                const float nn = st_norm3(nx, ny, nz);
+                const double w = m == 0 ? 1.0 - (double)t : (double)t;
+                const float sc = (float)__dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(w, (double)st),
+                                                                      (double)(-kif)), A),
+                                                  (double)rho);
+                atomicAdd(force + v, (double)__fmul_rn(sc, __fdiv_rn(nx, nn)));
+                atomicAdd(force + np + v, (double)__fmul_rn(sc, __fdiv_rn(ny, nn)));
+                atomicAdd(force + 2 * np + v, (double)__fmul_rn(sc, __fdiv_rn(nz, nn)));
+            }
+        }
+    }
+}
+
 }  // namespace fts
 
 using namespace fts;
@@ -455,6 +656,17 @@ struct fts_ls {
     fts_dist* dist = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::string last_error;
+    bool have_reset = false;  // vec[11] holds the last update's full reset values
+    // surface tension (allocated by its first call)
+    double* st_phi = nullptr;    // [np] current phi
+    double* st_ifn = nullptr;    // [np] reset values given by the caller
+    float* st_ge = nullptr;      // [3 nt] element gradients
+    float* st_nrm = nullptr;     // [3 np] nodal normals (grad_nodes of phi_reset)
+    float* st_gn = nullptr;      // [3][np] normalised components
+    float* st_k = nullptr;       // [np] nodal curvature
+    float* st_area = nullptr;    // [nnz] patch area per crossing edge slot
+    double* st_force = nullptr;  // [3 np]
+    double* st_acc = nullptr;    // total area (x3)
 };
 
 namespace {
@@ -469,7 +681,8 @@ T* ls_alloc(size_t n) {
 void ls_free(fts_ls& S) {
     void* ptrs[] = {S.xyz, S.tets, S.rowptr, S.cols, S.p2t_ptr, S.p2t, S.geom, S.M, S.A, S.L,
                     S.flow, S.phi, S.keep, S.ifp, S.count, S.flag, S.norm2, S.S,
-                    S.red.partials, S.red.ticket};
+                    S.red.partials, S.red.ticket, S.st_phi, S.st_ifn, S.st_ge, S.st_nrm,
+                    S.st_gn, S.st_k, S.st_area, S.st_force, S.st_acc};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (double* p : S.vec)
@@ -709,6 +922,7 @@ int fts_ls_update(fts_ls* S, const fts_ls_params* P, const double* flow, double*
             dist_reset_device(S->dist, pts.data(), (int32_t)nif, ifn, FTS_DIST_PRUNED, s, nullptr);
             k_ls_mix<<<g, kLsThreads, 0, s>>>(np, x, ifn, S->keep, S->phi);
             launches += 2;
+            S->have_reset = true;
             st.interface_points = nif;
             FTS_CUDA(cudaMemcpyAsync(phi, S->phi, np * sizeof(double), cudaMemcpyDeviceToHost, s));
         }
@@ -728,6 +942,109 @@ int fts_ls_update(fts_ls* S, const fts_ls_params* P, const double* flow, double*
     } catch (const std::bad_alloc&) {
         S->last_error = "host allocation failed";
         rc = FTS_ERR_OOM;
+    }
+    st.status = rc;
+    st.ms_total = wall_ms() - t0;
+    if (stats) *stats = st;
+    return rc;
+}
+
+int fts_ls_reset_values(const fts_ls* S, double* phi_reset) {
+    if (!S || !phi_reset) return FTS_ERR_BAD_INPUT;
+    if (!S->have_reset) {
+        const_cast<fts_ls*>(S)->last_error = "no update with a distance reset has run yet";
+        return FTS_ERR_BAD_INPUT;
+    }
+    try {
+        FTS_CUDA(cudaSetDevice(S->device));
+        FTS_CUDA(cudaMemcpyAsync(phi_reset, S->vec[11], S->np * sizeof(double),
+                                 cudaMemcpyDeviceToHost, S->stream));
+        FTS_CUDA(cudaStreamSynchronize(S->stream));
+    } catch (const CudaError& e) {
+        const_cast<fts_ls*>(S)->last_error = e.what;
+        return FTS_ERR_CUDA;
+    }
+    return FTS_OK;
+}
+
+int fts_ls_surface_tension(fts_ls* S, const double* phi, const double* phi_reset,
+                           double surface_tension, int32_t node_density, double* force,
+                           fts_st_stats* stats) {
+    if (!S || !phi || !force) return FTS_ERR_BAD_INPUT;
+    const double t0 = wall_ms();
+    fts_st_stats st;
+    std::memset(&st, 0, sizeof(st));
+    int rc = FTS_OK;
+    try {
+        if (!phi_reset && !S->have_reset) {
+            S->last_error = "phi_reset is NULL and no update with a distance reset has run";
+            throw (int)FTS_ERR_BAD_INPUT;
+        }
+        FTS_CUDA(cudaSetDevice(S->device));
+        cudaStream_t s = S->stream;
+        const int64_t np = S->np, nt = S->nt;
+        if (!S->st_phi) {
+            S->st_phi = ls_alloc<double>(np);
+            S->st_ifn = ls_alloc<double>(np);
+            S->st_ge = ls_alloc<float>(3 * nt);
+            S->st_nrm = ls_alloc<float>(3 * np);
+            S->st_gn = ls_alloc<float>(3 * np);
+            S->st_k = ls_alloc<float>(np);
+            S->st_area = ls_alloc<float>(S->nnz);
+            S->st_force = ls_alloc<double>(3 * np);
+            S->st_acc = ls_alloc<double>(1);
+        }
+        FTS_CUDA(cudaMemcpyAsync(S->st_phi, phi, np * sizeof(double), cudaMemcpyHostToDevice, s));
+        const double* ifn = S->vec[11];
+        if (phi_reset) {
+            FTS_CUDA(cudaMemcpyAsync(S->st_ifn, phi_reset, np * sizeof(double),
+                                     cudaMemcpyHostToDevice, s));
+            ifn = S->st_ifn;
+        }
+        FTS_CUDA(cudaMemsetAsync(S->st_force, 0, 3 * np * sizeof(double), s));
+        FTS_CUDA(cudaMemsetAsync(S->st_acc, 0, sizeof(double), s));
+        FTS_CUDA(cudaMemsetAsync(S->count, 0, sizeof(unsigned), s));
+        FTS_CUDA(cudaMemsetAsync(S->flag, 0, sizeof(int), s));
+        const int ge = grid_of(*S, nt), gn = grid_of(*S, np);
+        FTS_CUDA(cudaEventRecord(S->ev[0], s));
+        k_st_elem_grad<<<ge, kLsThreads, 0, s>>>(nt, S->tets, S->geom, ifn, S->st_ge);
+        k_st_node_avg<<<gn, kLsThreads, 0, s>>>(np, S->p2t_ptr, S->p2t, S->st_ge, 0, S->st_nrm,
+                                                S->st_gn, S->st_k);
+        k_st_elem_div<<<ge, kLsThreads, 0, s>>>(nt, S->tets, S->geom, S->st_gn, np, S->st_ge);
+        k_st_node_avg<<<gn, kLsThreads, 0, s>>>(np, S->p2t_ptr, S->p2t, S->st_ge, 1, S->st_nrm,
+                                                S->st_gn, S->st_k);
+        k_st_areas<<<gn, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->p2t_ptr, S->p2t, S->tets,
+                                             S->xyz, S->st_phi, S->st_area, S->count, S->st_acc,
+                                             S->flag);
+        k_st_force<<<gn, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->st_phi, S->st_area,
+                                             S->st_k, S->st_nrm, (float)surface_tension,
+                                             (int)node_density, S->st_force);
+        FTS_CUDA(cudaGetLastError());
+        FTS_CUDA(cudaEventRecord(S->ev[1], s));
+        unsigned nif = 0;
+        int bad = 0;
+        double atot = 0.0;
+        FTS_CUDA(cudaMemcpyAsync(&nif, S->count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+        FTS_CUDA(cudaMemcpyAsync(&bad, S->flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+        FTS_CUDA(cudaMemcpyAsync(&atot, S->st_acc, sizeof(double), cudaMemcpyDeviceToHost, s));
+        FTS_CUDA(cudaMemcpyAsync(force, S->st_force, 3 * np * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s));
+        FTS_CUDA(cudaStreamSynchronize(s));
+        float ms = 0.f;
+        FTS_CUDA(cudaEventElapsedTime(&ms, S->ev[0], S->ev[1]));
+        st.ms_kernels = ms;
+        st.interface_points = nif;
+        st.area = atot / 3.0;
+        st.kernel_launches = 6;
+        if (bad) {
+            S->last_error = "an element crosses the interface on other than 3 or 4 edges";
+            rc = FTS_ERR_BAD_INPUT;
+        }
+    } catch (int code) {
+        rc = code;
+    } catch (const CudaError& e) {
+        S->last_error = e.what;
+        rc = e.code == cudaErrorMemoryAllocation ? FTS_ERR_OOM : FTS_ERR_CUDA;
     }
     st.status = rc;
     st.ms_total = wall_ms() - t0;

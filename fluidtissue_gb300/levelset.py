@@ -6,6 +6,7 @@ Jacobi-BiCGSTAB, then the distance reset and the 0.75 / 0.25 mixing.
     ls = LevelSet()
     ls.init(Mesh(xyz, tets))
     ls.update(flow, phi, par)     # phi (float64[np]) updated in place
+    f = ls.surface_tension(phi, par)   # Flow::surfaceTension_'s nodal load [3, np]
 """
 from __future__ import annotations
 
@@ -46,6 +47,7 @@ class LevelSet:
         rc = self._lib.fts_ls_create(C.byref(m), device, C.byref(self._ctx))
         if rc != 0:
             self._ctx = C.c_void_p()
+        self._n_nodes = m.np
         return rc
 
     def update(self, flow: np.ndarray, phi: np.ndarray, par: dict, reset: bool = True) -> int:
@@ -59,6 +61,39 @@ class LevelSet:
                                      N.ptr(phi, C.c_double), C.byref(st))
         self.last_stats = st.as_dict()
         return rc
+
+    def reset_values(self) -> np.ndarray:
+        """LevelSet::phi_ifn_ (LevelSet.cpp:440): the last update's full
+        distance-reset values, before the mixing."""
+        out = np.empty(self._np())
+        rc = self._lib.fts_ls_reset_values(self._ctx, N.ptr(out, C.c_double))
+        if rc != 0:
+            raise FtsError(rc, self.last_error())
+        return out
+
+    def surface_tension(self, phi: np.ndarray, par: dict,
+                        phi_reset: np.ndarray | None = None) -> np.ndarray:
+        """Flow::surfaceTension_ (Flow.cpp:307-341) with the LevelSet's
+        normals, curvature and interface patches: the nodal load [fx, fy, fz]
+        (shape [3, np]) that Flow.solve takes as `force` when "Surface tension"
+        > 0.  phi_reset None: the reset values of this context's last update."""
+        if not self._ctx:
+            raise FtsError(1, "LevelSet.init() has not succeeded")
+        phi = np.ascontiguousarray(phi, np.float64)
+        pr = None if phi_reset is None else np.ascontiguousarray(phi_reset, np.float64)
+        force = np.zeros(3 * phi.shape[0])
+        st = A.FtsStStats()
+        rc = self._lib.fts_ls_surface_tension(
+            self._ctx, N.ptr(phi, C.c_double), None if pr is None else N.ptr(pr, C.c_double),
+            float(_par(par, "Surface tension")), int(_par(par, "Node density")),
+            N.ptr(force, C.c_double), C.byref(st))
+        self.last_st_stats = st.as_dict()
+        if rc != 0:
+            raise FtsError(rc, self.last_error())
+        return force.reshape(3, -1)
+
+    def _np(self) -> int:
+        return self._n_nodes
 
     def last_error(self) -> str:
         return self._lib.fts_ls_last_error(self._ctx if self._ctx else None).decode()

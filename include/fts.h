@@ -36,7 +36,8 @@ typedef enum fts_status {
     FTS_ERR_NOT_CONVERGED = 3,      /* the solver stopped above the tolerance (Flow.cpp:281-285) */
     FTS_ERR_CUDA = 4,               /* a CUDA runtime call failed */
     FTS_ERR_OOM = 5,                /* device allocation failed */
-    FTS_ERR_UNSUPPORTED = 6,        /* a reference option outside this path (surface tension, P2) */
+    FTS_ERR_UNSUPPORTED = 6,        /* a reference option outside this path (P2; surface tension
+                                       without its load) */
     FTS_ERR_NAN = 7                 /* NaN or Inf in the inputs or in the iteration */
 } fts_status;
 
@@ -108,7 +109,8 @@ typedef struct fts_params {
     double rd_iterations;       /* "RD iterations" (selects maxGF and the early exit) */
     double gf_production;       /* "GF production" */
     double advection_dt;        /* "Advection dt" (< FLT_MIN: nothing to solve) */
-    double surface_tension;     /* "Surface tension": must be 0 on this path */
+    double surface_tension;     /* "Surface tension": > 0 needs the load from
+                                   fts_ls_surface_tension in fts_solve's force */
     /* GB300 options */
     int32_t precision;          /* FTS_PREC_* */
     int32_t solver;             /* FTS_SOLVER_* */
@@ -164,7 +166,9 @@ int fts_create(const fts_mesh* mesh, const fts_params* params, fts_ctx** out);
  *   mu[nt]     nullable: per-element viscosity; NULL = setViscosity's profile
  *              (ViscosityProfiles.hpp:27-72)
  *   force[3*np] nullable: nodal body force [fx(np), fy(np), fz(np)] (the
- *              surface-tension load slot of Flow.cpp:352-363)
+ *              surface-tension load slot of Flow.cpp:352-363, computed by
+ *              fts_ls_surface_tension); required when "Surface tension" > 0
+ *              (FTS_ERR_UNSUPPORTED without it)
  *   flow[4*np] output [ux, uy, uz, p]; left untouched by the early exits
  *   stats      nullable
  * The inputs are copied to the device, the system is assembled and solved on
@@ -403,6 +407,38 @@ int fts_ls_update(fts_ls* ls, const fts_ls_params* params, const double* flow, d
                   fts_ls_stats* stats);
 void fts_ls_destroy(fts_ls* ls);
 const char* fts_ls_last_error(const fts_ls* ls);
+
+/* The last update's full distance-reset values (LevelSet::phi_ifn_,
+ * LevelSet.cpp:440, before the 0.75 / 0.25 mixing), host [np].
+ * FTS_ERR_BAD_INPUT before any update with reset = 1. */
+int fts_ls_reset_values(const fts_ls* ls, double* phi_reset);
+
+/* ---------------------------------------------------------------------------
+ * Surface tension: Flow::surfaceTension_ (src/growth/Flow.cpp:307-341) with the
+ * LevelSet quantities it reads — normals = nodal gradient of phi_reset
+ * (LevelSet.cpp:453, Assembler.cpp:46-69), curvature div(n/|n|) at the nodes
+ * interpolated to the interface points (LevelSet.cpp:215-253), interface
+ * points and the area of their interface-triangle patches (LevelSet.cpp:261-300,
+ * :326-420).  The result is the nodal load `force` that fts_solve takes
+ * (Flow.cpp:356-363, 392-395: F += N fx ...): pass it there with "Surface
+ * tension" > 0.
+ * ------------------------------------------------------------------------- */
+typedef struct fts_st_stats {
+    int32_t status;
+    int64_t interface_points;  /* edges whose end values differ in sign bit */
+    double area;               /* total area of the interface triangles */
+    double ms_kernels;         /* device time */
+    double ms_total;           /* wall time of the call */
+    int64_t kernel_launches;
+} fts_st_stats;
+
+/* phi[np]: the current level set; phi_reset[np]: the last full reset values
+ * (NULL: this context's from its last fts_ls_update with reset = 1);
+ * surface_tension: "Surface tension"; node_density: "Node density" (the
+ * reference's integer rho); force[3 np] out = [fx(np), fy(np), fz(np)]. */
+int fts_ls_surface_tension(fts_ls* ls, const double* phi, const double* phi_reset,
+                           double surface_tension, int32_t node_density, double* force,
+                           fts_st_stats* stats);
 
 #ifdef __cplusplus
 }

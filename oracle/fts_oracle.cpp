@@ -33,6 +33,9 @@
 //  * distance reset of the level set (host path)       src/fem/EuclideanDistance.cu:16-38, :92-117
 //  * level-set update: Crank-Nicolson advection,        src/fem/LevelSet.cpp:89-151, :261-300,
 //    Jacobi-BiCGSTAB, distance reset and mixing          :429-455; Assembler.hpp:179-190
+//  * surface-tension load: element / nodal gradients     src/growth/Flow.cpp:307-341;
+//    (Assembler.cpp:11-69), curvature, interface points  src/fem/LevelSet.cpp:215-253,
+//    and interface-patch areas                           :261-300, :326-420, :453
 #include <algorithm>
 #include <cfloat>
 #include <chrono>
@@ -1146,6 +1149,178 @@ int ora_ls_update(int64_t np, int64_t nt, const float* xyz, const int32_t* tets,
         const double kept = keep[i] ? x[i] : ifn[i];
         phi[i] = 0.75 * kept + 0.25 * ifn[i];
     }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Surface tension (Flow::surfaceTension_, Flow.cpp:307-341) with the LevelSet
+// quantities it reads.  Inputs: phi (the current level set) and phi_reset (the
+// last full distance reset, LevelSet::phi_ifn_, LevelSet.cpp:440).
+//  * element gradient of a nodal field (Assembler::grad, Assembler.cpp:11-42):
+//    u0 g0 + u1 g1 + u2 g2 + u3 g3 in FP64, stored as float;
+//  * nodal gradient (grad_nodes, Assembler.cpp:46-69): float sum of the
+//    element gradients over the node's elements / (float) their count;
+//  * normals = grad_nodes(phi_reset) (LevelSet.cpp:453);
+//  * curvature k = div(grad_nodes(phi_reset) / |.|) by grad_nodes of each
+//    normalised component (LevelSet.cpp:215-238), interpolated along the
+//    crossing edge with t = phi0 / (phi0 - phi1) (:243-250);
+//  * interface points on the edges whose end values differ in sign bit, at
+//    t (0.5 when |phi0 - phi1| <= FLT_MIN), as float (LevelSet.cpp:261-300);
+//  * patches: per element with mixed signs, its crossing edges in the local
+//    order 01 02 03 12 13 23 give one triangle (3 crossings: e0 e1 e2) or two
+//    (4 crossings: e0 e2 e3 and e0 e1 e3); each triangle adds 0.5 |e1 x e2|
+//    (float cross product) to each of its three points, elements in index
+//    order (LevelSet.cpp:326-420);
+//  * force: f = (1 - t) st (-k) area rho n0/|n0| to e0 and t st (-k) area rho
+//    n1/|n1| to e1, the scalar converted to float before it scales the float
+//    normal (Flow.cpp:326-339).
+// Edges are taken as (i, j) with i < j (the force is symmetric in the edge's
+// orientation).  Returns 0; n_ifp = crossing edges, area = sum of the
+// triangle areas (each triangle once).
+// ---------------------------------------------------------------------------
+namespace {
+
+void elem_grad(int64_t nt, const float* xyz, const int32_t* tets, const double* u,
+               std::vector<float>& g) {
+    g.assign(3 * (size_t)nt, 0.f);
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < nt; ++k) {
+        const int32_t* t = tets + 4 * k;
+        Geom G;
+        if (!element_geom(xyz, t, G)) continue;
+        for (int c = 0; c < 3; ++c)
+            g[3 * k + c] = (float)(((u[t[0]] * G.g[0][c] + u[t[1]] * G.g[1][c]) +
+                                    u[t[2]] * G.g[2][c]) + u[t[3]] * G.g[3][c]);
+    }
+}
+
+void node_avg(const Topology& T, const std::vector<float>& ge, std::vector<float>& gn) {
+    gn.assign(3 * (size_t)T.np, 0.f);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < T.np; ++i) {
+        float s[3] = {0.f, 0.f, 0.f};
+        for (int64_t q = T.p2t_ptr[i]; q < T.p2t_ptr[i + 1]; ++q)
+            for (int c = 0; c < 3; ++c) s[c] += ge[3 * (size_t)T.p2t[q] + c];
+        const float cnt = (float)(T.p2t_ptr[i + 1] - T.p2t_ptr[i]);
+        for (int c = 0; c < 3; ++c) gn[3 * i + c] = s[c] / cnt;
+    }
+}
+
+inline float norm3f(const float* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+
+inline void edge_point(const float* xyz, const double* phi, int32_t a, int32_t b, float out[3]) {
+    double t = 0.5;
+    const double div = phi[a] - phi[b];
+    if (std::fabs(div) > FLT_MIN) t = phi[a] / div;
+    for (int c = 0; c < 3; ++c)
+        out[c] = (float)((1.0 - t) * (double)xyz[3 * (int64_t)a + c] +
+                         t * (double)xyz[3 * (int64_t)b + c]);
+}
+
+const int kLocalEdge[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+
+}  // namespace
+
+int ora_surface_tension(int64_t np, int64_t nt, const float* xyz, const int32_t* tets,
+                        const double* phi, const double* phi_reset, double st, int32_t rho,
+                        double* force, int64_t* n_ifp, double* area_total) {
+    Topology T;
+    build_topology(np, nt, tets, T);
+    std::vector<float> ge, normals, gn;
+    elem_grad(nt, xyz, tets, phi_reset, ge);
+    node_avg(T, ge, normals);
+    // normalised nodal gradient components, then the divergence
+    std::vector<double> comp[3];
+    for (int c = 0; c < 3; ++c) comp[c].assign(np, 0.0);
+    for (int64_t i = 0; i < np; ++i) {
+        const float nn = norm3f(&normals[3 * i]);
+        for (int c = 0; c < 3; ++c) comp[c][i] = (double)(normals[3 * i + c] / nn);
+    }
+    std::vector<float> kmesh(np, 0.f), dsum[3];
+    for (int c = 0; c < 3; ++c) {
+        std::vector<float> e;
+        elem_grad(nt, xyz, tets, comp[c].data(), e);
+        node_avg(T, e, dsum[c]);
+    }
+    for (int64_t i = 0; i < np; ++i)
+        kmesh[i] = dsum[0][3 * i + 0] + dsum[1][3 * i + 1] + dsum[2][3 * i + 2];
+    // crossing edges (i < j) and their slots
+    std::vector<int64_t> slot_of;  // per CSR slot: interface point index or -1
+    slot_of.assign(T.nb_ptr[np], -1);
+    int64_t nif = 0;
+    for (int64_t i = 0; i < np; ++i)
+        for (int64_t q = T.nb_ptr[i]; q < T.nb_ptr[i + 1]; ++q) {
+            const int32_t j = T.nb[q];
+            if (j <= i || std::signbit(phi[i]) == std::signbit(phi[j])) continue;
+            slot_of[q] = nif++;
+        }
+    auto point_of = [&](int32_t a, int32_t b) -> int64_t {
+        if (a > b) std::swap(a, b);
+        const int32_t* cols = T.nb.data() + T.nb_ptr[a];
+        const int n = (int)(T.nb_ptr[a + 1] - T.nb_ptr[a]);
+        return slot_of[T.nb_ptr[a] + find_col(cols, n, b)];
+    };
+    // patch areas, elements in index order
+    std::vector<float> area(nif, 0.f);
+    double atot = 0.0;
+    for (int64_t k = 0; k < nt; ++k) {
+        const int32_t* t = tets + 4 * k;
+        int s = 0;
+        for (int m = 0; m < 4; ++m) s += std::signbit(phi[t[m]]) ? 1 : 0;
+        if (s == 0 || s == 4) continue;
+        int64_t eif[4];
+        float pts[4][3];
+        int ne = 0;
+        for (int e = 0; e < 6; ++e) {
+            const int32_t a = t[kLocalEdge[e][0]], b = t[kLocalEdge[e][1]];
+            if (std::signbit(phi[a]) == std::signbit(phi[b])) continue;
+            if (ne == 4) return 1;
+            eif[ne] = point_of(a, b);
+            edge_point(xyz, phi, std::min(a, b), std::max(a, b), pts[ne]);
+            ++ne;
+        }
+        if (ne != 3 && ne != 4) return 1;
+        const int tri[2][3] = {{0, ne == 3 ? 1 : 2, ne == 3 ? 2 : 3}, {0, 1, 3}};
+        for (int tr = 0; tr < (ne == 3 ? 1 : 2); ++tr) {
+            const float* p0 = pts[tri[tr][0]];
+            const float* p1 = pts[tri[tr][1]];
+            const float* p2 = pts[tri[tr][2]];
+            float e1[3], e2[3];
+            for (int c = 0; c < 3; ++c) {
+                e1[c] = p1[c] - p0[c];
+                e2[c] = p2[c] - p0[c];
+            }
+            const float cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                                 e1[0] * e2[1] - e1[1] * e2[0]};
+            const double ha = 0.5 * (double)norm3f(cr);
+            atot += ha;
+            for (int m = 0; m < 3; ++m) {
+                float& A = area[eif[tri[tr][m]]];
+                A = (float)((double)A + ha);
+            }
+        }
+    }
+    // forces
+    std::fill(force, force + 3 * np, 0.0);
+    const float stf = (float)st;
+    for (int64_t i = 0; i < np; ++i)
+        for (int64_t q = T.nb_ptr[i]; q < T.nb_ptr[i + 1]; ++q) {
+            if (slot_of[q] < 0) continue;
+            const int32_t e0 = (int32_t)i, e1 = T.nb[q];
+            const float t = (float)(phi[e0] / (phi[e0] - phi[e1]));
+            const float kif = (float)((1.0 - (double)t) * (double)kmesh[e0] + (double)(t * kmesh[e1]));
+            const float A = area[slot_of[q]];
+            const int32_t ends[2] = {e0, e1};
+            for (int m = 0; m < 2; ++m) {
+                const float* nv = &normals[3 * (size_t)ends[m]];
+                const float nn = norm3f(nv);
+                const double w = m == 0 ? (1.0 - (double)t) : (double)t;
+                const float sc = (float)(w * (double)stf * (double)(-kif) * (double)A * (double)rho);
+                for (int c = 0; c < 3; ++c) force[c * np + ends[m]] += (double)(sc * (nv[c] / nn));
+            }
+        }
+    if (n_ifp) *n_ifp = nif;
+    if (area_total) *area_total = atot;
     return 0;
 }
 

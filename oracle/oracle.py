@@ -73,6 +73,8 @@ def lib():
         "ora_dist_reset": (C.c_int, [i64, _p(f32), _p(f32), i32, i64, i64, _p(dbl)]),
         "ora_ls_update": (C.c_int, [i64, i64, _p(f32), _p(i32), _p(dbl), _p(dbl), dbl, dbl, i64,
                                     C.c_int, _p(i64), _p(dbl), _p(i64)]),
+        "ora_surface_tension": (C.c_int, [i64, i64, _p(f32), _p(i32), _p(dbl), _p(dbl), dbl,
+                                          i32, _p(dbl), _p(i64), _p(dbl)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -395,7 +397,25 @@ def ls_update(xyz, tets, flow, phi, dt, tol=1e-6, maxit=0, reset=True):
     return st, it.value, err.value, nif.value
 
 
+def surface_tension(xyz, tets, phi, phi_reset, st, rho):
+    """Flow::surfaceTension_ with its LevelSet inputs restated: returns
+    (force[3, np] as [fx, fy, fz], interface points, total patch area)."""
+    xyz = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+    tets = np.ascontiguousarray(tets, np.int32)
+    phi = np.ascontiguousarray(phi, np.float64)
+    phi_reset = np.ascontiguousarray(phi_reset, np.float64)
+    npn = xyz.shape[0]
+    force = np.zeros(3 * npn)
+    nif, area = C.c_int64(), C.c_double()
+    st_ = lib().ora_surface_tension(npn, tets.shape[0], _ptr(xyz, F32), _ptr(tets, I32),
+                                    _ptr(phi, D), _ptr(phi_reset, D), float(st), int(rho),
+                                    _ptr(force, D), C.byref(nif), C.byref(area))
+    assert st_ == 0, "element with a crossing count other than 3 or 4"
+    return force.reshape(3, npn), nif.value, area.value
+
+
 __all__ = ["build", "lib", "ref_tables", "boundary_nodes", "set_viscosity", "source",
            "assemble_blocks", "reduce", "spmv", "bicgstab", "true_residual", "scatter",
            "system", "direct_solve", "solve_tight", "flow_solve", "rd_solve", "RD_KEYS",
+           "surface_tension",
            "dist_reset", "ls_update"]

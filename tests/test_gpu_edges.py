@@ -94,11 +94,18 @@ def test_iteration_cap_reports_not_converged():
     f.close()
 
 
-def test_surface_tension_refused():
+def test_surface_tension_without_its_load_refused():
+    """"Surface tension" > 0 needs the nodal load that fts_ls_surface_tension
+    computes from the level set; without it the solve is refused and flow
+    stays untouched."""
     inst = workload("sphere17", 9)
     par = dict(inst.params, **{"Surface tension": 1.0})
-    _, rc = _flow(inst, par)
-    assert rc == UNSUPPORTED
+    f, rc = _flow(inst, par)
+    assert rc == OK
+    flow = np.full(4 * inst.np, 3.0)
+    assert f.solve(inst.phi, inst.source, flow, mu=inst.mu) == UNSUPPORTED
+    assert np.all(flow == 3.0)
+    f.close()
 
 
 def test_warm_start_converges_immediately_on_the_same_input():

@@ -350,3 +350,46 @@ def test_levelset_reset_is_distance_away_from_crossings():
     O.dist_reset(inst.xyz, pts, d)
     far = ~crossing
     assert np.allclose(phi[far], d[far], rtol=1e-6, atol=1e-7)
+
+
+def _sphere_lattice(n, r=0.25):
+    from fluidtissue_gb300 import workloads as W
+    xyz, tets, _ = W.kuhn_mesh(n, 0.0, 1)
+    c = np.array([0.5, 0.5, 0.5])
+    d = np.linalg.norm(xyz.astype(np.float64) - c, axis=1)
+    return xyz, tets, d - r, (xyz.astype(np.float64) - c) / np.maximum(d, 1e-12)[:, None]
+
+
+def test_surface_tension_sphere_known_answers():
+    """phi = phi_reset = exact distance to a sphere of radius r: the patches
+    tile the sphere (total area -> 4 pi r^2), the curvature is 2/r, so the
+    inward load sums to st rho (2/r) 3 (4 pi r^2) = 24 pi r st rho (each
+    triangle's area goes to its 3 points); the net force vanishes by symmetry;
+    the load is linear in st * rho."""
+    r = 0.25
+    xyz, tets, phi, radial = _sphere_lattice(33, r)
+    f, nif, area = O.surface_tension(xyz, tets, phi, phi, 1.0, 1)
+    assert nif > 1000
+    assert abs(area - 4 * np.pi * r * r) <= 0.01 * 4 * np.pi * r * r
+    fr = np.sum(f.T * radial)
+    assert abs(fr + 24 * np.pi * r) <= 0.01 * 24 * np.pi * r, fr
+    assert np.abs(f.sum(axis=1)).max() <= 1e-6 * np.abs(f).sum()
+    f6, _, _ = O.surface_tension(xyz, tets, phi, phi, 2.0, 3)
+    assert np.allclose(f6, 6.0 * f, rtol=1e-6, atol=1e-9 * np.abs(f).max())
+
+
+@pytest.mark.parametrize("signs,count,area", [
+    ((-1.0, 1.0, 1.0, 1.0), 3, 0.5 * np.sqrt(3.0) / 4.0),     # one triangle
+    ((-1.0, -1.0, 1.0, 1.0), 4, 0.5 * np.sqrt(0.5)),          # a quad as two triangles
+])
+def test_surface_tension_patches_by_hand(signs, count, area):
+    """One unit right tetrahedron: the crossing edges' midpoints (|phi| equal)
+    form one triangle (one node inside) or a 0.5 x sqrt(0.5) rectangle split
+    in two (two inside); a linear phi has zero curvature, so no load."""
+    xyz = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float32)
+    tets = np.array([[0, 1, 2, 3]], np.int32)
+    phi = np.array(signs)
+    f, nif, a = O.surface_tension(xyz, tets, phi, phi, 1.0, 1)
+    assert nif == count
+    assert abs(a - area) <= 1e-6
+    assert np.all(f == 0.0)
