@@ -17,7 +17,7 @@ namespace fts {
 void free_all(Ctx& c) {
     void* ptrs[] = {c.xyz, c.tets, c.bnd, c.rowptr, c.cols, c.diag, c.p2t_ptr, c.p2t, c.geom,
                     c.phi, c.src, c.force, c.mu, c.s, c.flow, c.A64, c.A32, c.ell_val,
-                    c.ell_col, c.ell_ptr, c.lat_val, c.lat_src, c.lat64, c.pc64, c.pc32,
+                    c.ell_col, c.ell_ptr, c.lat_val, c.lat_src, c.lat64, c.pc64, c.pc32, c.dofs, c.xp2t_ptr, c.xp2t,
                     c.b, c.x, c.r, c.w64.q, c.w64.R[0], c.w64.R[1], c.w64.Y[0], c.w64.Y[1],
                     c.w64.W[0], c.w64.W[1], c.w64.X, c.w32.q, c.w32.R[0], c.w32.R[1],
                     c.w32.Y[0], c.w32.Y[1], c.w32.W[0], c.w32.W[1], c.w32.X, c.w32.r0, c.ms,
@@ -133,8 +133,18 @@ void ensure_fp32(Ctx& c) {
 }
 
 int validate_params(const fts_params& p, std::string& err) {
-    if (p.velocity_degree != 1) {
-        err = "only the P1-P1 stabilised element (velocity degree 1) is on this path";
+    if (p.velocity_degree != 1 && p.velocity_degree != 2) {
+        err = "velocity degree must be 1 (P1-P1 stabilised) or 2 (P2-P1)";
+        return FTS_ERR_UNSUPPORTED;
+    }
+    if (p.velocity_degree == 2 &&
+        (p.operator_kind == FTS_OP_MATFREE || p.operator_kind == FTS_OP_STENCIL)) {
+        err = "P2-P1 runs on the assembled operator (FTS_OP_AUTO or FTS_OP_ASSEMBLED)";
+        return FTS_ERR_UNSUPPORTED;
+    }
+    if (p.velocity_degree == 2 && p.preconditioner != FTS_PC_AUTO &&
+        p.preconditioner != FTS_PC_JACOBI) {
+        err = "P2-P1 uses the block-Jacobi preconditioner (FTS_PC_AUTO or FTS_PC_JACOBI)";
         return FTS_ERR_UNSUPPORTED;
     }
     if (p.precision != FTS_PREC_FP64 && p.precision != FTS_PREC_MIXED) {
@@ -223,9 +233,11 @@ void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
     for (auto& e : c.ev) FTS_CUDA(cudaEventCreate(&e));
     const HostTopology& T = c.topo;
     c.np = T.np;
+    c.nv = T.nv;
+    c.p2 = p.velocity_degree == 2;
     c.nt = T.nt;
     c.nnzb = T.rowptr[T.np];
-    c.xyz = dev_alloc<float>(c, 3 * c.np);
+    c.xyz = dev_alloc<float>(c, 3 * c.nv);
     c.tets = dev_alloc<int32_t>(c, 4 * c.nt);
     c.bnd = dev_alloc<uint8_t>(c, c.np);
     c.rowptr = dev_alloc<int32_t>(c, c.np + 1);
@@ -234,10 +246,10 @@ void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
     c.p2t_ptr = dev_alloc<int32_t>(c, c.np + 1);
     c.p2t = dev_alloc<uint32_t>(c, 4 * c.nt);
     c.geom = dev_alloc<ElemGeom>(c, c.nt);
-    c.phi = dev_alloc<double>(c, c.np);
-    c.src = dev_alloc<double>(c, c.np);
+    c.phi = dev_alloc<double>(c, c.nv);
+    c.src = dev_alloc<double>(c, c.nv);
     c.mu = dev_alloc<double>(c, c.nt);
-    c.s = dev_alloc<double>(c, c.np);
+    c.s = dev_alloc<double>(c, c.nv);
     c.flow = dev_alloc<double>(c, 4 * c.np);
     c.matfree = p.operator_kind == FTS_OP_MATFREE;
     // Single solves allocate the FP64 BSR at its first assembly
@@ -260,7 +272,7 @@ void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
     FTS_CUDA(cudaMemsetAsync(c.red.ticket, 0, sizeof(unsigned), c.stream));
     FTS_CUDA(cudaMemsetAsync(c.err_flag, 0, sizeof(int), c.stream));
     FTS_CUDA(cudaMemsetAsync(c.x, 0, c.np * sizeof(V4<double>), c.stream));
-    FTS_CUDA(cudaMemcpyAsync(c.xyz, m.xyz, 3 * c.np * sizeof(float), cudaMemcpyHostToDevice,
+    FTS_CUDA(cudaMemcpyAsync(c.xyz, m.xyz, 3 * c.nv * sizeof(float), cudaMemcpyHostToDevice,
                              c.stream));
     FTS_CUDA(cudaMemcpyAsync(c.tets, m.tets, 4 * c.nt * sizeof(int32_t), cudaMemcpyHostToDevice,
                              c.stream));
@@ -275,6 +287,17 @@ void create(Ctx& c, const fts_mesh& m, const fts_params& p) {
                              cudaMemcpyHostToDevice, c.stream));
     FTS_CUDA(cudaMemcpyAsync(c.p2t, T.p2t.data(), 4 * c.nt * sizeof(uint32_t),
                              cudaMemcpyHostToDevice, c.stream));
+    if (c.p2) {
+        c.dofs = dev_alloc<int32_t>(c, 10 * c.nt);
+        c.xp2t_ptr = dev_alloc<int32_t>(c, c.np + 1);
+        c.xp2t = dev_alloc<uint32_t>(c, 10 * c.nt);
+        FTS_CUDA(cudaMemcpyAsync(c.dofs, T.dofs.data(), 10 * c.nt * sizeof(int32_t),
+                                 cudaMemcpyHostToDevice, c.stream));
+        FTS_CUDA(cudaMemcpyAsync(c.xp2t_ptr, T.xp2t_ptr.data(), (c.np + 1) * sizeof(int32_t),
+                                 cudaMemcpyHostToDevice, c.stream));
+        FTS_CUDA(cudaMemcpyAsync(c.xp2t, T.xp2t.data(), 10 * c.nt * sizeof(uint32_t),
+                                 cudaMemcpyHostToDevice, c.stream));
+    }
     // total volume (for the rank-one constant-pressure term of the preconditioner)
     double vol = 0.0;
 #pragma omp parallel for reduction(+ : vol) schedule(static)
@@ -335,7 +358,7 @@ static int solve_device(Ctx& c, bool have_mu, bool have_force, double* flow_out,
     if (P.mu_interior - P.mu_exterior > flt_min && P.rd_iterations > 0.0) {
         // max |source| <= FLT_MIN: nothing to solve
         FTS_CUDA(cudaMemsetAsync(c.err_flag, 0, sizeof(int), c.stream));
-        launch_any_abs_above(c, c.src, c.np, flt_min);
+        launch_any_abs_above(c, c.src, c.nv, flt_min);
         int any = 0;
         FTS_CUDA(cudaMemcpyAsync(&any, c.err_flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         FTS_CUDA(cudaStreamSynchronize(c.stream));
@@ -344,15 +367,16 @@ static int solve_device(Ctx& c, bool have_mu, bool have_force, double* flow_out,
     if (P.advection_dt < flt_min) return FTS_OK;
 
     FTS_CUDA(cudaMemsetAsync(c.err_flag, 0, sizeof(int), c.stream));
-    launch_check_finite(c, c.phi, c.np);
-    launch_check_finite(c, c.src, c.np);
+    launch_check_finite(c, c.phi, c.nv);
+    launch_check_finite(c, c.src, c.nv);
     if (have_mu) launch_check_finite(c, c.mu, c.nt);
-    if (have_force) launch_check_finite(c, c.force, 3 * c.np);
+    if (have_force) launch_check_finite(c, c.force, 3 * c.nv);
     FTS_CUDA(cudaEventRecord(c.ev[0], c.stream));
     if (!have_mu) launch_viscosity_profile(c);
     launch_mu_minmax(c);
     launch_source(c);
-    launch_rhs(c, have_force);
+    if (c.p2) launch_rhs_p2(c, have_force);
+    else launch_rhs(c, have_force);
     // the zero-load exit (Flow.cpp:248-251) needs ||F||: computed with the
     // residual kernel on x = 0 below when the matrix exists; here directly.
     if (c.matfree) {
@@ -360,6 +384,13 @@ static int solve_device(Ctx& c, bool have_mu, bool have_force, double* flow_out,
         // straight from the elements
         launch_mf_pc(c);
         setup_preconditioner<float>(c);
+    } else if (c.p2) {
+        launch_assemble_p2(c);
+        launch_preconditioner(c);
+        if (P.precision == FTS_PREC_MIXED) {
+            ensure_fp32(c);
+            launch_to_f32(c);
+        }
     } else if (c.use_lat64) {
         // Kuhn lattice, mixed precision: FP64 and FP32 half stencils straight
         // from the elements (no BSR)
@@ -401,7 +432,7 @@ static int solve_device(Ctx& c, bool have_mu, bool have_force, double* flow_out,
     if (P.verbose)
         std::printf("  Viscosity min: %g, max: %g\n", st.mu_min, st.mu_max);
     const double tol = P.tol > 0.0 ? P.tol : DBL_EPSILON;
-    const long long N = 3 * c.topo.n_interior + c.np;
+    const long long N = 3 * c.topo.n_interior + c.nv;
     const long long maxit = P.max_iter > 0 ? P.max_iter : 2 * N;
     FTS_CUDA(cudaEventRecord(c.ev[2], c.stream));
     if (P.solver == FTS_SOLVER_BICGSTAB) {
@@ -587,6 +618,19 @@ int create_context(const fts_mesh* mesh, const fts_params* params, fts_ctx** out
             delete h;
             return rc;
         }
+        if (p.velocity_degree == 2) {
+            if (in_batch) {
+                g_create_error = "batched solves are P1-P1 only";
+                delete h;
+                return FTS_ERR_UNSUPPORTED;
+            }
+            rc = extend_p2(*mesh, h->c.topo, err);
+            if (rc != FTS_OK) {
+                g_create_error = err;
+                delete h;
+                return rc;
+            }
+        }
         h->c.in_batch = in_batch;
         create(h->c, *mesh, p);
     } catch (const CudaError& e) {
@@ -627,18 +671,18 @@ static int solve_common(fts_ctx* ctx, const double* phi, const double* source, c
     try {
         FTS_CUDA(cudaSetDevice(c.device));
         const cudaMemcpyKind k = device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-        FTS_CUDA(cudaMemcpyAsync(c.phi, phi, c.np * sizeof(double), k, c.stream));
-        FTS_CUDA(cudaMemcpyAsync(c.src, source, c.np * sizeof(double), k, c.stream));
+        FTS_CUDA(cudaMemcpyAsync(c.phi, phi, c.nv * sizeof(double), k, c.stream));
+        FTS_CUDA(cudaMemcpyAsync(c.src, source, c.nv * sizeof(double), k, c.stream));
         if (mu) FTS_CUDA(cudaMemcpyAsync(c.mu, mu, c.nt * sizeof(double), k, c.stream));
         if (force) {
-            if (!c.force) c.force = dev_alloc<double>(c, 3 * c.np);
-            FTS_CUDA(cudaMemcpyAsync(c.force, force, 3 * c.np * sizeof(double), k, c.stream));
+            if (!c.force) c.force = dev_alloc<double>(c, 3 * c.nv);
+            FTS_CUDA(cudaMemcpyAsync(c.force, force, 3 * c.nv * sizeof(double), k, c.stream));
         }
         if (c.par.precision == FTS_PREC_FP64) ensure_fp64_work(c);
         double* out = device ? flow : c.flow;
         rc = solve_device(c, mu != nullptr, force != nullptr, out, st);
         if (rc == FTS_OK && st.solved && !device) {
-            FTS_CUDA(cudaMemcpyAsync(flow, c.flow, 4 * c.np * sizeof(double),
+            FTS_CUDA(cudaMemcpyAsync(flow, c.flow, 4 * c.nv * sizeof(double),
                                      cudaMemcpyDeviceToHost, c.stream));
         }
         FTS_CUDA(cudaStreamSynchronize(c.stream));
@@ -705,6 +749,10 @@ int fts_update_params(fts_ctx* ctx, const fts_params* params) {
         ctx->c.last_error = "the device of a context cannot change";
         return FTS_ERR_BAD_INPUT;
     }
+    if (params->velocity_degree != ctx->c.par.velocity_degree) {
+        ctx->c.last_error = "the velocity degree of a context cannot change";
+        return FTS_ERR_BAD_INPUT;
+    }
     const fts_params old = ctx->c.par;
     ctx->c.par = *params;
     try {
@@ -742,7 +790,7 @@ int fts_get_sizes(const fts_ctx* ctx, int64_t* np, int64_t* nnzb, int64_t* n_red
     if (!ctx) return FTS_ERR_BAD_INPUT;
     if (np) *np = ctx->c.np;
     if (nnzb) *nnzb = ctx->c.nnzb;
-    if (n_reduced) *n_reduced = 3 * ctx->c.topo.n_interior + ctx->c.np;
+    if (n_reduced) *n_reduced = 3 * ctx->c.topo.n_interior + ctx->c.nv;
     return FTS_OK;
 }
 

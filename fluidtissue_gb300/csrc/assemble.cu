@@ -213,7 +213,7 @@ __global__ void k_source(int64_t np, const double* __restrict__ phi, const doubl
 
 void launch_source(Ctx& c) {
     const fts_params& P = c.par;
-    k_source<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(c.np, c.phi, c.src, P.gf_growth,
+    k_source<<<grid_for(c, c.nv), kThreads, 0, c.stream>>>(c.nv, c.phi, c.src, P.gf_growth,
                                                            P.level_sink, P.growth_threshold,
                                                            c.s, c.red, c.os);
     FTS_CUDA(cudaGetLastError());
@@ -539,7 +539,9 @@ __global__ void k_preconditioner(int64_t np, Diag dg, const int32_t* __restrict_
             int64_t k = p2t[q] >> 2;
             w += geom[k].vol / (4.0 * mu[k]);
         }
-        o[6] = 1.0 / (-D[15] + w);
+        // a node without pressure (P2 edge node: zero pressure row) gets weight 0
+        const double dp = -D[15] + w;
+        o[6] = dp != 0.0 ? 1.0 / dp : 0.0;
         o[7] = 0.0;
 #pragma unroll
         for (int u = 0; u < 8; ++u) pc[8 * i + u] = o[u];
@@ -661,7 +663,8 @@ __global__ void k_scatter_flow(int64_t np, const V4<double>* __restrict__ x,
 }
 
 void launch_scatter_flow(Ctx& c, double* flow_out) {
-    k_scatter_flow<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(c.np, c.x, c.bnd, flow_out);
+    // the vertices are the first nv system nodes (P2: the edges follow)
+    k_scatter_flow<<<grid_for(c, c.nv), kThreads, 0, c.stream>>>(c.nv, c.x, c.bnd, flow_out);
     FTS_CUDA(cudaGetLastError());
     c.launches += 1;
 }

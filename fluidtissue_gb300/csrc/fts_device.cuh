@@ -113,7 +113,12 @@ struct Ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     HostTopology topo;
-    int64_t np = 0, nt = 0, nnzb = 0;
+    int64_t np = 0, nt = 0, nnzb = 0;  // np: system nodes (block rows)
+    int64_t nv = 0;                    // mesh vertices (== np for P1-P1)
+    bool p2 = false;                   // P2-P1: edges are system nodes too
+    int32_t* dofs = nullptr;           // P2: [10 nt] element DOFs
+    int32_t* xp2t_ptr = nullptr;       // P2: system node -> (element, local DOF)
+    uint32_t* xp2t = nullptr;
     int num_sms = 148;
     std::string last_error;
 
@@ -231,6 +236,8 @@ void launch_source(Ctx& c);
 void launch_rhs(Ctx& c, bool have_force);
 void launch_assemble(Ctx& c);       // FP64 BSR (allocated on first use)
 void launch_assemble_lat(Ctx& c);   // FP64 + FP32 lattice half stencils
+void launch_assemble_p2(Ctx& c);    // P2-P1 FP64 BSR over vertices + edges (p2.cu)
+void launch_rhs_p2(Ctx& c, bool have_force);
 void ensure_bsr64(Ctx& c);          // BSR of the current system for callers that read it
 void launch_preconditioner(Ctx& c);
 void launch_to_f32(Ctx& c);

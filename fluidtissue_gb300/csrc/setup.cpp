@@ -44,6 +44,82 @@ RefConstants ref_constants() {
     return R;
 }
 
+// Quadrature rules of degree 3 (10 points) and 4 (20 points) on the unit
+// tetrahedron as the reference lists them (Quadrature.hpp:37-56): the point
+// coordinates and weights have to be these numbers for the element integrals
+// to match.
+namespace {
+const double kQ3x[10] = {0.7784952948213300, 0.0738349017262234, 0.0738349017262234, 0.0738349017262234, 0.4062443438840510, 0.4062443438840510, 0.4062443438840510, 0.0937556561159491, 0.0937556561159491, 0.0937556561159491};
+const double kQ3y[10] = {0.0738349017262234, 0.7784952948213300, 0.0738349017262234, 0.0738349017262234, 0.4062443438840510, 0.0937556561159491, 0.0937556561159491, 0.4062443438840510, 0.4062443438840510, 0.0937556561159491};
+const double kQ3z[10] = {0.0738349017262234, 0.0738349017262234, 0.7784952948213300, 0.0738349017262234, 0.0937556561159491, 0.4062443438840510, 0.0937556561159491, 0.4062443438840510, 0.0937556561159491, 0.4062443438840510};
+const double kQ3w[10] = {0.0476331348432089, 0.0476331348432089, 0.0476331348432089, 0.0476331348432089, 0.1349112434378610, 0.1349112434378610, 0.1349112434378610, 0.1349112434378610, 0.1349112434378610, 0.1349112434378610};
+const double kQ4x[20] = {0.9029422158182680, 0.0323525947272439, 0.0323525947272439, 0.0323525947272439, 0.2626825838877790, 0.6165965330619370, 0.2626825838877790, 0.6165965330619370, 0.2626825838877790, 0.6165965330619370, 0.0603604415251421, 0.0603604415251421, 0.0603604415251421, 0.0603604415251421, 0.0603604415251421, 0.0603604415251421, 0.3097693042728620, 0.3097693042728620, 0.3097693042728620, 0.0706920871814129};
+const double kQ4y[20] = {0.0323525947272439, 0.9029422158182680, 0.0323525947272439, 0.0323525947272439, 0.6165965330619370, 0.2626825838877790, 0.0603604415251421, 0.0603604415251421, 0.0603604415251421, 0.0603604415251421, 0.2626825838877790, 0.6165965330619370, 0.2626825838877790, 0.6165965330619370, 0.0603604415251421, 0.0603604415251421, 0.3097693042728620, 0.3097693042728620, 0.0706920871814129, 0.3097693042728620};
+const double kQ4z[20] = {0.0323525947272439, 0.0323525947272439, 0.9029422158182680, 0.0323525947272439, 0.0603604415251421, 0.0603604415251421, 0.6165965330619370, 0.2626825838877790, 0.0603604415251421, 0.0603604415251421, 0.6165965330619370, 0.2626825838877790, 0.0603604415251421, 0.0603604415251421, 0.2626825838877790, 0.6165965330619370, 0.3097693042728620, 0.0706920871814129, 0.3097693042728620, 0.3097693042728620};
+const double kQ4w[20] = {0.0070670747944695, 0.0070670747944695, 0.0070670747944695, 0.0070670747944695, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.1019369182898680, 0.1019369182898680, 0.1019369182898680, 0.1019369182898680};
+
+// P2 basis (vertices 0..3, then the edges 01 02 03 12 13 23) and its
+// reference gradient at float (x, y, z): expressions in double, results
+// rounded to float as the reference's std::function<float(float,float,float)>.
+void p2_basis(float x, float y, float z, double phi[10], double g[10][3]) {
+    const double X = x, Y = y, Z = z, L = 1.0 - X - Y - Z;
+    phi[0] = (float)(L * (1.0 - 2.0 * X - 2.0 * Y - 2.0 * Z));
+    phi[1] = (float)(X * (2.0 * X - 1.0));
+    phi[2] = (float)(Y * (2.0 * Y - 1.0));
+    phi[3] = (float)(Z * (2.0 * Z - 1.0));
+    phi[4] = (float)(4.0 * X * L);
+    phi[5] = (float)(4.0 * Y * L);
+    phi[6] = (float)(4.0 * Z * L);
+    phi[7] = (float)(4.0 * X * Y);
+    phi[8] = (float)(4.0 * X * Z);
+    phi[9] = (float)(4.0 * Y * Z);
+    const double s = 4.0 * X + 4.0 * Y + 4.0 * Z - 3.0;
+    const double gx[10] = {s, 4.0 * X - 1.0, 0.0, 0.0, -8.0 * X - 4.0 * Y - 4.0 * Z + 4.0,
+                           -4.0 * Y, -4.0 * Z, 4.0 * Y, 4.0 * Z, 0.0};
+    const double gy[10] = {s, 0.0, 4.0 * Y - 1.0, 0.0, -4.0 * X,
+                           -4.0 * X - 8.0 * Y - 4.0 * Z + 4.0, -4.0 * Z, 4.0 * X, 0.0, 4.0 * Z};
+    const double gz[10] = {s, 0.0, 0.0, 4.0 * Z - 1.0, -4.0 * X, -4.0 * Y,
+                           -4.0 * X - 4.0 * Y - 8.0 * Z + 4.0, 0.0, 4.0 * X, 4.0 * Y};
+    for (int a = 0; a < 10; ++a) {
+        g[a][0] = (float)gx[a];
+        g[a][1] = (float)gy[a];
+        g[a][2] = (float)gz[a];
+    }
+}
+
+void p1_basis(float x, float y, float z, double psi[4]) {
+    psi[0] = (float)(1.0 - (double)x - (double)y - (double)z);
+    psi[1] = x;
+    psi[2] = y;
+    psi[3] = z;
+}
+}  // namespace
+
+RefP2 ref_p2() {
+    RefP2 R;
+    std::memset(&R, 0, sizeof(R));
+    for (int q = 0; q < 20; ++q) {
+        double phi[10], g[10][3];
+        p2_basis((float)kQ4x[q], (float)kQ4y[q], (float)kQ4z[q], phi, g);
+        for (int a = 0; a < 10; ++a)
+            for (int b = 0; b < 10; ++b)
+                for (int m = 0; m < 3; ++m)
+                    for (int n = 0; n < 3; ++n) R.K[a][b][m][n] += kQ4w[q] * (g[a][m] * g[b][n]);
+    }
+    for (int q = 0; q < 10; ++q) {
+        double phi[10], g[10][3], psi[4];
+        const float x = (float)kQ3x[q], y = (float)kQ3y[q], z = (float)kQ3z[q];
+        p2_basis(x, y, z, phi, g);
+        p1_basis(x, y, z, psi);
+        for (int a = 0; a < 10; ++a)
+            for (int k = 0; k < 4; ++k) {
+                R.N[a][k] += kQ3w[q] * (phi[a] * psi[k]);
+                for (int m = 0; m < 3; ++m) R.B[a][k][m] += kQ3w[q] * (g[a][m] * psi[k]);
+            }
+    }
+    return R;
+}
+
 void boundary_from_faces(const fts_mesh& m, const HostTopology& T, std::vector<uint8_t>& bnd) {
     const int64_t nt = m.nt;
     const int32_t* tets = m.tets;
@@ -216,6 +292,139 @@ int build_topology(const fts_mesh& m, HostTopology& T, std::string& err) {
     T.n_interior = nI;
     T.lattice_n = detect_lattice(T);
     T.kuhn_elements = T.lattice_n > 0 && kuhn_element_order(m, T.lattice_n);
+    T.nv = np;
+    return FTS_OK;
+}
+
+int extend_p2(const fts_mesh& m, HostTopology& T, std::string& err) {
+    static const int kEdge[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+    const int64_t nv = T.np, nt = T.nt;
+    // edge ids: the slots (i, j > i) of the vertex graph, in row order
+    std::vector<int64_t> eid((size_t)T.rowptr[nv], -1);
+    int64_t ne = 0;
+    for (int64_t i = 0; i < nv; ++i)
+        for (int32_t q = T.rowptr[i]; q < T.rowptr[i + 1]; ++q)
+            if (T.cols[q] > i) eid[q] = ne++;
+    const int64_t nn = nv + ne;
+    if (nn >= (int64_t)1 << 31) {
+        err = "mesh: too many P2 nodes for 32-bit indices";
+        return FTS_ERR_BAD_INPUT;
+    }
+    auto edge_of = [&](int32_t a, int32_t b) -> int64_t {
+        if (a > b) std::swap(a, b);
+        const int32_t* c0 = T.cols.data() + T.rowptr[a];
+        const int32_t* c1 = T.cols.data() + T.rowptr[a + 1];
+        return eid[(size_t)(std::lower_bound(c0, c1, b) - T.cols.data())];
+    };
+    T.dofs.resize((size_t)nt * 10);
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < nt; ++k) {
+        const int32_t* t = m.tets + 4 * k;
+        int32_t* d = T.dofs.data() + 10 * k;
+        for (int j = 0; j < 4; ++j) d[j] = t[j];
+        for (int e = 0; e < 6; ++e)
+            d[4 + e] = (int32_t)(nv + edge_of(t[kEdge[e][0]], t[kEdge[e][1]]));
+    }
+    // system node -> (element, local DOF), ascending element per node
+    T.xp2t_ptr.assign((size_t)nn + 1, 0);
+    for (int64_t q = 0; q < 10 * nt; ++q) T.xp2t_ptr[T.dofs[q] + 1]++;
+    for (int64_t i = 0; i < nn; ++i) T.xp2t_ptr[i + 1] += T.xp2t_ptr[i];
+    T.xp2t.resize((size_t)nt * 10);
+    {
+        std::vector<int32_t> fill(T.xp2t_ptr.begin(), T.xp2t_ptr.end() - 1);
+        for (int64_t k = 0; k < nt; ++k)
+            for (int j = 0; j < 10; ++j)
+                T.xp2t[fill[T.dofs[10 * k + j]]++] = (uint32_t)((k << 4) | j);
+    }
+    // boundary edges: the edges of the triangles that belong to one element
+    std::vector<uint8_t> ebnd((size_t)ne, 0);
+    {
+        static const int kFace[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+#pragma omp parallel for schedule(static)
+        for (int64_t k = 0; k < nt; ++k) {
+            const int32_t* t = m.tets + 4 * k;
+            for (int f = 0; f < 4; ++f) {
+                const int32_t v[3] = {t[kFace[f][0]], t[kFace[f][1]], t[kFace[f][2]]};
+                bool shared = false;
+                for (int32_t q = T.p2t_ptr[v[0]]; q < T.p2t_ptr[v[0] + 1] && !shared; ++q) {
+                    const int64_t k2 = T.p2t[q] >> 2;
+                    if (k2 == k) continue;
+                    const int32_t* t2 = m.tets + 4 * k2;
+                    int hit = 0;
+                    for (int j = 0; j < 4; ++j) hit += (t2[j] == v[1]) + (t2[j] == v[2]);
+                    shared = hit == 2;
+                }
+                if (shared) continue;
+                for (int a = 0; a < 3; ++a)
+                    for (int b = a + 1; b < 3; ++b) {
+                        const int64_t e = edge_of(v[a], v[b]);
+#pragma omp atomic write
+                        ebnd[e] = 1;
+                    }
+            }
+        }
+    }
+    // extended graph: the DOFs of the node's elements, sorted unique
+    std::vector<int32_t> cnt((size_t)nn);
+    auto row = [&](int64_t i, std::vector<int32_t>& buf) {
+        buf.clear();
+        for (int32_t q = T.xp2t_ptr[i]; q < T.xp2t_ptr[i + 1]; ++q) {
+            const int32_t* d = T.dofs.data() + 10 * (int64_t)(T.xp2t[q] >> 4);
+            buf.insert(buf.end(), d, d + 10);
+        }
+        std::sort(buf.begin(), buf.end());
+        buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
+    };
+#pragma omp parallel
+    {
+        std::vector<int32_t> buf;
+#pragma omp for schedule(dynamic, 4096)
+        for (int64_t i = 0; i < nn; ++i) {
+            row(i, buf);
+            cnt[i] = (int32_t)buf.size();
+        }
+    }
+    std::vector<int32_t> rowptr((size_t)nn + 1, 0);
+    int64_t acc = 0;
+    int32_t maxr = 0;
+    for (int64_t i = 0; i < nn; ++i) {
+        rowptr[i] = (int32_t)acc;
+        acc += cnt[i];
+        maxr = std::max(maxr, cnt[i]);
+    }
+    if (acc >= (int64_t)1 << 31) {
+        err = "mesh: P2 node graph too large for 32-bit block indices";
+        return FTS_ERR_BAD_INPUT;
+    }
+    rowptr[nn] = (int32_t)acc;
+    std::vector<int32_t> cols((size_t)acc), diag((size_t)nn);
+#pragma omp parallel
+    {
+        std::vector<int32_t> buf;
+#pragma omp for schedule(dynamic, 4096)
+        for (int64_t i = 0; i < nn; ++i) {
+            row(i, buf);
+            std::copy(buf.begin(), buf.end(), cols.begin() + rowptr[i]);
+            diag[i] = rowptr[i] +
+                      (int32_t)(std::lower_bound(buf.begin(), buf.end(), (int32_t)i) - buf.begin());
+        }
+    }
+    T.rowptr.swap(rowptr);
+    T.cols.swap(cols);
+    T.diag.swap(diag);
+    T.max_row = maxr;
+    T.bnd.resize((size_t)nn);
+    for (int64_t e = 0; e < ne; ++e) T.bnd[nv + e] = ebnd[e];
+    // the vertex element lists stay; the edge nodes have none
+    T.p2t_ptr.resize((size_t)nn + 1, T.p2t_ptr[nv]);
+    int64_t nI = 0;
+    for (int64_t i = 0; i < nn; ++i) nI += T.bnd[i] ? 0 : 1;
+    T.n_interior = nI;
+    T.nv = nv;
+    T.ne = ne;
+    T.np = nn;
+    T.lattice_n = 0;
+    T.kuhn_elements = false;
     return FTS_OK;
 }
 

@@ -33,6 +33,11 @@
 //  * distance reset of the level set (host path)       src/fem/EuclideanDistance.cu:16-38, :92-117
 //  * level-set update: Crank-Nicolson advection,        src/fem/LevelSet.cpp:89-151, :261-300,
 //    Jacobi-BiCGSTAB, distance reset and mixing          :429-455; Assembler.hpp:179-190
+//  * P2-P1 (velocity degree 2): element integrals by     src/fem/Assembler.hpp:321-424,
+//    quadrature at the rule of degree deg_i + deg_j     src/fem/Quadrature.hpp:24-56,
+//    P2 / P1 basis tables float-rounded                 src/fem/Tetrahedron.hpp:56-115,
+//    DOFs vertices then edges, boundary edges           src/fem/TetraMesh.cpp:219-290,
+//    block system without the BP term                   src/growth/Flow.cpp:102-214, :345-399
 //  * surface-tension load: element / nodal gradients     src/growth/Flow.cpp:307-341;
 //    (Assembler.cpp:11-69), curvature, interface points  src/fem/LevelSet.cpp:215-253,
 //    and interface-patch areas                           :261-300, :326-420, :453
@@ -1323,6 +1328,250 @@ int ora_surface_tension(int64_t np, int64_t nt, const float* xyz, const int32_t*
     if (area_total) *area_total = atot;
     return 0;
 }
+
+// ---------------------------------------------------------------------------
+// P2-P1 system (the reference's velocity degree 2), in the reference's own
+// form: unknowns [ux(nd), uy(nd), uz(nd), p(np)] with nd = np + ne (vertices,
+// then edges), rows
+//   [A11 A12 A13 -Bx; A12' A22 A23 -By; A13' A23' A33 -Bz; Bx' By' Bz' eps M]
+// (Flow.cpp:160-203 with uDeg_ = 2), every P2 integral by the element loop of
+// bilin_without_p2t_ij: for trial j, test i, feval at the quadrature points
+// of the rule of degree deg_i + deg_j, dot (w/6), times |det B|
+// (Assembler.hpp:321-424); M by the P1 path.  F = [N fx + Cx s; N fy + Cy s;
+// N fz + Cz s; M s] (Flow.cpp:392-396).  The triplets are returned unsummed
+// (setFromTriplets sums them); sidx = interior velocity DOFs of the three
+// components and all pressure DOFs (Flow.cpp:35-44).
+// ---------------------------------------------------------------------------
+namespace {
+
+const double kR3x[10] = {0.7784952948213300, 0.0738349017262234, 0.0738349017262234, 0.0738349017262234, 0.4062443438840510, 0.4062443438840510, 0.4062443438840510, 0.0937556561159491, 0.0937556561159491, 0.0937556561159491};
+const double kR3y[10] = {0.0738349017262234, 0.7784952948213300, 0.0738349017262234, 0.0738349017262234, 0.4062443438840510, 0.0937556561159491, 0.0937556561159491, 0.4062443438840510, 0.4062443438840510, 0.0937556561159491};
+const double kR3z[10] = {0.0738349017262234, 0.0738349017262234, 0.7784952948213300, 0.0738349017262234, 0.0937556561159491, 0.4062443438840510, 0.0937556561159491, 0.4062443438840510, 0.0937556561159491, 0.4062443438840510};
+const double kR3w[10] = {0.0476331348432089, 0.0476331348432089, 0.0476331348432089, 0.0476331348432089, 0.1349112434378610, 0.1349112434378610, 0.1349112434378610, 0.1349112434378610, 0.1349112434378610, 0.1349112434378610};
+const double kR4x[20] = {0.9029422158182680, 0.0323525947272439, 0.0323525947272439, 0.0323525947272439, 0.2626825838877790, 0.6165965330619370, 0.2626825838877790, 0.6165965330619370, 0.2626825838877790, 0.6165965330619370, 0.0603604415251421, 0.0603604415251421, 0.0603604415251421, 0.0603604415251421, 0.0603604415251421, 0.0603604415251421, 0.3097693042728620, 0.3097693042728620, 0.3097693042728620, 0.0706920871814129};
+const double kR4y[20] = {0.0323525947272439, 0.9029422158182680, 0.0323525947272439, 0.0323525947272439, 0.6165965330619370, 0.2626825838877790, 0.0603604415251421, 0.0603604415251421, 0.0603604415251421, 0.0603604415251421, 0.2626825838877790, 0.6165965330619370, 0.2626825838877790, 0.6165965330619370, 0.0603604415251421, 0.0603604415251421, 0.3097693042728620, 0.3097693042728620, 0.0706920871814129, 0.3097693042728620};
+const double kR4z[20] = {0.0323525947272439, 0.0323525947272439, 0.9029422158182680, 0.0323525947272439, 0.0603604415251421, 0.0603604415251421, 0.6165965330619370, 0.2626825838877790, 0.0603604415251421, 0.0603604415251421, 0.6165965330619370, 0.2626825838877790, 0.0603604415251421, 0.0603604415251421, 0.2626825838877790, 0.6165965330619370, 0.3097693042728620, 0.0706920871814129, 0.3097693042728620, 0.3097693042728620};
+const double kR4w[20] = {0.0070670747944695, 0.0070670747944695, 0.0070670747944695, 0.0070670747944695, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.0469986689718877, 0.1019369182898680, 0.1019369182898680, 0.1019369182898680, 0.1019369182898680};
+
+// Basis tables at a rule: value[a][q], grad[a][c][q] (float-rounded).
+struct Tab {
+    int nq;
+    double w[20];
+    double p2[10][20], g2[10][3][20], p1[4][20];
+};
+
+Tab make_tab(int nq, const double* x, const double* y, const double* z, const double* w) {
+    Tab T;
+    T.nq = nq;
+    for (int q = 0; q < nq; ++q) {
+        T.w[q] = w[q] / 6.0;
+        const float fx = (float)x[q], fy = (float)y[q], fz = (float)z[q];
+        const double X = fx, Y = fy, Z = fz, L = 1.0 - X - Y - Z;
+        const double v[10] = {L * (1.0 - 2.0 * X - 2.0 * Y - 2.0 * Z), X * (2.0 * X - 1.0),
+                              Y * (2.0 * Y - 1.0), Z * (2.0 * Z - 1.0), 4.0 * X * L, 4.0 * Y * L,
+                              4.0 * Z * L, 4.0 * X * Y, 4.0 * X * Z, 4.0 * Y * Z};
+        const double sg = 4.0 * X + 4.0 * Y + 4.0 * Z - 3.0;
+        const double gx[10] = {sg, 4.0 * X - 1.0, 0.0, 0.0, -8.0 * X - 4.0 * Y - 4.0 * Z + 4.0,
+                               -4.0 * Y, -4.0 * Z, 4.0 * Y, 4.0 * Z, 0.0};
+        const double gy[10] = {sg, 0.0, 4.0 * Y - 1.0, 0.0, -4.0 * X,
+                               -4.0 * X - 8.0 * Y - 4.0 * Z + 4.0, -4.0 * Z, 4.0 * X, 0.0, 4.0 * Z};
+        const double gz[10] = {sg, 0.0, 0.0, 4.0 * Z - 1.0, -4.0 * X, -4.0 * Y,
+                               -4.0 * X - 4.0 * Y - 8.0 * Z + 4.0, 0.0, 4.0 * X, 4.0 * Y};
+        for (int a = 0; a < 10; ++a) {
+            T.p2[a][q] = (float)v[a];
+            T.g2[a][0][q] = (float)gx[a];
+            T.g2[a][1][q] = (float)gy[a];
+            T.g2[a][2][q] = (float)gz[a];
+        }
+        T.p1[0][q] = (float)(1.0 - X - Y - Z);
+        T.p1[1][q] = X;
+        T.p1[2][q] = Y;
+        T.p1[3][q] = Z;
+    }
+    return T;
+}
+
+struct P2Sys {
+    std::vector<int64_t> r;
+    std::vector<int32_t> c;
+    std::vector<double> v;
+    std::vector<double> F;
+    std::vector<int64_t> sidx;
+    int64_t nd = 0, ne = 0;
+};
+
+}  // namespace
+
+// Builds the system; returns a handle, the triplet count, nd and the reduced size.
+void* ora_p2_build(int64_t np, int64_t nt, const float* xyz, const int32_t* tets,
+                   const uint8_t* bnd, const double* mu, const double* s_in, const double* fst,
+                   double eps, int64_t* ntrip, int64_t* nd_out, int64_t* nred) {
+    Topology T;
+    build_topology(np, nt, tets, T);
+    // edges: (i, j > i) of the node graph in row order
+    std::vector<int64_t> eid(T.nb_ptr[np], -1);
+    int64_t ne = 0;
+    for (int64_t i = 0; i < np; ++i)
+        for (int64_t q = T.nb_ptr[i]; q < T.nb_ptr[i + 1]; ++q)
+            if (T.nb[q] > i) eid[q] = ne++;
+    auto edge = [&](int32_t a, int32_t b) {
+        if (a > b) std::swap(a, b);
+        const int n = (int)(T.nb_ptr[a + 1] - T.nb_ptr[a]);
+        return eid[T.nb_ptr[a] + find_col(T.nb.data() + T.nb_ptr[a], n, b)];
+    };
+    static const int le[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+    const int64_t nd = np + ne;
+    auto* S = new P2Sys;
+    S->nd = nd;
+    S->ne = ne;
+    // boundary DOFs: boundary vertices (given) and the edges of boundary faces
+    std::vector<char> dbnd(nd, 0);
+    for (int64_t i = 0; i < np; ++i) dbnd[i] = bnd[i] ? 1 : 0;
+    {
+        static const int fc[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+        for (int64_t k = 0; k < nt; ++k) {
+            const int32_t* t = tets + 4 * k;
+            for (int f = 0; f < 4; ++f) {
+                const int32_t v[3] = {t[fc[f][0]], t[fc[f][1]], t[fc[f][2]]};
+                bool shared = false;
+                for (int64_t q = T.p2t_ptr[v[0]]; q < T.p2t_ptr[v[0] + 1] && !shared; ++q) {
+                    const int64_t k2 = T.p2t[q];
+                    if (k2 == k) continue;
+                    const int32_t* t2 = tets + 4 * k2;
+                    int hit = 0;
+                    for (int j = 0; j < 4; ++j) hit += (t2[j] == v[1]) + (t2[j] == v[2]);
+                    shared = hit == 2;
+                }
+                if (shared) continue;
+                for (int a = 0; a < 3; ++a)
+                    for (int b = a + 1; b < 3; ++b) dbnd[np + edge(v[a], v[b])] = 1;
+            }
+        }
+    }
+    const Tab t4 = make_tab(20, kR4x, kR4y, kR4z, kR4w);
+    const Tab t3 = make_tab(10, kR3x, kR3y, kR3z, kR3w);
+    const RefTables& R1 = tables();
+    // zero-mean source (Flow.cpp:376)
+    std::vector<double> s(s_in, s_in + np);
+    double mean = 0.0;
+    for (double v : s) mean += v;
+    mean /= (double)np;
+    for (double& v : s) v -= mean;
+    S->F.assign(3 * nd + np, 0.0);
+    auto add = [&](int64_t r, int64_t c, double v) {
+        S->r.push_back(r);
+        S->c.push_back((int32_t)c);
+        S->v.push_back(v);
+    };
+    for (int64_t k = 0; k < nt; ++k) {
+        const int32_t* t = tets + 4 * k;
+        int64_t dof[10];
+        for (int j = 0; j < 4; ++j) dof[j] = t[j];
+        for (int e = 0; e < 6; ++e) dof[4 + e] = np + edge(t[le[e][0]], t[le[e][1]]);
+        Geom G;
+        if (!element_geom(xyz, t, G)) continue;
+        // invB^T (Geom.g[c+1][r] = invB^T(r, c)); global gradients at the points
+        double it[3][3];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) it[r][c] = G.g[c + 1][r];
+        auto grads = [&](const Tab& tb, double out[10][3][20]) {
+            for (int a = 0; a < 10; ++a)
+                for (int q = 0; q < tb.nq; ++q)
+                    for (int r = 0; r < 3; ++r)
+                        out[a][r][q] = it[r][0] * tb.g2[a][0][q] + it[r][1] * tb.g2[a][1][q] +
+                                       it[r][2] * tb.g2[a][2][q];
+        };
+        static thread_local double g4[10][3][20], g3[10][3][20];
+        grads(t4, g4);
+        grads(t3, g3);
+        const double detB = G.detB, m = mu[k];
+        auto integ4 = [&](auto f) {
+            double acc = 0.0;
+            for (int q = 0; q < 20; ++q) acc += f(q) * t4.w[q];
+            return acc * detB;
+        };
+        auto integ3 = [&](auto f) {
+            double acc = 0.0;
+            for (int q = 0; q < 10; ++q) acc += f(q) * t3.w[q];
+            return acc * detB;
+        };
+        // viscous blocks: trial j (u), test i (v)
+        for (int j = 0; j < 10; ++j)
+            for (int i = 0; i < 10; ++i) {
+                const auto& gu = g4[j];
+                const auto& gv = g4[i];
+                const double a11 = integ4([&](int q) { return (2.0 * gu[0][q] * gv[0][q] + gu[1][q] * gv[1][q] + gu[2][q] * gv[2][q]) * m; });
+                const double a22 = integ4([&](int q) { return (gu[0][q] * gv[0][q] + 2.0 * gu[1][q] * gv[1][q] + gu[2][q] * gv[2][q]) * m; });
+                const double a33 = integ4([&](int q) { return (gu[0][q] * gv[0][q] + gu[1][q] * gv[1][q] + 2.0 * gu[2][q] * gv[2][q]) * m; });
+                const double a12 = integ4([&](int q) { return gu[0][q] * gv[1][q] * m; });
+                const double a13 = integ4([&](int q) { return gu[0][q] * gv[2][q] * m; });
+                const double a23 = integ4([&](int q) { return gu[1][q] * gv[2][q] * m; });
+                const int64_t I = dof[i], J = dof[j];
+                add(I, J, a11);
+                add(nd + I, nd + J, a22);
+                add(2 * nd + I, 2 * nd + J, a33);
+                add(I, nd + J, a12);           // row x, column y: A12
+                add(nd + J, I, a12);           // A12' in row y
+                add(I, 2 * nd + J, a13);
+                add(2 * nd + J, I, a13);
+                add(nd + I, 2 * nd + J, a23);
+                add(2 * nd + J, nd + I, a23);
+            }
+        // B (test P2 i, trial P1 j), N, C, degree 3
+        for (int j = 0; j < 4; ++j)
+            for (int i = 0; i < 10; ++i) {
+                const int64_t I = dof[i], J = t[j];
+                const double bx = integ3([&](int q) { return g3[i][0][q] * t3.p1[j][q]; });
+                const double by = integ3([&](int q) { return g3[i][1][q] * t3.p1[j][q]; });
+                const double bz = integ3([&](int q) { return g3[i][2][q] * t3.p1[j][q]; });
+                add(I, 3 * nd + J, -bx);
+                add(nd + I, 3 * nd + J, -by);
+                add(2 * nd + I, 3 * nd + J, -bz);
+                add(3 * nd + J, I, bx);
+                add(3 * nd + J, nd + I, by);
+                add(3 * nd + J, 2 * nd + I, bz);
+                const double cm = 2.0 / 3 * m;
+                const double nij = integ3([&](int q) { return t3.p2[i][q] * t3.p1[j][q]; });
+                for (int al = 0; al < 3; ++al) {
+                    const double cij = integ3([&](int q) { return cm * (t3.p1[j][q] * g3[i][al][q]); });
+                    S->F[al * nd + I] += cij * s[J];
+                    if (fst) S->F[al * nd + I] += nij * fst[al * np + J];
+                }
+            }
+        // eps M and M s (P1, degree 2)
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) {
+                double f[4];
+                for (int q = 0; q < 4; ++q) f[q] = R1.phi[b][q] * R1.phi[a][q];
+                const double mab = integ(f, R1.qw, G.detB);
+                add(3 * nd + t[a], 3 * nd + t[b], eps * mab);
+                S->F[3 * nd + t[a]] += mab * s[t[b]];
+            }
+    }
+    int64_t nI = 0;
+    for (int64_t d = 0; d < nd; ++d) nI += dbnd[d] ? 0 : 1;
+    S->sidx.resize(3 * nI + np);
+    int64_t w = 0;
+    for (int c = 0; c < 3; ++c)
+        for (int64_t d = 0; d < nd; ++d)
+            if (!dbnd[d]) S->sidx[w++] = c * nd + d;
+    for (int64_t i = 0; i < np; ++i) S->sidx[w++] = 3 * nd + i;
+    *ntrip = (int64_t)S->v.size();
+    *nd_out = nd;
+    *nred = (int64_t)S->sidx.size();
+    return S;
+}
+
+void ora_p2_fetch(void* h, int64_t* rows, int32_t* cols, double* vals, double* F, int64_t* sidx) {
+    auto* S = static_cast<P2Sys*>(h);
+    std::copy(S->r.begin(), S->r.end(), rows);
+    std::copy(S->c.begin(), S->c.end(), cols);
+    std::copy(S->v.begin(), S->v.end(), vals);
+    std::copy(S->F.begin(), S->F.end(), F);
+    std::copy(S->sidx.begin(), S->sidx.end(), sidx);
+}
+
+void ora_p2_free(void* h) { delete static_cast<P2Sys*>(h); }
 
 // Timing helper for the CPU baseline.
 double ora_now_ms(void) { return now_ms(); }

@@ -75,6 +75,10 @@ def lib():
                                     C.c_int, _p(i64), _p(dbl), _p(i64)]),
         "ora_surface_tension": (C.c_int, [i64, i64, _p(f32), _p(i32), _p(dbl), _p(dbl), dbl,
                                           i32, _p(dbl), _p(i64), _p(dbl)]),
+        "ora_p2_build": (C.c_void_p, [i64, i64, _p(f32), _p(i32), _p(u8), _p(dbl), _p(dbl),
+                                      _p(dbl), dbl, _p(i64), _p(i64), _p(i64)]),
+        "ora_p2_fetch": (None, [C.c_void_p, _p(i64), _p(i32), _p(dbl), _p(dbl), _p(i64)]),
+        "ora_p2_free": (None, [C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -397,6 +401,67 @@ def ls_update(xyz, tets, flow, phi, dt, tol=1e-6, maxit=0, reset=True):
     return st, it.value, err.value, nif.value
 
 
+def p2_edges(tets):
+    """The P2 edge DOFs in the oracle's numbering: pairs (i < j) of the node
+    graph in row order (DOF np + e is the midpoint of edge e)."""
+    t = np.asarray(tets, np.int64)
+    pairs = np.concatenate([t[:, [a, b]] for a, b in ((0, 1), (0, 2), (0, 3), (1, 2), (1, 3),
+                                                      (2, 3))])
+    pairs.sort(axis=1)
+    return np.unique(pairs, axis=0)
+
+
+def p2_system(xyz, tets, boundary, phi, c, mu, par, fst=None, full=False):
+    """The P2-P1 system of Flow::Stokes_ with velocity degree 2, in the
+    reference's form, restricted to sidx: (scipy CSR A, F, sidx, nd); full:
+    the unrestricted matrix and load instead."""
+    import scipy.sparse as sp
+    g = lambda k: params_get(par, k)  # noqa: E731
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    tets = np.ascontiguousarray(tets, np.int32)
+    npn = xyz.shape[0]
+    s = source(phi, c, g("GF growth"), g("Level sink"), g("Growth threshold"))
+    bnd = np.ascontiguousarray(boundary, np.uint8)
+    mu = np.ascontiguousarray(mu, np.float64)
+    s_raw = np.ascontiguousarray(s, np.float64)
+    f = None if fst is None else np.ascontiguousarray(fst, np.float64)
+    ntrip, nd, nred = C.c_int64(), C.c_int64(), C.c_int64()
+    L = lib()
+    h = L.ora_p2_build(npn, tets.shape[0], _ptr(xyz, F32), _ptr(tets, I32), _ptr(bnd, U8),
+                       _ptr(mu, D), _ptr(s_raw, D), _ptr(f, D), g("eps"), C.byref(ntrip),
+                       C.byref(nd), C.byref(nred))
+    try:
+        rows = np.empty(ntrip.value, np.int64)
+        cols = np.empty(ntrip.value, np.int32)
+        vals = np.empty(ntrip.value)
+        F = np.empty(3 * nd.value + npn)
+        sidx = np.empty(nred.value, np.int64)
+        L.ora_p2_fetch(h, _ptr(rows, I64), _ptr(cols, I32), _ptr(vals, D), _ptr(F, D),
+                       _ptr(sidx, I64))
+    finally:
+        L.ora_p2_free(h)
+    n = 3 * nd.value + npn
+    A = sp.coo_matrix((vals, (rows, cols)), shape=(n, n)).tocsr()
+    A.sum_duplicates()
+    if full:
+        return A, F, sidx, nd.value
+    return A[sidx][:, sidx].tocsr(), F[sidx], sidx, nd.value
+
+
+def p2_flow(xyz, tets, boundary, phi, c, mu, par, fst=None):
+    """Direct solve of the P2-P1 reduced system, scattered as Flow.cpp:290-300:
+    [ux, uy, uz, p] at the vertices (boundary velocity 0)."""
+    import scipy.sparse.linalg as spla
+    A, F, sidx, nd = p2_system(xyz, tets, boundary, phi, c, mu, par, fst)
+    x = spla.spsolve(A.tocsc(), F)
+    npn = xyz.shape[0]
+    full = np.zeros(3 * nd + npn)
+    full[sidx] = x
+    flow = np.concatenate([full[0:npn], full[nd:nd + npn], full[2 * nd:2 * nd + npn],
+                           full[3 * nd:3 * nd + npn]])
+    return flow, A, F
+
+
 def surface_tension(xyz, tets, phi, phi_reset, st, rho):
     """Flow::surfaceTension_ with its LevelSet inputs restated: returns
     (force[3, np] as [fx, fy, fz], interface points, total patch area)."""
@@ -417,5 +482,5 @@ def surface_tension(xyz, tets, phi, phi_reset, st, rho):
 __all__ = ["build", "lib", "ref_tables", "boundary_nodes", "set_viscosity", "source",
            "assemble_blocks", "reduce", "spmv", "bicgstab", "true_residual", "scatter",
            "system", "direct_solve", "solve_tight", "flow_solve", "rd_solve", "RD_KEYS",
-           "surface_tension",
+           "surface_tension", "p2_edges", "p2_system", "p2_flow",
            "dist_reset", "ls_update"]

@@ -65,8 +65,10 @@ def test_create_rejects_bad_meshes_on_the_host(lib_built):
                     precision="fp64")
     assert lib.fts_create(C.byref(m), C.byref(p), C.byref(ctx)) == 1
     assert "out of range" in lib.fts_last_error(None).decode()
-    p.velocity_degree = 2  # P2-P1 is outside this path
+    p.velocity_degree = 3  # neither P1-P1 nor P2-P1
     assert lib.fts_create(C.byref(m), C.byref(p), C.byref(ctx)) == 6
+    p.velocity_degree = 2  # P2-P1 passes the parameter check; the mesh is still refused
+    assert lib.fts_create(C.byref(m), C.byref(p), C.byref(ctx)) == 1
     p.velocity_degree = 1
     # surface tension passes the parameter check (its load comes with the
     # solve); the mesh is still refused

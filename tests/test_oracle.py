@@ -393,3 +393,52 @@ def test_surface_tension_patches_by_hand(signs, count, area):
     assert nif == count
     assert abs(a - area) <= 1e-6
     assert np.all(f == 0.0)
+
+
+def _p2_case(n=7):
+    inst = workload("sphere17", n)
+    par = dict(inst.params)
+    return inst, par
+
+
+def test_p2_rigid_motions_are_in_the_kernel():
+    """Rigid rotations and translations have zero symmetric gradient and
+    divergence: the full P2-P1 operator maps them (velocity at the vertices
+    and edge midpoints, zero pressure) to zero, up to the float rounding of
+    the reference's basis tables."""
+    inst, par = _p2_case()
+    A, F, sidx, nd = O.p2_system(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source,
+                                 inst.mu, par, full=True)
+    E = O.p2_edges(inst.tets)
+    assert nd == inst.np + len(E)
+    X = inst.xyz.astype(np.float64)
+    P = np.concatenate([X, 0.5 * (X[E[:, 0]] + X[E[:, 1]])])
+    for u in ((-P[:, 1], P[:, 0], 0 * P[:, 0]), (0 * P[:, 0], -P[:, 2], P[:, 1]),
+              (np.ones(nd), np.zeros(nd), np.zeros(nd))):
+        x = np.concatenate([u[0], u[1], u[2], np.zeros(inst.np)])
+        r = A @ x
+        # the basis tables pass through float (Tetrahedron.hpp:17-18): identities
+        # hold to float rounding
+        assert np.abs(r).max() <= 1e-7 * abs(A).max() * np.abs(x).max(), np.abs(r).max()
+
+
+def test_p2_load_partition_of_unity_and_hydrostatic_balance():
+    """A uniform body force f = (1, 0, 0) with no source: the x load sums to
+    the volume (sum_i phi_i = 1); as eps -> 0 the discrete solution is u = 0,
+    p = x + const (-B p = N f holds exactly for linear p on P2-P1)."""
+    inst, par = _p2_case()
+    par = dict(par, **{"GF growth": 0.0, "eps": 1e-10})
+    npn = inst.np
+    f = np.zeros(3 * npn)
+    f[:npn] = 1.0
+    A, F, sidx, nd = O.p2_system(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source,
+                                 inst.mu, par, fst=f, full=True)
+    vol = _volumes(inst).sum()
+    assert abs(F[:nd].sum() - vol) <= 1e-7 * vol
+    assert np.abs(F[nd:]).max() == 0.0
+    flow, _, _ = O.p2_flow(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source, inst.mu,
+                           par, fst=f)
+    assert np.abs(flow[:3 * npn]).max() <= 1e-6
+    p = flow[3 * npn:]
+    x = inst.xyz[:, 0].astype(np.float64)
+    assert np.abs((p - p.mean()) - (x - x.mean())).max() <= 1e-6
