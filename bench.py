@@ -630,6 +630,114 @@ def run_dist(args):
     d.close()
 
 
+def run_p2(args):
+    """P2-P1 (Taylor-Hood, "Stokes velocity degree" 2) on the jittered 33^3
+    sphere workload (mu = 1, 8 Gaussian centres, tol 1e-8): value = mixed-
+    precision solves/s with device-resident inputs, e2e through fts_solve with
+    host buffers, beside the FP64 GPU path.  CPU baseline: the oracle's P2-P1
+    assembly (the reference's element loop) in full plus its reduced system's
+    sparse products, two per iteration of the reference's BiCGSTAB, times the
+    iterations the GPU's FP64 MINRES needs (a lower bound: the reference's
+    un-preconditioned BiCGSTAB needs more)."""
+    import torch
+    from fluidtissue_gb300 import workloads as W
+    from fluidtissue_gb300.flow import Flow, Mesh
+
+    ws, rank, local = _dist()
+    dist = _setup_dist(ws, local)
+    torch.cuda.set_device(local)
+    inst = W.sphere65(33)
+    par = dict(inst.params, **{"Stokes velocity degree": 2.0, "Stokes tolerance": 1e-8})
+    res = {}
+    for prec in ("mixed", "fp64"):
+        f = Flow()
+        if f.init(Mesh(inst.xyz, inst.tets), par, precision=prec, warm_start=False,
+                  device=local) != 0:
+            raise RuntimeError(f.last_error())
+        phi_d = torch.from_numpy(inst.phi).cuda()
+        src_d = torch.from_numpy(inst.source).cuda()
+        mu_d = torch.from_numpy(inst.mu).cuda()
+        flow_d = torch.zeros(4 * inst.np, dtype=torch.float64, device="cuda")
+        phi_h = torch.from_numpy(inst.phi).pin_memory()
+        src_h = torch.from_numpy(inst.source).pin_memory()
+        mu_h = torch.from_numpy(inst.mu).pin_memory()
+        flow_h = torch.zeros(4 * inst.np, dtype=torch.float64).pin_memory()
+
+        def dev_step():
+            rc = f.solve_device(phi_d.data_ptr(), src_d.data_ptr(), mu_d.data_ptr(),
+                                flow_d.data_ptr())
+            if rc != 0:
+                raise RuntimeError(f"fts_solve_device failed ({rc}): {f.last_error()}")
+            return dict(f.last_stats)
+
+        def e2e_step():
+            rc = f.solve(phi_h.numpy(), src_h.numpy(), flow_h.numpy(), mu=mu_h.numpy())
+            if rc != 0:
+                raise RuntimeError(f"fts_solve failed ({rc}): {f.last_error()}")
+
+        for _ in range(args.warmup):
+            dev_step()
+        _barrier(dist)
+        clk = Clocks(local) if prec == "mixed" else None
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        stats = [dev_step() for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        wall = _max_over_ranks((time.perf_counter() - t0) * 1e3, dist)
+        clocks = clk.stop() if clk else None
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        wall_e2e = _max_over_ranks((time.perf_counter() - t0) * 1e3, dist)
+        res[prec] = {"ms": wall / args.steps, "ms_e2e": wall_e2e / args.steps, "st": stats[-1],
+                     "clocks": clocks, "flow": flow_d.cpu().numpy()}
+        npx, nnzb, nred = f.sizes()
+        f.close()
+    m, d = res["mixed"], res["fp64"]
+    npn = inst.np
+    vel_err = float(np.linalg.norm(m["flow"][:3 * npn] - d["flow"][:3 * npn]) /
+                    np.linalg.norm(d["flow"][:3 * npn]))
+    line = {"metric": "P2-P1 Stokes solves/s (33^3 sphere, mu 1, tol 1e-8), mixed vs FP64 GPU",
+            "value": round(ws * 1e3 / m["ms"], 4), "unit": "solves/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(m["ms"], 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 inner / f64 outer",
+            "data": "synthetic (seeded jittered Kuhn lattice, analytic level set)",
+            "config": {"workload": f"p2sphere33: {npn} vertices + {npx - npn} edges, "
+                                   f"{nnzb} 4x4 blocks, {nred} reduced unknowns"},
+            "e2e": {"value": round(ws * 1e3 / m["ms_e2e"], 4), "unit": "solves/s",
+                    "h2d_bytes_per_step": 8 * (2 * npn + inst.nt),
+                    "d2h_bytes_per_step": 8 * 4 * npn},
+            "fp64": {"value": round(ws * 1e3 / d["ms"], 4), "unit": "solves/s",
+                     "iterations": d["st"]["iterations"]},
+            "mixed": {"iterations": m["st"]["iterations"], "outer": m["st"]["outer_iterations"],
+                      "rel_residual": m["st"]["rel_residual"], "vel_err_vs_fp64": vel_err},
+            "ms_assembly": round(m["st"]["ms_assembly"], 3),
+            "gpu_launches": int(m["st"]["kernel_launches"]), "clocks": m["clocks"]}
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle as O
+        t0 = time.perf_counter()
+        A, F, _, _ = O.p2_system(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source,
+                                 inst.mu, par)
+        t_asm = time.perf_counter() - t0
+        x = np.ones(A.shape[0])
+        reps = 20
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            A @ x
+        t_spmv = (time.perf_counter() - t0) / reps
+        its = d["st"]["iterations"]
+        t_cpu = t_asm + 2 * its * t_spmv
+        line["cpu_baseline"] = {
+            "value": 1.0 / t_cpu, "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": (f"oracle P2-P1 assembly in full ({t_asm:.2f} s) + 2 x {its} sparse "
+                       f"products of the reduced system ({t_spmv * 1e3:.1f} ms each, scipy, "
+                       f"1 thread): a lower bound for the reference's BiCGSTAB")}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_st(args):
     """Surface-tension load (Flow::surfaceTension_ with LevelSet's normals,
     curvature and interface patches) on the ellipsoid129 mesh, phi = the
@@ -807,6 +915,8 @@ def main():
         run_ls(args)
     elif args.workload == "st129":
         run_st(args)
+    elif args.workload == "p2sphere33":
+        run_p2(args)
     else:
         run_ours(args)
 
