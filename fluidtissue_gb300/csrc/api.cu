@@ -199,6 +199,9 @@ static void configure_preconditioner(Ctx& c) {
         throw (int)FTS_ERR_UNSUPPORTED;
     }
     c.use_mg = mg_ok && c.par.preconditioner != FTS_PC_JACOBI;
+    // batched solves keep the pressure diagonal: on batch96 (jumps of mu up to
+    // 1e3 across spheres) a pressure V-cycle inside the persistent kernel cut
+    // no iterations and its registers slowed every phase
     c.use_pmg = c.use_mg && !c.in_batch && c.par.preconditioner != FTS_PC_MULTIGRID_DIAG;
     if (c.use_pmg && !c.aux_stream) {
         FTS_CUDA(cudaStreamCreateWithFlags(&c.aux_stream, cudaStreamNonBlocking));
