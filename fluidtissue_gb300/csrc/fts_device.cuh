@@ -273,6 +273,30 @@ inline T* dev_alloc(Ctx& c, size_t n) {
     return static_cast<T*>(p);
 }
 
+// Programmatic dependent launch: a kernel started by pdl_launch may be
+// scheduled while the previous kernel of its stream drains (its launch and
+// block start-up overlap the predecessor's tail).  Every such kernel calls
+// pdl_wait() before it touches global memory; the wait returns once the
+// predecessor has completed and its writes are visible (and at once for a
+// kernel launched without the attribute).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline void pdl_launch(void (*kern)(KArgs...), int grid, int block, cudaStream_t s,
+                       Args&&... args) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)grid);
+    lc.blockDim = dim3((unsigned)block);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    FTS_CUDA(cudaLaunchKernelEx(&lc, kern, static_cast<KArgs>(args)...));
+}
+
 inline int grid_for(const Ctx& c, int64_t work, int threads = kThreads, int per_sm = 8) {
     int64_t need = (work + threads - 1) / threads;
     int64_t cap = (int64_t)c.num_sms * per_sm;

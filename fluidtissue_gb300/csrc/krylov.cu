@@ -372,6 +372,7 @@ __global__ void __launch_bounds__(kThreads)
 k_minres_A(int64_t np, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ cols,
            const T* __restrict__ A, const V4<T>* __restrict__ Y, int ybuf,
            const V4<T>* __restrict__ R1, T* __restrict__ q, Reduction red, MinresScalars* s) {
+    pdl_wait();
     if (s->stop) return;
     const double invb = 1.0 / s->beta;
     const T tinv = (T)invb;
@@ -415,6 +416,7 @@ k_minres_A_ell(int64_t np, int64_t nslices, const int32_t* __restrict__ ell_ptr,
                const int32_t* __restrict__ ell_col, const float* __restrict__ ell_val,
                const V4<float>* __restrict__ Y, int ybuf, const V4<float>* __restrict__ R1,
                float* __restrict__ q, Reduction red, MinresScalars* s) {
+    pdl_wait();
     if (s->stop) return;
     const float tinv = (float)(1.0 / s->beta);
     const float wadd = (float)s->ycorr[ybuf];
@@ -463,6 +465,7 @@ __global__ void __launch_bounds__(kThreads)
 k_minres_A_lat(int n, int64_t np, const float4* __restrict__ L, const V4<float>* __restrict__ Y,
                int ybuf, const V4<float>* __restrict__ R1, V4<float>* __restrict__ q,
                Reduction red, MinresScalars* s) {
+    pdl_wait();
     if (s->stop) return;
     const float tinv = (float)(1.0 / s->beta);
     const float wadd = (float)s->ycorr[ybuf];
@@ -502,6 +505,7 @@ k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
              const V4<T>* __restrict__ R2, V4<T>* Rn, const T* __restrict__ pc,
              V4<T>* __restrict__ Ynew, int ybuf, LevelView<T> L0, PView<T> P0, int pmg,
              Reduction red, MinresScalars* s) {
+    pdl_wait();
     if (s->stop) return;
     T c1 = T(0), c2 = T(0);
     if (!init) {
@@ -566,9 +570,13 @@ __global__ void __launch_bounds__(kThreads)
 k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, PView<T> P0,
              int pmg, int init, const V4<T>* __restrict__ Rn, V4<T>* __restrict__ Ynew,
              int ybuf, Reduction red, MinresScalars* s) {
+    pdl_wait();
     if (s->stop) return;
     double acc[1] = {0.0};
-    const T* pdin = (step & 1) ? P0.d0 : P0.d1;
+    // the pressure V-cycle's last finest step (its own smoothing degree)
+    constexpr int ps = kPSmooth - 1;
+    constexpr int pmode = ps == 1 ? kStepAfterFirst : kStepRegular;
+    const T* pdin = (ps & 1) ? P0.d0 : P0.d1;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L0.N;
          i += (int64_t)gridDim.x * blockDim.x) {
         T xo[3];
@@ -579,7 +587,7 @@ k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, PVi
         z.y = xo[1];
         z.z = xo[2];
         if (pmg) {
-            z.w = pmg_step_node<T>(P0, i, step, mode, pdin, nullptr, false);
+            z.w = pmg_step_node<T>(P0, i, ps, pmode, pdin, nullptr, false);
             acc[0] += (double)(n.w * z.w);
         }
         Ynew[i] = z;
@@ -599,6 +607,7 @@ __global__ void __launch_bounds__(kThreads)
 k_minres_C(int64_t np, const V4<T>* __restrict__ Yk, int ybuf, V4<T>* Wprev,
            const V4<T>* __restrict__ Wcur, V4<T>* __restrict__ X, Reduction red,
            MinresScalars* s) {
+    pdl_wait();
     if (!s->c_pending) return;
     const T inv = (T)(1.0 / s->oldb);
     const T wadd = (T)s->ycorr[ybuf];
@@ -664,7 +673,7 @@ static void launch_pc(Ctx& c, bool use_mg, int init, const V4<T>* q, V4<T>* R1, 
         const LevelView<T> L0 = level_view(mg, 0);
         const bool pmg = c.use_pmg;
         const PView<T> P0 = pmg ? pview(pmg_of<T>(c), 0) : PView<T>{};
-        k_minres_pc1<T, true><<<gn, kThreads, 0, c.stream>>>(c.np, init, q, R1, R2, Rn, pc, Ynew,
+        pdl_launch(k_minres_pc1<T, true>, gn, kThreads, c.stream, c.np, init, q, R1, R2, Rn, pc, Ynew,
                                                              ybuf, L0, P0, pmg ? 1 : 0, c.red,
                                                              c.ms);
         if (pmg) {  // pressure V-cycle on the second stream, beside the velocity one
@@ -677,12 +686,12 @@ static void launch_pc(Ctx& c, bool use_mg, int init, const V4<T>* q, V4<T>* R1, 
         if (pmg) FTS_CUDA(cudaStreamWaitEvent(c.stream, c.ev_join, 0));
         // the last post-smoothing step: step kSmooth - 1 reads d0 when it is odd
         constexpr int s = kSmooth - 1;
-        k_minres_pc2<T><<<gn, kThreads, 0, c.stream>>>(
+        pdl_launch(k_minres_pc2<T>, gn, kThreads, c.stream,
             L0, s, s == 1 ? kStepAfterFirst : kStepRegular, (s & 1) ? L0.d0 : L0.d1, P0,
             pmg ? 1 : 0, init, Rn, Ynew, ybuf, c.red, c.ms);
         c.launches += 2;
     } else {
-        k_minres_pc1<T, false><<<gn, kThreads, 0, c.stream>>>(c.np, init, q, R1, R2, Rn, pc, Ynew,
+        pdl_launch(k_minres_pc1<T, false>, gn, kThreads, c.stream, c.np, init, q, R1, R2, Rn, pc, Ynew,
                                                               ybuf, LevelView<T>{}, PView<T>{}, 0,
                                                               c.red, c.ms);
         c.launches += 1;
@@ -732,24 +741,24 @@ long long minres_inner(Ctx& c, double rtol, long long maxit, double* achieved, i
                                    reinterpret_cast<const V4<float>*>(R1),
                                    reinterpret_cast<V4<float>*>(w.q));
             else if (sizeof(T) == 4 && c.use_lat)
-                k_minres_A_lat<<<gn, kThreads, 0, c.stream>>>(
+                pdl_launch(k_minres_A_lat, gn, kThreads, c.stream,
                     c.topo.lattice_n, np, reinterpret_cast<const float4*>(c.lat_val),
                     reinterpret_cast<const V4<float>*>(w.Y[yk]),
                     yk, reinterpret_cast<const V4<float>*>(R1), reinterpret_cast<V4<float>*>(w.q),
                     c.red, c.ms);
             else if (sizeof(T) == 4 && c.use_ell)
-                k_minres_A_ell<<<grid_for(c, c.nslices * 32), kThreads, 0, c.stream>>>(
+                pdl_launch(k_minres_A_ell, grid_for(c, c.nslices * 32), kThreads, c.stream,
                     np, c.nslices, c.ell_ptr, c.ell_col, c.ell_val,
                     reinterpret_cast<const V4<float>*>(w.Y[yk]), yk,
                     reinterpret_cast<const V4<float>*>(R1), reinterpret_cast<float*>(w.q),
                     c.red, c.ms);
             else
-                k_minres_A<T><<<ge, kThreads, 0, c.stream>>>(np, c.rowptr, c.cols, A, w.Y[yk], yk,
+                pdl_launch(k_minres_A<T>, ge, kThreads, c.stream, np, c.rowptr, c.cols, A, w.Y[yk], yk,
                                                              R1, reinterpret_cast<T*>(w.q), c.red,
                                                              c.ms);
             if (timed) FTS_CUDA(cudaEventRecord(c.tev[2 * u + 1], c.stream));
             launch_pc<T>(c, use_mg, 0, w.q, R1, R2, R1, w.Y[yn], yn);
-            k_minres_C<T><<<gn, kThreads, 0, c.stream>>>(np, w.Y[yk], yk, Wprev, Wcur, w.X, c.red,
+            pdl_launch(k_minres_C<T>, gn, kThreads, c.stream, np, w.Y[yk], yk, Wprev, Wcur, w.X, c.red,
                                                          c.ms);
             c.launches += 2;
         }

@@ -393,6 +393,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads, 4)
 k_mg_step(LevelView<T> L, int step, int mode, const T* __restrict__ din, T* __restrict__ dout,
           const int* __restrict__ stop) {
+    pdl_wait();
     if (stop && *stop) return;
     T xo[3];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.N;
@@ -403,6 +404,7 @@ k_mg_step(LevelView<T> L, int step, int mode, const T* __restrict__ din, T* __re
 template <typename T>
 __global__ void __launch_bounds__(kThreads, 4)
 k_mg_residual(LevelView<T> L, const int* __restrict__ stop) {
+    pdl_wait();
     if (stop && *stop) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.N;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -412,6 +414,7 @@ k_mg_residual(LevelView<T> L, const int* __restrict__ stop) {
 template <typename T>
 __global__ void __launch_bounds__(kThreads, 4)
 k_mg_resid_first(LevelView<T> L, const int* __restrict__ stop) {
+    pdl_wait();
     if (stop && *stop) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.N;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -420,6 +423,7 @@ k_mg_resid_first(LevelView<T> L, const int* __restrict__ stop) {
 
 template <typename T>
 __global__ void k_mg_restrict(LevelView<T> F, LevelView<T> C, const int* __restrict__ stop) {
+    pdl_wait();
     if (stop && *stop) return;
     for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < C.N;
          I += (int64_t)gridDim.x * blockDim.x)
@@ -428,6 +432,7 @@ __global__ void k_mg_restrict(LevelView<T> F, LevelView<T> C, const int* __restr
 
 template <typename T>
 __global__ void k_mg_prolong(LevelView<T> F, LevelView<T> C, const int* __restrict__ stop) {
+    pdl_wait();
     if (stop && *stop) return;
     for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < F.N;
          f += (int64_t)gridDim.x * blockDim.x)
@@ -437,6 +442,7 @@ __global__ void k_mg_prolong(LevelView<T> F, LevelView<T> C, const int* __restri
 template <typename T>
 __global__ void __launch_bounds__(kCoarseThreads)
 k_mg_coarse_solve(LevelView<T> L, int steps, const int* __restrict__ stop) {
+    pdl_wait();
     if (stop && *stop) return;
     mg_coarse_block<T>(L, steps);
 }
@@ -462,6 +468,7 @@ __global__ void __launch_bounds__(kTailThreads, 1)
 k_mg_tail(const __grid_constant__ MGTailArgs<T> a, const int* __restrict__ stop) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
+    pdl_wait();
     if (stop && *stop) return;  // uniform: nothing writes the flag during the V-cycle
     const int64_t tid = (int64_t)cl.block_rank() * blockDim.x + threadIdx.x;
     const int64_t nth = (int64_t)cl.num_blocks() * blockDim.x;
@@ -688,7 +695,7 @@ static void vcycle_level(Ctx& c, MG<T>& mg, size_t l, const int* stop, bool skip
         return;
     }
     if (l + 1 == mg.L.size()) {
-        k_mg_coarse_solve<T><<<1, kCoarseThreads, 0, c.stream>>>(L, L.n == 3 ? 1 : kCoarse, stop);
+        pdl_launch(k_mg_coarse_solve<T>, 1, kCoarseThreads, c.stream, L, L.n == 3 ? 1 : kCoarse, stop);
         c.launches += 1;
         return;
     }
@@ -697,23 +704,23 @@ static void vcycle_level(Ctx& c, MG<T>& mg, size_t l, const int* stop, bool skip
     T* din = L.d0;
     T* dout = L.d1;
     for (int s = 1; s < kSmooth; ++s) {
-        k_mg_step<T><<<g, kThreads, 0, c.stream>>>(L, s, s == 1 ? kStepFromZero : kStepRegular,
+        pdl_launch(k_mg_step<T>, g, kThreads, c.stream, L, s, s == 1 ? kStepFromZero : kStepRegular,
                                                    din, dout, stop);
         std::swap(din, dout);
     }
-    k_mg_residual<T><<<g, kThreads, 0, c.stream>>>(L, stop);
+    pdl_launch(k_mg_residual<T>, g, kThreads, c.stream, L, stop);
     k_mg_restrict<T><<<grid_for(c, C.N), kThreads, 0, c.stream>>>(L, C, stop);
     c.launches += kSmooth + 1;
     vcycle_level<T>(c, mg, l + 1, stop, false);
-    k_mg_prolong<T><<<g, kThreads, 0, c.stream>>>(L, C, stop);
+    pdl_launch(k_mg_prolong<T>, g, kThreads, c.stream, L, C, stop);
     // post-smoothing from the corrected x
-    k_mg_resid_first<T><<<g, kThreads, 0, c.stream>>>(L, stop);
+    pdl_launch(k_mg_resid_first<T>, g, kThreads, c.stream, L, stop);
     c.launches += 2;
     din = L.d0;
     dout = L.d1;
     for (int s = 1; s < kSmooth; ++s) {
         if (skip_final && s == kSmooth - 1) break;
-        k_mg_step<T><<<g, kThreads, 0, c.stream>>>(L, s, s == 1 ? kStepAfterFirst : kStepRegular,
+        pdl_launch(k_mg_step<T>, g, kThreads, c.stream, L, s, s == 1 ? kStepAfterFirst : kStepRegular,
                                                    din, dout, stop);
         std::swap(din, dout);
         c.launches += 1;

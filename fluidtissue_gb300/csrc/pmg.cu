@@ -207,6 +207,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads)
 k_pmg_step(PView<T> L, int step, int mode, const T* __restrict__ din, T* __restrict__ dout,
            const int* __restrict__ stop) {
+    pdl_wait();
     if (stop && *stop) return;
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < L.N;
          v += (int64_t)gridDim.x * blockDim.x)
@@ -216,6 +217,7 @@ k_pmg_step(PView<T> L, int step, int mode, const T* __restrict__ din, T* __restr
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 k_pmg_residual(PView<T> L, const int* __restrict__ stop) {
+    pdl_wait();
     if (stop && *stop) return;
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < L.N;
          v += (int64_t)gridDim.x * blockDim.x)
@@ -225,6 +227,7 @@ k_pmg_residual(PView<T> L, const int* __restrict__ stop) {
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 k_pmg_resid_first(PView<T> L, const int* __restrict__ stop) {
+    pdl_wait();
     if (stop && *stop) return;
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < L.N;
          v += (int64_t)gridDim.x * blockDim.x)
@@ -233,6 +236,7 @@ k_pmg_resid_first(PView<T> L, const int* __restrict__ stop) {
 
 template <typename T>
 __global__ void k_pmg_restrict(PView<T> F, PView<T> C, const int* __restrict__ stop) {
+    pdl_wait();
     if (stop && *stop) return;
     for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < C.N;
          I += (int64_t)gridDim.x * blockDim.x)
@@ -241,6 +245,7 @@ __global__ void k_pmg_restrict(PView<T> F, PView<T> C, const int* __restrict__ s
 
 template <typename T>
 __global__ void k_pmg_prolong(PView<T> F, PView<T> C, const int* __restrict__ stop) {
+    pdl_wait();
     if (stop && *stop) return;
     for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < F.N;
          f += (int64_t)gridDim.x * blockDim.x)
@@ -259,11 +264,12 @@ struct PTailArgs {
 template <typename T>
 __global__ void __launch_bounds__(kPTailThreads, 1)
 k_pmg_tail(const __grid_constant__ PTailArgs<T> a, const int* __restrict__ stop) {
+    pdl_wait();
     if (stop && *stop) return;  // uniform over the block
     const int tid = threadIdx.x, nth = blockDim.x;
     for (int l = a.l0; l + 1 < a.nlev; ++l) {
         const PView<T> L = a.lv[l];
-        for (int s = 1; s < kSmooth; ++s) {
+        for (int s = 1; s < kPSmooth; ++s) {
             const int mode = s == 1 ? kStepFromZero : kStepRegular;
             for (int64_t v = tid; v < L.N; v += nth)
                 pmg_step_node<T>(L, v, s, mode, (s & 1) ? L.d0 : L.d1, (s & 1) ? L.d1 : L.d0,
@@ -292,7 +298,7 @@ k_pmg_tail(const __grid_constant__ PTailArgs<T> a, const int* __restrict__ stop)
         __syncthreads();
         for (int64_t v = tid; v < L.N; v += nth) pmg_resid_first_node<T>(L, v);
         __syncthreads();
-        const int last = (l == 0 && a.skip_final) ? kSmooth - 2 : kSmooth - 1;
+        const int last = (l == 0 && a.skip_final) ? kPSmooth - 2 : kPSmooth - 1;
         for (int s = 1; s <= last; ++s) {
             const int mode = s == 1 ? kStepAfterFirst : kStepRegular;
             for (int64_t v = tid; v < L.N; v += nth)
@@ -340,7 +346,7 @@ static void pmg_build(Ctx& c, PMG<T>& pm) {
 // Chebyshev coefficients on [lam / 10, lam] (same recurrence as the velocity
 // hierarchy's): 1/theta, then (rho_s rho_{s-1}, 2 rho_s / delta) for s >= 1.
 static void pcheb_table(double lam, double* out) {
-    const double lmax = lam, lmin = 0.1 * lam;
+    const double lmax = lam, lmin = kPLowFrac * lam;
     const double th = 0.5 * (lmax + lmin), de = 0.5 * (lmax - lmin), sg = th / de;
     out[0] = 1.0 / th;
     double rho = 1.0 / sg;
@@ -483,7 +489,7 @@ static void pvcycle_level(Ctx& c, PMG<T>& pm, size_t l, cudaStream_t st, const i
         a.l0 = (int)l;
         a.nlev = (int)pm.L.size();
         a.skip_final = skip_final ? 1 : 0;
-        k_pmg_tail<T><<<1, kPTailThreads, 0, st>>>(a, stop);
+        pdl_launch(k_pmg_tail<T>, 1, kPTailThreads, st, a, stop);
         c.launches += 1;
         return;
     }
@@ -491,23 +497,23 @@ static void pvcycle_level(Ctx& c, PMG<T>& pm, size_t l, cudaStream_t st, const i
     const int g = grid_for(c, L.N);
     T* din = L.d0;
     T* dout = L.d1;
-    for (int s = 1; s < kSmooth; ++s) {
-        k_pmg_step<T><<<g, kThreads, 0, st>>>(L, s, s == 1 ? kStepFromZero : kStepRegular, din,
+    for (int s = 1; s < kPSmooth; ++s) {
+        pdl_launch(k_pmg_step<T>, g, kThreads, st, L, s, s == 1 ? kStepFromZero : kStepRegular, din,
                                               dout, stop);
         std::swap(din, dout);
     }
-    k_pmg_residual<T><<<g, kThreads, 0, st>>>(L, stop);
+    pdl_launch(k_pmg_residual<T>, g, kThreads, st, L, stop);
     k_pmg_restrict<T><<<grid_for(c, C.N), kThreads, 0, st>>>(L, C, stop);
-    c.launches += kSmooth + 1;
+    c.launches += kPSmooth + 1;
     pvcycle_level<T>(c, pm, l + 1, st, stop, false);
-    k_pmg_prolong<T><<<g, kThreads, 0, st>>>(L, C, stop);
-    k_pmg_resid_first<T><<<g, kThreads, 0, st>>>(L, stop);
+    pdl_launch(k_pmg_prolong<T>, g, kThreads, st, L, C, stop);
+    pdl_launch(k_pmg_resid_first<T>, g, kThreads, st, L, stop);
     c.launches += 2;
     din = L.d0;
     dout = L.d1;
-    for (int s = 1; s < kSmooth; ++s) {
-        if (skip_final && s == kSmooth - 1) break;
-        k_pmg_step<T><<<g, kThreads, 0, st>>>(L, s, s == 1 ? kStepAfterFirst : kStepRegular,
+    for (int s = 1; s < kPSmooth; ++s) {
+        if (skip_final && s == kPSmooth - 1) break;
+        pdl_launch(k_pmg_step<T>, g, kThreads, st, L, s, s == 1 ? kStepAfterFirst : kStepRegular,
                                               din, dout, stop);
         std::swap(din, dout);
         c.launches += 1;

@@ -12,7 +12,7 @@
 // the weight 1/2 of its Kuhn edges.  Per level a scalar half stencil SoA
 // K[d][N] (d = 0 self, 1..7 the positive Kuhn directions; the entry towards
 // -e of node v is K[e][v - e]), the inverse diagonal, and the V-cycle vectors.
-// Chebyshev smoothing of degree kSmooth in D^-1 Kp on [lambda/10, lambda] with
+// Chebyshev smoothing of degree kPSmooth in D^-1 Kp on [kPLowFrac lambda, lambda] with
 // lambda the Gershgorin bound max_i sum_j |Kp_ij| / Kp_ii of each level: an
 // upper bound of the spectrum, so every smoother is convergent and the
 // V-cycle is SPD whatever the coefficients.  Coarsest level (3^3 or 4^3
@@ -27,6 +27,9 @@
 #include "mg.cuh"
 
 namespace fts {
+
+constexpr int kPSmooth = 2;          // Chebyshev degree of each pressure pre / post smoothing
+constexpr double kPLowFrac = 0.1;    // lower end of the smoothing interval / lambda
 
 // Levels with at most this many nodes run in one launch of a single CTA.
 constexpr int64_t kPTailNodes = 1000;
