@@ -683,13 +683,15 @@ static void vcycle_level(Ctx& c, MG<T>& mg, size_t l, const int* stop, bool skip
         lc.gridDim = dim3((unsigned)mg.tail_blocks);
         lc.blockDim = dim3((unsigned)kTailThreads);
         lc.stream = c.stream;
-        cudaLaunchAttribute attr[1];
+        cudaLaunchAttribute attr[2];
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = (unsigned)mg.tail_blocks;
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
+        attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[1].val.programmaticStreamSerializationAllowed = 1;
         lc.attrs = attr;
-        lc.numAttrs = 1;
+        lc.numAttrs = 2;
         FTS_CUDA(cudaLaunchKernelEx(&lc, k_mg_tail<T>, a, stop));
         c.launches += 1;
         return;
