@@ -84,3 +84,15 @@ def test_p2_options_refused_and_degree_fixed():
     f, _ = _solve(inst, par, precision="fp64")
     assert f.update_params(dict(par, **{"Stokes velocity degree": 1.0})) == 1
     f.close()
+
+
+def test_p2_matches_golden_fixture():
+    """The committed P2-P1 fixture (the oracle's direct solve, 7^3 sphere)."""
+    from conftest import ROOT
+    g = np.load(ROOT / "tests" / "golden" / "p2_sphere17_n7.npz")
+    inst = workload(str(g["name"]), int(g["n"]))
+    par = dict(inst.params, **{"Stokes velocity degree": 2.0, "Stokes tolerance": 1e-11})
+    f, flow = _solve(inst, par, precision="fp64")
+    assert f.solve(inst.phi, inst.source, flow, mu=inst.mu) == 0, f.last_error()
+    assert _rel(flow, g["flow"]) <= 1e-8
+    f.close()

@@ -111,3 +111,17 @@ def test_reset_values_need_an_update():
     with pytest.raises(FtsError):
         ls.surface_tension(inst.phi, {"Surface tension": 1.0, "Node density": 1.0})
     ls.close()
+
+
+def test_load_matches_golden_fixture():
+    """The committed surface-tension fixture (the oracle's load, 17^3 sphere)."""
+    from conftest import ROOT
+    from fluidtissue_gb300 import workloads as W
+    g = np.load(ROOT / "tests" / "golden" / "st_sphere_n17.npz")
+    xyz, tets, _ = W.kuhn_mesh(int(g["n"]), 0.0, 1)
+    ls = _ls(xyz, tets)
+    f = ls.surface_tension(g["phi"], {"Surface tension": 1.0, "Node density": 1.0},
+                           phi_reset=g["phi"])
+    assert ls.last_st_stats["interface_points"] == int(g["interface_points"])
+    assert _rel(f, g["force"]) <= TOL
+    ls.close()

@@ -442,3 +442,40 @@ def test_p2_load_partition_of_unity_and_hydrostatic_balance():
     p = flow[3 * npn:]
     x = inst.xyz[:, 0].astype(np.float64)
     assert np.abs((p - p.mean()) - (x - x.mean())).max() <= 1e-6
+
+
+def _golden_module():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mk", ROOT / "tests/golden/make_golden.py")
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    return mk
+
+
+def test_golden_p2_fixture():
+    """The oracle's P2-P1 solve reproduces the committed fixture."""
+    from fluidtissue_gb300 import workloads as W
+    mk = _golden_module()
+    g = np.load(ROOT / "tests" / "golden" / "p2_sphere17_n7.npz")
+    inst = W.WORKLOADS[str(g["name"])](int(g["n"]))
+    assert mk.mesh_hash(inst.xyz, inst.tets) == str(g["mesh_sha256"])
+    par = dict(inst.params, **{"Stokes velocity degree": 2.0})
+    flow, _, F = O.p2_flow(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source, inst.mu,
+                           par)
+    assert np.allclose(F, g["F"], rtol=0, atol=1e-13 * np.abs(g["F"]).max())
+    assert np.linalg.norm(flow - g["flow"]) <= 1e-10 * np.linalg.norm(g["flow"])
+
+
+def test_golden_surface_tension_fixture():
+    """The oracle's surface-tension load reproduces the committed fixture
+    (float arithmetic: to 1e-6 of the largest nodal value)."""
+    from fluidtissue_gb300 import workloads as W
+    mk = _golden_module()
+    g = np.load(ROOT / "tests" / "golden" / "st_sphere_n17.npz")
+    xyz, tets, _ = W.kuhn_mesh(int(g["n"]), 0.0, 1)
+    assert mk.mesh_hash(xyz, tets) == str(g["mesh_sha256"])
+    f, nif, area = O.surface_tension(xyz, tets, g["phi"], g["phi"], 1.0, 1)
+    assert nif == int(g["interface_points"])
+    assert abs(area - float(g["area"])) <= 1e-9 * float(g["area"])
+    assert np.abs(f - g["force"]).max() <= 1e-6 * np.abs(g["force"]).max()
+
