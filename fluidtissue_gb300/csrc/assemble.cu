@@ -381,7 +381,9 @@ void launch_assemble(Ctx& c) {
 }
 
 void ensure_bsr64(Ctx& c) {
-    if (!c.a64_valid && !c.matfree) launch_assemble(c);
+    if (c.a64_valid || c.matfree) return;
+    if (c.p2) launch_assemble_p2(c);
+    else launch_assemble(c);
 }
 
 // ---------------------------------------------------------------------------
