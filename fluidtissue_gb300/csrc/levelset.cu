@@ -39,6 +39,7 @@ constexpr int kLsThreads = 256;
 struct LsConst {
     double phi[4][4];  // float-rounded basis table phi[a][q]
     double qw;
+    double mq[4][4];   // qw sum_q phi_a(q) phi_j(q)
 };
 
 static LsConst ls_const() {
@@ -46,6 +47,12 @@ static LsConst ls_const() {
     LsConst c;
     std::memcpy(c.phi, R.phi, sizeof(c.phi));
     c.qw = 0.25 / 6.0;
+    for (int a = 0; a < 4; ++a)
+        for (int j = 0; j < 4; ++j) {
+            double s = 0.0;
+            for (int q = 0; q < 4; ++q) s += R.phi[a][q] * R.phi[j][q];
+            c.mq[a][j] = c.qw * s;
+        }
     return c;
 }
 
@@ -121,18 +128,74 @@ __device__ __forceinline__ double ls_integ(const double f[4], double qw, double 
     return ((f[0] * qw + f[2] * qw) + (f[1] * qw + f[3] * qw)) * detB;
 }
 
+// Row slot of every (node-element entry, column node b): slots[4 e + b] =
+// position of the element's node b in the row of the entry's node, minus the
+// row start (rows of at most 255 entries), once per mesh.
+__global__ void k_ls_slots(int64_t np, const int32_t* __restrict__ rowptr,
+                           const int32_t* __restrict__ cols, const int32_t* __restrict__ p2t_ptr,
+                           const uint32_t* __restrict__ p2t, const int32_t* __restrict__ tets,
+                           uint8_t* __restrict__ slots) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t r0 = rowptr[i], r1 = rowptr[i + 1];
+        for (int32_t e = p2t_ptr[i]; e < p2t_ptr[i + 1]; ++e) {
+            const int4 tt = reinterpret_cast<const int4*>(tets)[p2t[e] >> 2];
+            const int ids[4] = {tt.x, tt.y, tt.z, tt.w};
+            for (int b = 0; b < 4; ++b) {
+                int32_t slot = r0;
+                while (slot < r1 && cols[slot] != ids[b]) ++slot;
+                slots[4 * (int64_t)e + b] = (uint8_t)(slot - r0);
+            }
+        }
+    }
+}
+
 // Row gather of M (flow == NULL) or A (nodal velocity `flow`), one thread per
-// node, from the stored element geometry.
+// node, from the stored element geometry.  With slots (k_ls_slots) the
+// advection entries use the regrouped exact sum
+//   int phi_a (V . grad phi_b) = |det B| sum_c (grad phi_b)_c sum_j V_jc mq[a][j]
+// (V interpolated with the same float-rounded table: the quadrature sum
+// reordered, 24 FMAs per node-element pair) and M_ab = |det B| mq[a][b];
+// without, the reference's per-point expressions and a row search.
 __global__ void k_ls_assemble(int64_t np, const int32_t* __restrict__ rowptr,
                               const int32_t* __restrict__ cols,
                               const int32_t* __restrict__ p2t_ptr,
                               const uint32_t* __restrict__ p2t, const int32_t* __restrict__ tets,
                               const LsGeom* __restrict__ geom, const double* __restrict__ flow,
-                              LsConst K, double* __restrict__ out) {
+                              LsConst K, const uint8_t* __restrict__ slots,
+                              double* __restrict__ out) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t r0 = rowptr[i], r1 = rowptr[i + 1];
         for (int32_t q = r0; q < r1; ++q) out[q] = 0.0;
+        if (slots) {
+            for (int32_t e = p2t_ptr[i]; e < p2t_ptr[i + 1]; ++e) {
+                const uint32_t pe = p2t[e];
+                const int64_t k = pe >> 2;
+                const int a = pe & 3;
+                const LsGeom& G = geom[k];
+                const double detB = G.detB;
+                const uint32_t sl = reinterpret_cast<const uint32_t*>(slots)[e];
+                if (flow) {
+                    const int4 tt = reinterpret_cast<const int4*>(tets)[k];
+                    const int ids[4] = {tt.x, tt.y, tt.z, tt.w};
+                    double W[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) W[c] += K.mq[a][j] * flow[ids[j] + c * np];
+#pragma unroll
+                    for (int b = 0; b < 4; ++b)
+                        out[r0 + ((sl >> (8 * b)) & 255u)] +=
+                            detB * (G.g[b][0] * W[0] + G.g[b][1] * W[1] + G.g[b][2] * W[2]);
+                } else {
+#pragma unroll
+                    for (int b = 0; b < 4; ++b)
+                        out[r0 + ((sl >> (8 * b)) & 255u)] += detB * K.mq[a][b];
+                }
+            }
+            continue;
+        }
         for (int32_t e = p2t_ptr[i]; e < p2t_ptr[i + 1]; ++e) {
             const uint32_t pe = p2t[e];
             const int64_t k = pe >> 2;
@@ -638,6 +701,7 @@ struct fts_ls {
     int32_t* p2t_ptr = nullptr;
     uint32_t* p2t = nullptr;
     LsGeom* geom = nullptr;
+    uint8_t* slots = nullptr;  // [4 * 4 nt] row offsets (NULL: rows too long)
     double* M = nullptr;
     double* A = nullptr;
     double* L = nullptr;
@@ -679,7 +743,8 @@ T* ls_alloc(size_t n) {
 }
 
 void ls_free(fts_ls& S) {
-    void* ptrs[] = {S.xyz, S.tets, S.rowptr, S.cols, S.p2t_ptr, S.p2t, S.geom, S.M, S.A, S.L,
+    void* ptrs[] = {S.xyz, S.tets, S.rowptr, S.cols, S.p2t_ptr, S.p2t, S.geom, S.slots, S.M, S.A,
+                    S.L,
                     S.flow, S.phi, S.keep, S.ifp, S.count, S.flag, S.norm2, S.S,
                     S.red.partials, S.red.ticket, S.st_phi, S.st_ifn, S.st_ge, S.st_nrm,
                     S.st_gn, S.st_k, S.st_area, S.st_force, S.st_acc};
@@ -762,8 +827,14 @@ int fts_ls_create(const fts_mesh* mesh, int32_t device, fts_ls** out) {
         FTS_CUDA(cudaMemset(S->flag, 0, sizeof(int)));
         k_ls_geometry<<<grid_of(*S, S->nt), kLsThreads, 0, S->stream>>>(S->nt, S->tets, S->xyz,
                                                                          S->geom, S->flag);
+        if (T.max_row <= 255) {
+            S->slots = ls_alloc<uint8_t>(16 * (size_t)S->nt);
+            k_ls_slots<<<grid_of(*S, S->np), kLsThreads, 0, S->stream>>>(
+                S->np, S->rowptr, S->cols, S->p2t_ptr, S->p2t, S->tets, S->slots);
+        }
         k_ls_assemble<<<grid_of(*S, S->np), kLsThreads, 0, S->stream>>>(
-            S->np, S->rowptr, S->cols, S->p2t_ptr, S->p2t, S->tets, S->geom, nullptr, K, S->M);
+            S->np, S->rowptr, S->cols, S->p2t_ptr, S->p2t, S->tets, S->geom, nullptr, K, S->slots,
+            S->M);
         int bad = 0;
         FTS_CUDA(cudaMemcpyAsync(&bad, S->flag, sizeof(int), cudaMemcpyDeviceToHost, S->stream));
         FTS_CUDA(cudaStreamSynchronize(S->stream));
@@ -844,7 +915,7 @@ int fts_ls_update(fts_ls* S, const fts_ls_params* P, const double* flow, double*
         double* ifn = S->vec[11];
         FTS_CUDA(cudaEventRecord(S->ev[0], s));
         k_ls_assemble<<<g, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->p2t_ptr, S->p2t,
-                                               S->tets, S->geom, S->flow, K, S->A);
+                                               S->tets, S->geom, S->flow, K, S->slots, S->A);
         k_ls_system<<<g, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->M, S->A, 0.5 * P->dt,
                                              S->phi, S->L, b, inv, x);
         FTS_CUDA(cudaEventRecord(S->ev[1], s));
