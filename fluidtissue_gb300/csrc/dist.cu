@@ -5,13 +5,14 @@
 // (O(np * n_ifp), every point re-read from global memory by every thread).
 // Here the points are sorted along a Morton curve (host, once per call) into
 // blocks of 32 with bounding boxes, and blocks of 32 blocks with their own
-// boxes; a thread scans only the blocks whose box is closer than its current
-// best.  The first pass finds the minimum squared distance in float; a
-// second pass re-evaluates every point within a relative margin of that
-// minimum with norm3df, the reference's distance, so the result is the same
-// float as the exhaustive minimum of norm3df values (the margin covers the
-// few-ulp difference between the squared-distance order and the norm3df
-// order).  The exhaustive kernel (the reference's algorithm) is kept for
+// boxes; the nodes are taken in Morton order (once per mesh) by CTAs of 256,
+// which share a sorted candidate list of blocks (k_dist_cta), and a thread
+// scans only the candidate blocks whose box is closer than its current best.
+// The first pass finds the minimum squared distance in float; a second pass
+// re-evaluates every point within a relative margin of that minimum with
+// norm3df, the reference's distance, so the result is the same float as the
+// exhaustive minimum of norm3df values (the margin covers the few-ulp
+// difference between the squared-distance order and the norm3df order).  The exhaustive kernel (the reference's algorithm) is kept for
 // comparison and for bit-exact parity tests.
 #include <algorithm>
 #include <cfloat>
@@ -61,17 +62,15 @@ __global__ void k_dist_exhaustive(int64_t np, const float* __restrict__ xyz,
     }
 }
 
-// Pruned search.  pts: sorted points (x, y, z, 0); blo/bhi: block boxes;
-// slo/shi: super-block boxes; nb blocks, ns super-blocks.
-__global__ void __launch_bounds__(256)
-k_dist_pruned(int64_t np, const float* __restrict__ xyz, const float4* __restrict__ pts,
-              int32_t n_ifp, const float4* __restrict__ blo, const float4* __restrict__ bhi,
-              int32_t nb, const float4* __restrict__ slo, const float4* __restrict__ shi,
-              int32_t ns, double* __restrict__ phi, unsigned long long* __restrict__ scanned) {
-    unsigned long long mine = 0;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < np;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        const float px = xyz[3 * k], py = xyz[3 * k + 1], pz = xyz[3 * k + 2];
+// Per-node pruned search over all super-blocks (the fallback of k_dist_cta
+// when a CTA's candidate list overflows).  pts: sorted points (x, y, z, 0);
+// blo/bhi: block boxes; slo/shi: super-block boxes; nb blocks, ns super-blocks.
+__device__ float pruned_node(float px, float py, float pz, const float4* __restrict__ pts,
+                             int32_t n_ifp, const float4* __restrict__ blo,
+                             const float4* __restrict__ bhi, int32_t nb,
+                             const float4* __restrict__ slo, const float4* __restrict__ shi,
+                             int32_t ns, unsigned long long& mine) {
+    {
         float best = FLT_MAX;
         // seed: the super-block with the nearest box first
         int32_t s0 = 0;
@@ -120,9 +119,182 @@ k_dist_pruned(int64_t np, const float* __restrict__ xyz, const float4* __restric
                 }
             }
         }
-        double out = dmin;
-        if (phi[k] < 0.0f) out = -out;
-        phi[k] = out;
+        return dmin;
+    }
+}
+
+// Cooperative pruned search.  Each CTA takes 256 nodes in Morton order (a
+// compact brick), so their candidate points are shared: the CTA bounds its
+// nodes' box, gets an upper bound U of every node's nearest squared distance
+// from the block nearest to the box, keeps the blocks whose box lies within
+// U (1 + margin) of the node box, sorts them by that distance (bitonic, in
+// shared memory) and each thread walks the sorted list until the box
+// distance passes its own best.  Pass 1 and pass 2 are those of the
+// per-node search (same expressions), so the result is the same float.
+constexpr int kCtaNodes = 256;
+constexpr int kCandCap = 2048;
+
+__device__ __forceinline__ float boxbox_dist2(float4 alo, float4 ahi, float4 blo, float4 bhi) {
+    const float dx = fmaxf(fmaxf(blo.x - ahi.x, alo.x - bhi.x), 0.f);
+    const float dy = fmaxf(fmaxf(blo.y - ahi.y, alo.y - bhi.y), 0.f);
+    const float dz = fmaxf(fmaxf(blo.z - ahi.z, alo.z - bhi.z), 0.f);
+    return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
+__global__ void __launch_bounds__(kCtaNodes)
+k_dist_cta(int64_t np, const int32_t* __restrict__ order, const float* __restrict__ xyz,
+           const float4* __restrict__ pts, int32_t n_ifp, const float4* __restrict__ blo,
+           const float4* __restrict__ bhi, int32_t nb, const float4* __restrict__ slo,
+           const float4* __restrict__ shi, int32_t ns, double* __restrict__ phi,
+           unsigned long long* __restrict__ scanned) {
+    __shared__ unsigned long long cand[kCandCap];
+    __shared__ unsigned long long seed;
+    __shared__ unsigned int ubits;
+    __shared__ int ncand;
+    __shared__ unsigned kmin[3], kmax[3];  // node box as order-preserving keys
+    __shared__ float bmin[3], bmax[3];
+    unsigned long long mine = 0;
+    const int64_t nchunks = (np + kCtaNodes - 1) / kCtaNodes;
+    for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int64_t slot = c * kCtaNodes + threadIdx.x;
+        const bool active = slot < np;
+        const int32_t k = active ? order[slot] : 0;
+        const float px = active ? xyz[3 * (int64_t)k] : 0.f;
+        const float py = active ? xyz[3 * (int64_t)k + 1] : 0.f;
+        const float pz = active ? xyz[3 * (int64_t)k + 2] : 0.f;
+        if (threadIdx.x == 0) {
+            for (int a = 0; a < 3; ++a) {
+                kmin[a] = 0xffffffffu;
+                kmax[a] = 0u;
+            }
+            seed = ~0ull;
+            ubits = 0u;
+            ncand = 0;
+        }
+        __syncthreads();
+        // node box: the float bits with the sign folded (negatives inverted,
+        // positives with the top bit set) order like the numbers
+        if (active) {
+            const float p[3] = {px, py, pz};
+            for (int a = 0; a < 3; ++a) {
+                const unsigned u = __float_as_uint(p[a]);
+                const unsigned key = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+                atomicMin(&kmin[a], key);
+                atomicMax(&kmax[a], key);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            const unsigned a = kmin[threadIdx.x], b = kmax[threadIdx.x];
+            bmin[threadIdx.x] = __uint_as_float((a & 0x80000000u) ? (a & 0x7fffffffu) : ~a);
+            bmax[threadIdx.x] = __uint_as_float((b & 0x80000000u) ? (b & 0x7fffffffu) : ~b);
+        }
+        __syncthreads();
+        const float4 clo = make_float4(bmin[0], bmin[1], bmin[2], 0.f);
+        const float4 chi = make_float4(bmax[0], bmax[1], bmax[2], 0.f);
+        // seed: the block nearest to the node box
+        for (int32_t b = threadIdx.x; b < nb; b += blockDim.x) {
+            const float d = boxbox_dist2(clo, chi, __ldg(blo + b), __ldg(bhi + b));
+            atomicMin(&seed, ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)b);
+        }
+        __syncthreads();
+        float best = FLT_MAX;
+        if (active) {
+            const int32_t b = (int32_t)(seed & 0xffffffffull);
+            const int32_t j1 = min(n_ifp, (b + 1) * kDistBlock);
+            for (int32_t j = b * kDistBlock; j < j1; ++j) {
+                const float4 q = __ldg(pts + j);
+                const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+                best = fminf(best, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+            }
+            mine += (unsigned long long)(j1 - b * kDistBlock);
+            atomicMax(&ubits, __float_as_uint(best));  // non-negative: bits order
+        }
+        __syncthreads();
+        const float U = __uint_as_float(ubits) * (1.f + kDistMargin);
+        // candidates: super-blocks, then their blocks, within U of the node box
+        for (int32_t t = threadIdx.x; t < ns; t += blockDim.x) {
+            if (boxbox_dist2(clo, chi, __ldg(slo + t), __ldg(shi + t)) > U) continue;
+            const int32_t b1 = min(nb, (t + 1) * kDistSuper);
+            for (int32_t b = t * kDistSuper; b < b1; ++b) {
+                const float d = boxbox_dist2(clo, chi, __ldg(blo + b), __ldg(bhi + b));
+                if (d > U) continue;
+                const int at = atomicAdd(&ncand, 1);
+                if (at < kCandCap)
+                    cand[at] = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)b;
+            }
+        }
+        __syncthreads();
+        const int nc = ncand;
+        if (nc > kCandCap) {  // too many: the per-node search for this chunk
+            if (active) {
+                const float d = pruned_node(px, py, pz, pts, n_ifp, blo, bhi, nb, slo, shi, ns,
+                                            mine);
+                double out = d;
+                if (phi[k] < 0.0f) out = -out;
+                phi[k] = out;
+            }
+            __syncthreads();
+            continue;
+        }
+        // bitonic sort of the candidates (padded to a power of two)
+        int m = 1;
+        while (m < nc) m <<= 1;
+        for (int i = nc + threadIdx.x; i < m; i += blockDim.x) cand[i] = ~0ull;
+        __syncthreads();
+        for (int kk = 2; kk <= m; kk <<= 1)
+            for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+                for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                    const int l = i ^ jj;
+                    if (l > i) {
+                        const unsigned long long a = cand[i], b = cand[l];
+                        const bool up = (i & kk) == 0;
+                        if ((a > b) == up) {
+                            cand[i] = b;
+                            cand[l] = a;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        if (active) {
+            // pass 1: minimum squared distance over the sorted candidates
+            for (int i = 0; i < nc; ++i) {
+                const unsigned long long key = cand[i];
+                if (__uint_as_float((unsigned)(key >> 32)) > best) break;
+                const int32_t b = (int32_t)(key & 0xffffffffull);
+                if (box_dist2(__ldg(blo + b), __ldg(bhi + b), px, py, pz) > best) continue;
+                const int32_t j1 = min(n_ifp, (b + 1) * kDistBlock);
+                for (int32_t j = b * kDistBlock; j < j1; ++j) {
+                    const float4 q = __ldg(pts + j);
+                    const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+                    best = fminf(best, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+                }
+                mine += (unsigned long long)(j1 - b * kDistBlock);
+            }
+            // pass 2: norm3df over the points within the margin of the minimum
+            const float thr = best * (1.f + kDistMargin);
+            float dmin = FLT_MAX;
+            for (int i = 0; i < nc; ++i) {
+                const unsigned long long key = cand[i];
+                if (__uint_as_float((unsigned)(key >> 32)) > thr) break;
+                const int32_t b = (int32_t)(key & 0xffffffffull);
+                if (box_dist2(__ldg(blo + b), __ldg(bhi + b), px, py, pz) > thr) continue;
+                const int32_t j1 = min(n_ifp, (b + 1) * kDistBlock);
+                for (int32_t j = b * kDistBlock; j < j1; ++j) {
+                    const float4 q = __ldg(pts + j);
+                    const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+                    if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= thr) {
+                        const float d = norm3df(dx, dy, dz);
+                        if (d < dmin) dmin = d;
+                    }
+                }
+            }
+            double out = dmin;
+            if (phi[k] < 0.0f) out = -out;
+            phi[k] = out;
+        }
+        __syncthreads();
     }
     for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
     if ((threadIdx.x & 31) == 0 && mine) atomicAdd(scanned, mine);
@@ -138,6 +310,7 @@ struct fts_dist {
     cudaStream_t stream = nullptr;
     int64_t np = 0;
     float* xyz = nullptr;
+    int32_t* order = nullptr;  // nodes in Morton order of their coordinates
     double* phi = nullptr;
     float* buf = nullptr;     // points: sorted float4 (pruned) or the raw float3 list
     size_t buf_cap = 0;       // floats
@@ -149,7 +322,7 @@ struct fts_dist {
 namespace {
 
 void dist_free(fts_dist& D) {
-    for (void* p : {(void*)D.xyz, (void*)D.phi, (void*)D.buf, (void*)D.scanned})
+    for (void* p : {(void*)D.xyz, (void*)D.order, (void*)D.phi, (void*)D.buf, (void*)D.scanned})
         if (p) cudaFree(p);
     for (auto& e : D.ev)
         if (e) cudaEventDestroy(e);
@@ -264,8 +437,10 @@ void dist_reset_device(fts_dist* D, const float* ifp, int32_t n_ifp, double* phi
         const float4* bhi = blo + nb;
         const float4* slo = bhi + nb;
         const float4* shi = slo + ns;
-        k_dist_pruned<<<grid, 256, 0, s>>>(np, D->xyz, pts, n_ifp, blo, bhi, nb, slo, shi, ns,
-                                           phi_dev, D->scanned);
+        const int cgrid = (int)std::min<int64_t>((np + kCtaNodes - 1) / kCtaNodes,
+                                                 (int64_t)D->num_sms * 8);
+        k_dist_cta<<<cgrid, kCtaNodes, 0, s>>>(np, D->order, D->xyz, pts, n_ifp, blo, bhi, nb,
+                                               slo, shi, ns, phi_dev, D->scanned);
     }
     FTS_CUDA(cudaGetLastError());
     FTS_CUDA(cudaEventRecord(D->ev[1], s));
@@ -302,6 +477,30 @@ int fts_dist_create(const float* xyz, int64_t np, int32_t device, fts_dist** out
         FTS_CUDA(cudaMalloc(&D->phi, np * sizeof(double)));
         FTS_CUDA(cudaMalloc(&D->scanned, sizeof(unsigned long long)));
         FTS_CUDA(cudaMemcpy(D->xyz, xyz, 3 * np * sizeof(float), cudaMemcpyHostToDevice));
+        // the nodes in Morton order (once per mesh): a CTA's 256 nodes form a brick
+        {
+            float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            for (int64_t k = 0; k < np; ++k)
+                for (int c = 0; c < 3; ++c) {
+                    lo[c] = std::min(lo[c], xyz[3 * k + c]);
+                    hi[c] = std::max(hi[c], xyz[3 * k + c]);
+                }
+            std::vector<std::pair<uint32_t, int32_t>> key((size_t)np);
+            for (int64_t k = 0; k < np; ++k) {
+                uint32_t q[3];
+                for (int c = 0; c < 3; ++c) {
+                    const float w = hi[c] > lo[c] ? (xyz[3 * k + c] - lo[c]) / (hi[c] - lo[c]) : 0.f;
+                    q[c] = (uint32_t)std::min(1023.f, std::max(0.f, w * 1023.f));
+                }
+                key[k] = {spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2),
+                          (int32_t)k};
+            }
+            std::sort(key.begin(), key.end());
+            std::vector<int32_t> ord((size_t)np);
+            for (int64_t k = 0; k < np; ++k) ord[k] = key[k].second;
+            FTS_CUDA(cudaMalloc(&D->order, np * sizeof(int32_t)));
+            FTS_CUDA(cudaMemcpy(D->order, ord.data(), np * sizeof(int32_t), cudaMemcpyHostToDevice));
+        }
     } catch (const CudaError& e) {
         g_dist_error() = e.what;
         rc = e.code == cudaErrorMemoryAllocation ? FTS_ERR_OOM : FTS_ERR_CUDA;

@@ -59,3 +59,17 @@ def test_no_interface_point_gives_flt_max():
     out, _ = _reset(inst.xyz, np.zeros((0, 3), np.float32), inst.phi, "pruned")
     assert np.all(np.abs(out) == FLT_MAX)
     assert np.array_equal(out < 0, inst.phi < 0)
+
+
+def test_candidate_overflow_falls_back_exactly():
+    """A far shell of 70,000 points around the mesh: every block of 32 points
+    lies within the bound of every CTA's node box (more than the 2048 shared
+    candidates), so each CTA takes the per-node search; values stay those of
+    the reference algorithm."""
+    inst = workload("sphere65", 21)
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal((70000, 3))
+    shell = (0.5 + 50.0 * v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+    ex, _ = _reset(inst.xyz, shell, inst.phi, "exhaustive")
+    pr, _ = _reset(inst.xyz, shell, inst.phi, "pruned")
+    assert np.array_equal(pr, ex), np.abs(pr - ex).max()
