@@ -611,7 +611,7 @@ def run_dist(args):
             "pruned": pr, "reference_algorithm_on_gpu": out["exhaustive"],
             "pruned_equals_reference_algorithm": same,
             "kernel_speedup": round(out["exhaustive"]["ms_kernel"] / max(pr["ms_kernel"], 1e-9), 1),
-            "gpu_launches": 1, "clocks": pr.pop("clocks")}
+            "gpu_launches": 6, "clocks": pr.pop("clocks")}
     if rank == 0 and not args.no_cpu_baseline:
         sys.path.insert(0, str(ROOT / "oracle"))
         import oracle as O

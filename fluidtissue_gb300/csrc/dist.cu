@@ -3,9 +3,10 @@
 //
 // The reference runs one thread per mesh node over ALL interface points
 // (O(np * n_ifp), every point re-read from global memory by every thread).
-// Here the points are sorted along a Morton curve (host, once per call) into
-// blocks of 32 with bounding boxes, and blocks of 32 blocks with their own
-// boxes; the nodes are taken in Morton order (once per mesh) by CTAs of 256,
+// Here the points are binned on the device into the cells of a 64^3 grid
+// over their bounding box, cells in Morton order (a counting sort: histogram,
+// scan, scatter), and cut into blocks of 32 with bounding boxes, and blocks of
+// 32 blocks with their own boxes; the nodes are taken in Morton order (once per mesh) by CTAs of 256,
 // which share a sorted candidate list of blocks (k_dist_cta), and a thread
 // scans only the candidate blocks whose box is closer than its current best.
 // The first pass finds the minimum squared distance in float; a second pass
@@ -42,6 +43,167 @@ __device__ __forceinline__ float box_dist2(const float4 lo, const float4 hi, flo
     const float dy = fmaxf(fmaxf(lo.y - py, py - hi.y), 0.f);
     const float dz = fmaxf(fmaxf(lo.z - pz, pz - hi.z), 0.f);
     return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
+// 10-bit Morton interleave.
+__host__ __device__ __forceinline__ uint32_t spread10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+// Float bits with the sign folded (negatives inverted, positives with the top
+// bit set): unsigned order is the order of the numbers.
+__device__ __forceinline__ unsigned fkey(float f) {
+    const unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_inv(unsigned k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+constexpr int kCellBits = 6;  // cells per axis of the binning grid: 64
+constexpr int kCells = 1 << (3 * kCellBits);
+constexpr int kScanThreads = 1024;
+
+// Bounding box of the points: keys[0..2] minima, keys[3..5] maxima (set to
+// all ones / zero before).
+__global__ void k_pts_box(int32_t n, const float* __restrict__ raw, unsigned* __restrict__ keys) {
+    unsigned lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        for (int c = 0; c < 3; ++c) {
+            const unsigned k = fkey(raw[3 * (int64_t)j + c]);
+            lo[c] = min(lo[c], k);
+            hi[c] = max(hi[c], k);
+        }
+    for (int c = 0; c < 3; ++c) {
+        lo[c] = __reduce_min_sync(0xffffffffu, lo[c]);
+        hi[c] = __reduce_max_sync(0xffffffffu, hi[c]);
+    }
+    if ((threadIdx.x & 31) == 0)
+        for (int c = 0; c < 3; ++c) {
+            atomicMin(keys + c, lo[c]);
+            atomicMax(keys + 3 + c, hi[c]);
+        }
+}
+
+// Cell of each point (Morton code of its 6-bit grid coordinates) and the
+// cell histogram.
+__global__ void k_pts_cells(int32_t n, const float* __restrict__ raw,
+                            const unsigned* __restrict__ keys, uint32_t* __restrict__ cell,
+                            uint32_t* __restrict__ counts) {
+    float lo[3], sc[3];
+    for (int c = 0; c < 3; ++c) {
+        lo[c] = fkey_inv(keys[c]);
+        const float hi = fkey_inv(keys[3 + c]);
+        sc[c] = hi > lo[c] ? (float)(1 << kCellBits) / (hi - lo[c]) : 0.f;
+    }
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        uint32_t code = 0;
+        for (int c = 0; c < 3; ++c) {
+            const float w = (raw[3 * (int64_t)j + c] - lo[c]) * sc[c];
+            const uint32_t q = (uint32_t)fminf(fmaxf(w, 0.f), (float)((1 << kCellBits) - 1));
+            code |= spread10(q) << c;
+        }
+        cell[j] = code;
+        atomicAdd(counts + code, 1u);
+    }
+}
+
+// Exclusive scan of the kCells counts in place, one CTA: each warp scans a
+// contiguous chunk of kCells / 32 counts in steps of 32 (coalesced), after the
+// chunk totals have been scanned across the warps.
+__global__ void __launch_bounds__(kScanThreads) k_cells_scan(uint32_t* __restrict__ counts) {
+    __shared__ uint32_t wsum[kScanThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    constexpr int kChunk = kCells / (kScanThreads / 32);
+    uint32_t* base = counts + (size_t)w * kChunk;
+    uint32_t t = 0;
+    for (int i = lane; i < kChunk; i += 32) t += base[i];
+    t = __reduce_add_sync(0xffffffffu, t);
+    if (lane == 0) wsum[w] = t;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t v = wsum[lane], x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        wsum[lane] = x - v;  // exclusive
+    }
+    __syncthreads();
+    uint32_t carry = wsum[w];
+    for (int i0 = 0; i0 < kChunk; i0 += 32) {
+        const uint32_t v = base[i0 + lane];
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        base[i0 + lane] = carry + x - v;
+        carry += __shfl_sync(0xffffffffu, x, 31);
+    }
+}
+
+// Scatter the points to their cell's range (order within a cell is that of
+// the atomics: the minimum over a fixed set does not depend on it).
+__global__ void k_pts_scatter(int32_t n, const float* __restrict__ raw,
+                              const uint32_t* __restrict__ cell, uint32_t* __restrict__ cursor,
+                              float4* __restrict__ pts) {
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t at = atomicAdd(cursor + cell[j], 1u);
+        pts[at] = make_float4(raw[3 * (int64_t)j], raw[3 * (int64_t)j + 1],
+                              raw[3 * (int64_t)j + 2], 0.f);
+    }
+}
+
+// Block and super-block boxes: one warp per super-block, one lane per point
+// of each of its blocks.
+__global__ void k_block_boxes(int32_t n, const float4* __restrict__ pts, int32_t nb, int32_t ns,
+                              float4* __restrict__ blo, float4* __restrict__ bhi,
+                              float4* __restrict__ slo, float4* __restrict__ shi) {
+    const int lane = threadIdx.x & 31;
+    for (int32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ns;
+         t += (gridDim.x * blockDim.x) >> 5) {
+        float4 sl = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f);
+        float4 sh = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
+        const int32_t b1 = min(nb, (t + 1) * 32);
+        for (int32_t b = t * 32; b < b1; ++b) {
+            const int32_t j = b * 32 + lane;
+            float4 l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f);
+            float4 h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
+            if (j < n) {
+                l = pts[j];
+                h = l;
+                l.w = h.w = 0.f;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                l.x = fminf(l.x, __shfl_xor_sync(0xffffffffu, l.x, o));
+                l.y = fminf(l.y, __shfl_xor_sync(0xffffffffu, l.y, o));
+                l.z = fminf(l.z, __shfl_xor_sync(0xffffffffu, l.z, o));
+                h.x = fmaxf(h.x, __shfl_xor_sync(0xffffffffu, h.x, o));
+                h.y = fmaxf(h.y, __shfl_xor_sync(0xffffffffu, h.y, o));
+                h.z = fmaxf(h.z, __shfl_xor_sync(0xffffffffu, h.z, o));
+            }
+            if (lane == 0) {
+                blo[b] = l;
+                bhi[b] = h;
+            }
+            sl.x = fminf(sl.x, l.x);
+            sl.y = fminf(sl.y, l.y);
+            sl.z = fminf(sl.z, l.z);
+            sh.x = fmaxf(sh.x, h.x);
+            sh.y = fmaxf(sh.y, h.y);
+            sh.z = fmaxf(sh.z, h.z);
+        }
+        if (lane == 0) {
+            slo[t] = sl;
+            shi[t] = sh;
+        }
+    }
 }
 
 // The reference's kernel, restated: every node against every point.
@@ -172,22 +334,18 @@ k_dist_cta(int64_t np, const int32_t* __restrict__ order, const float* __restric
             ncand = 0;
         }
         __syncthreads();
-        // node box: the float bits with the sign folded (negatives inverted,
-        // positives with the top bit set) order like the numbers
+        // node box
         if (active) {
             const float p[3] = {px, py, pz};
             for (int a = 0; a < 3; ++a) {
-                const unsigned u = __float_as_uint(p[a]);
-                const unsigned key = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-                atomicMin(&kmin[a], key);
-                atomicMax(&kmax[a], key);
+                atomicMin(&kmin[a], fkey(p[a]));
+                atomicMax(&kmax[a], fkey(p[a]));
             }
         }
         __syncthreads();
         if (threadIdx.x < 3) {
-            const unsigned a = kmin[threadIdx.x], b = kmax[threadIdx.x];
-            bmin[threadIdx.x] = __uint_as_float((a & 0x80000000u) ? (a & 0x7fffffffu) : ~a);
-            bmax[threadIdx.x] = __uint_as_float((b & 0x80000000u) ? (b & 0x7fffffffu) : ~b);
+            bmin[threadIdx.x] = fkey_inv(kmin[threadIdx.x]);
+            bmax[threadIdx.x] = fkey_inv(kmax[threadIdx.x]);
         }
         __syncthreads();
         const float4 clo = make_float4(bmin[0], bmin[1], bmin[2], 0.f);
@@ -312,42 +470,43 @@ struct fts_dist {
     float* xyz = nullptr;
     int32_t* order = nullptr;  // nodes in Morton order of their coordinates
     double* phi = nullptr;
-    float* buf = nullptr;     // points: sorted float4 (pruned) or the raw float3 list
-    size_t buf_cap = 0;       // floats
+    int64_t cap = 0;            // points the buffers below hold
+    float* raw = nullptr;       // [3 cap] points as the caller gave them (host uploads)
+    uint32_t* cell = nullptr;   // [cap] binning cell of each point
+    float4* pts = nullptr;      // [cap] points binned by cell
+    float4* boxes = nullptr;    // block boxes lo[nbc], hi[nbc], super-block lo[nsc], hi[nsc]
+    uint32_t* counts = nullptr; // [kCells] cell histogram, then cursors
+    unsigned* keys = nullptr;   // [6] bounding box of the points as order keys
     unsigned long long* scanned = nullptr;
-    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     std::string last_error;
 };
 
 namespace {
 
 void dist_free(fts_dist& D) {
-    for (void* p : {(void*)D.xyz, (void*)D.order, (void*)D.phi, (void*)D.buf, (void*)D.scanned})
+    for (void* p : {(void*)D.xyz, (void*)D.order, (void*)D.phi, (void*)D.raw, (void*)D.cell,
+                    (void*)D.pts, (void*)D.boxes, (void*)D.counts, (void*)D.keys,
+                    (void*)D.scanned})
         if (p) cudaFree(p);
     for (auto& e : D.ev)
         if (e) cudaEventDestroy(e);
     if (D.stream) cudaStreamDestroy(D.stream);
 }
 
-// 10-bit Morton interleave of (x, y, z) quantised to the box.
-uint32_t spread10(uint32_t v) {
-    v &= 0x3ffu;
-    v = (v | (v << 16)) & 0x030000ffu;
-    v = (v | (v << 8)) & 0x0300f00fu;
-    v = (v | (v << 4)) & 0x030c30c3u;
-    v = (v | (v << 2)) & 0x09249249u;
-    return v;
-}
-
 }  // namespace
 
 namespace fts {
 
-// The reset on device-resident phi (stream-ordered, no host wait): host sort
-// of the points, upload, kernel.  Records the kernel between D->ev[0] and
-// D->ev[1]; points_scanned is read back only by the caller that waits.
-void dist_reset_device(fts_dist* D, const float* ifp, int32_t n_ifp, double* phi_dev,
-                       int32_t method, cudaStream_t s, fts_dist_stats* st) {
+static int64_t blocks_for(int64_t n) { return (n + kDistBlock - 1) / kDistBlock; }
+static int64_t supers_for(int64_t n) { return (blocks_for(n) + kDistSuper - 1) / kDistSuper; }
+
+// The reset on device-resident phi, stream-ordered: the points (host or
+// device, ifp_on_device) are binned on the device and searched; no host wait
+// unless the buffers grow or st asks for the scan count.  Events: D->ev[0]
+// before the binning, D->ev[1] before the search kernel, D->ev[2] after it.
+void dist_reset_device(fts_dist* D, const float* ifp, bool ifp_on_device, int32_t n_ifp,
+                       double* phi_dev, int32_t method, cudaStream_t s, fts_dist_stats* st) {
     const int64_t np = D->np;
     const int grid = (int)std::min<int64_t>((np + 255) / 256, (int64_t)D->num_sms * 8);
     if (n_ifp == 0) {  // the reference's minimum over no point: FLT_MAX
@@ -356,99 +515,69 @@ void dist_reset_device(fts_dist* D, const float* ifp, int32_t n_ifp, double* phi
         return;
     }
     const double t0 = wall_ms();
-    int32_t nb = 0, ns = 0;
-    size_t need = 0;
-    std::vector<float> host;
-    if (method == FTS_DIST_EXHAUSTIVE) {
-        need = 3 * (size_t)n_ifp;
-    } else {
-        // Morton order of the points within their bounding box
-        float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-        for (int32_t j = 0; j < n_ifp; ++j)
-            for (int c = 0; c < 3; ++c) {
-                lo[c] = std::min(lo[c], ifp[3 * j + c]);
-                hi[c] = std::max(hi[c], ifp[3 * j + c]);
-            }
-        std::vector<std::pair<uint32_t, int32_t>> key(n_ifp);
-        for (int32_t j = 0; j < n_ifp; ++j) {
-            uint32_t q[3];
-            for (int c = 0; c < 3; ++c) {
-                const float w = hi[c] > lo[c] ? (ifp[3 * j + c] - lo[c]) / (hi[c] - lo[c]) : 0.f;
-                q[c] = (uint32_t)std::min(1023.f, std::max(0.f, w * 1023.f));
-            }
-            key[j] = {spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2), j};
-        }
-        std::sort(key.begin(), key.end());
-        nb = (n_ifp + kDistBlock - 1) / kDistBlock;
-        ns = (nb + kDistSuper - 1) / kDistSuper;
-        // layout: pts[n_ifp] float4, blo[nb], bhi[nb], slo[ns], shi[ns] (float4 each)
-        need = 4 * ((size_t)n_ifp + 2 * (size_t)nb + 2 * (size_t)ns);
-        host.assign(need, 0.f);
-        float* pts = host.data();
-        float* blo = pts + 4 * (size_t)n_ifp;
-        float* bhi = blo + 4 * (size_t)nb;
-        float* slo = bhi + 4 * (size_t)nb;
-        float* shi = slo + 4 * (size_t)ns;
-        for (int32_t j = 0; j < n_ifp; ++j)
-            for (int c = 0; c < 3; ++c) pts[4 * j + c] = ifp[3 * key[j].second + c];
-        for (int32_t b = 0; b < nb; ++b) {
-            for (int c = 0; c < 3; ++c) {
-                blo[4 * b + c] = FLT_MAX;
-                bhi[4 * b + c] = -FLT_MAX;
-            }
-            for (int32_t j = b * kDistBlock; j < std::min(n_ifp, (b + 1) * kDistBlock); ++j)
-                for (int c = 0; c < 3; ++c) {
-                    blo[4 * b + c] = std::min(blo[4 * b + c], pts[4 * j + c]);
-                    bhi[4 * b + c] = std::max(bhi[4 * b + c], pts[4 * j + c]);
-                }
-        }
-        for (int32_t t = 0; t < ns; ++t) {
-            for (int c = 0; c < 3; ++c) {
-                slo[4 * t + c] = FLT_MAX;
-                shi[4 * t + c] = -FLT_MAX;
-            }
-            for (int32_t b = t * kDistSuper; b < std::min(nb, (t + 1) * kDistSuper); ++b)
-                for (int c = 0; c < 3; ++c) {
-                    slo[4 * t + c] = std::min(slo[4 * t + c], blo[4 * b + c]);
-                    shi[4 * t + c] = std::max(shi[4 * t + c], bhi[4 * b + c]);
-                }
-        }
-    }
-    if (need > D->buf_cap) {
-        // the previous contents may still be read by queued work: wait first
+    if (n_ifp > D->cap) {
+        // the previous buffers may still be read by queued work: wait first
         FTS_CUDA(cudaStreamSynchronize(s));
-        if (D->buf) cudaFree(D->buf);
-        D->buf = nullptr;
-        FTS_CUDA(cudaMalloc(&D->buf, need * sizeof(float)));
-        D->buf_cap = need;
+        for (void** p : {(void**)&D->raw, (void**)&D->cell, (void**)&D->pts, (void**)&D->boxes}) {
+            if (*p) cudaFree(*p);
+            *p = nullptr;
+        }
+        D->cap = 0;
+        // room to grow by a quarter (the interface point count drifts per step)
+        const int64_t cap = n_ifp + n_ifp / 4;
+        FTS_CUDA(cudaMalloc(&D->raw, 3 * (size_t)cap * sizeof(float)));
+        FTS_CUDA(cudaMalloc(&D->cell, (size_t)cap * sizeof(uint32_t)));
+        FTS_CUDA(cudaMalloc(&D->pts, (size_t)cap * sizeof(float4)));
+        FTS_CUDA(cudaMalloc(&D->boxes, 2 * (size_t)(blocks_for(cap) + supers_for(cap)) * sizeof(float4)));
+        D->cap = cap;
     }
-    const float* src = method == FTS_DIST_EXHAUSTIVE ? ifp : host.data();
-    FTS_CUDA(cudaMemcpyAsync(D->buf, src, need * sizeof(float), cudaMemcpyHostToDevice, s));
-    // the pageable source must stay valid until the copy has been taken
-    if (method != FTS_DIST_EXHAUSTIVE) FTS_CUDA(cudaStreamSynchronize(s));
+    const float* raw = ifp;
+    if (!ifp_on_device) {  // pageable source: taken by the time the call returns
+        FTS_CUDA(cudaMemcpyAsync(D->raw, ifp, 3 * (size_t)n_ifp * sizeof(float),
+                                 cudaMemcpyHostToDevice, s));
+        raw = D->raw;
+    }
+    const int32_t nb = (int32_t)blocks_for(n_ifp), ns = (int32_t)supers_for(n_ifp);
+    const int64_t nbc = blocks_for(D->cap);
+    float4* blo = D->boxes;
+    float4* bhi = blo + nbc;
+    float4* slo = bhi + nbc;
+    float4* shi = slo + supers_for(D->cap);
     FTS_CUDA(cudaMemsetAsync(D->scanned, 0, sizeof(unsigned long long), s));
-    if (st) st->ms_setup = wall_ms() - t0;
     FTS_CUDA(cudaEventRecord(D->ev[0], s));
     if (method == FTS_DIST_EXHAUSTIVE) {
-        k_dist_exhaustive<<<grid, 256, 0, s>>>(np, D->xyz, D->buf, n_ifp, phi_dev);
+        FTS_CUDA(cudaEventRecord(D->ev[1], s));
+        k_dist_exhaustive<<<grid, 256, 0, s>>>(np, D->xyz, raw, n_ifp, phi_dev);
     } else {
-        const float4* pts = reinterpret_cast<const float4*>(D->buf);
-        const float4* blo = pts + n_ifp;
-        const float4* bhi = blo + nb;
-        const float4* slo = bhi + nb;
-        const float4* shi = slo + ns;
+        const int pgrid = (int)std::min<int64_t>((n_ifp + 255) / 256, (int64_t)D->num_sms * 4);
+        FTS_CUDA(cudaMemsetAsync(D->keys, 0xff, 3 * sizeof(unsigned), s));
+        FTS_CUDA(cudaMemsetAsync(D->keys + 3, 0, 3 * sizeof(unsigned), s));
+        FTS_CUDA(cudaMemsetAsync(D->counts, 0, kCells * sizeof(uint32_t), s));
+        k_pts_box<<<pgrid, 256, 0, s>>>(n_ifp, raw, D->keys);
+        k_pts_cells<<<pgrid, 256, 0, s>>>(n_ifp, raw, D->keys, D->cell, D->counts);
+        k_cells_scan<<<1, kScanThreads, 0, s>>>(D->counts);
+        k_pts_scatter<<<pgrid, 256, 0, s>>>(n_ifp, raw, D->cell, D->counts, D->pts);
+        k_block_boxes<<<(ns + 7) / 8, 256, 0, s>>>(n_ifp, D->pts, nb, ns, blo, bhi, slo, shi);
+        FTS_CUDA(cudaGetLastError());
+        FTS_CUDA(cudaEventRecord(D->ev[1], s));
         const int cgrid = (int)std::min<int64_t>((np + kCtaNodes - 1) / kCtaNodes,
                                                  (int64_t)D->num_sms * 8);
-        k_dist_cta<<<cgrid, kCtaNodes, 0, s>>>(np, D->order, D->xyz, pts, n_ifp, blo, bhi, nb,
+        k_dist_cta<<<cgrid, kCtaNodes, 0, s>>>(np, D->order, D->xyz, D->pts, n_ifp, blo, bhi, nb,
                                                slo, shi, ns, phi_dev, D->scanned);
     }
     FTS_CUDA(cudaGetLastError());
-    FTS_CUDA(cudaEventRecord(D->ev[1], s));
+    FTS_CUDA(cudaEventRecord(D->ev[2], s));
     if (st) {
+        st->ms_setup = wall_ms() - t0;
         unsigned long long scanned = 0;
         FTS_CUDA(cudaMemcpyAsync(&scanned, D->scanned, sizeof(scanned), cudaMemcpyDeviceToHost, s));
         FTS_CUDA(cudaStreamSynchronize(s));
-        st->blocks = nb;
+        float ms = 0.f;
+        FTS_CUDA(cudaEventElapsedTime(&ms, D->ev[0], D->ev[1]));
+        st->ms_setup += ms;
+        FTS_CUDA(cudaEventElapsedTime(&ms, D->ev[1], D->ev[2]));
+        st->ms_kernel = ms;
+        st->blocks = method == FTS_DIST_EXHAUSTIVE ? 0 : nb;
         st->points_scanned =
             method == FTS_DIST_EXHAUSTIVE ? np * (int64_t)n_ifp : (int64_t)scanned;
     }
@@ -476,6 +605,8 @@ int fts_dist_create(const float* xyz, int64_t np, int32_t device, fts_dist** out
         FTS_CUDA(cudaMalloc(&D->xyz, 3 * np * sizeof(float)));
         FTS_CUDA(cudaMalloc(&D->phi, np * sizeof(double)));
         FTS_CUDA(cudaMalloc(&D->scanned, sizeof(unsigned long long)));
+        FTS_CUDA(cudaMalloc(&D->counts, kCells * sizeof(uint32_t)));
+        FTS_CUDA(cudaMalloc(&D->keys, 6 * sizeof(unsigned)));
         FTS_CUDA(cudaMemcpy(D->xyz, xyz, 3 * np * sizeof(float), cudaMemcpyHostToDevice));
         // the nodes in Morton order (once per mesh): a CTA's 256 nodes form a brick
         {
@@ -527,12 +658,9 @@ int fts_dist_reset(fts_dist* D, const float* ifp, int32_t n_ifp, double* phi_n, 
         FTS_CUDA(cudaSetDevice(D->device));
         cudaStream_t s = D->stream;
         FTS_CUDA(cudaMemcpyAsync(D->phi, phi_n, D->np * sizeof(double), cudaMemcpyHostToDevice, s));
-        dist_reset_device(D, ifp, n_ifp, D->phi, method, s, &st);
+        dist_reset_device(D, ifp, false, n_ifp, D->phi, method, s, &st);
         FTS_CUDA(cudaMemcpyAsync(phi_n, D->phi, D->np * sizeof(double), cudaMemcpyDeviceToHost, s));
         FTS_CUDA(cudaStreamSynchronize(s));
-        float ms = 0.f;
-        if (n_ifp > 0) FTS_CUDA(cudaEventElapsedTime(&ms, D->ev[0], D->ev[1]));
-        st.ms_kernel = ms;
     } catch (const CudaError& e) {
         D->last_error = e.what;
         rc = e.code == cudaErrorMemoryAllocation ? FTS_ERR_OOM : FTS_ERR_CUDA;

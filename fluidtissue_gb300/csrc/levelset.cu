@@ -26,8 +26,8 @@ struct fts_dist;
 
 namespace fts {
 
-void dist_reset_device(fts_dist* D, const float* ifp, int32_t n_ifp, double* phi_dev,
-                       int32_t method, cudaStream_t s, fts_dist_stats* st);
+void dist_reset_device(fts_dist* D, const float* ifp, bool ifp_on_device, int32_t n_ifp,
+                       double* phi_dev, int32_t method, cudaStream_t s, fts_dist_stats* st);
 
 static std::string& g_ls_error() {
     static thread_local std::string e;
@@ -984,15 +984,10 @@ int fts_ls_update(fts_ls* S, const fts_ls_params* P, const double* flow, double*
             FTS_CUDA(cudaMemcpyAsync(&nif, S->count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
             FTS_CUDA(cudaStreamSynchronize(s));
             nif = std::min(nif, S->ifp_cap);
-            std::vector<float> pts(3 * (size_t)nif);
-            if (nif > 0)
-                FTS_CUDA(cudaMemcpyAsync(pts.data(), S->ifp, pts.size() * sizeof(float),
-                                         cudaMemcpyDeviceToHost, s));
             FTS_CUDA(cudaMemcpyAsync(ifn, x, np * sizeof(double), cudaMemcpyDeviceToDevice, s));
-            FTS_CUDA(cudaStreamSynchronize(s));
-            dist_reset_device(S->dist, pts.data(), (int32_t)nif, ifn, FTS_DIST_PRUNED, s, nullptr);
+            dist_reset_device(S->dist, S->ifp, true, (int32_t)nif, ifn, FTS_DIST_PRUNED, s, nullptr);
             k_ls_mix<<<g, kLsThreads, 0, s>>>(np, x, ifn, S->keep, S->phi);
-            launches += 2;
+            launches += nif > 0 ? 7 : 2;  // binning (5) and search, or the empty-set fill; mix
             S->have_reset = true;
             st.interface_points = nif;
             FTS_CUDA(cudaMemcpyAsync(phi, S->phi, np * sizeof(double), cudaMemcpyDeviceToHost, s));

@@ -339,10 +339,11 @@ const char* fts_rd_last_error(const fts_rd* rd);
  * points (float, each distance from norm3df as in the reference's kernel),
  * negated where the old phi_n[k] < 0.  With no interface point the minimum is
  * FLT_MAX, as in the reference.
- *   FTS_DIST_PRUNED: the points sorted along a Morton curve into blocks of 32
- *     with bounding boxes; each node scans only the blocks that can hold its
- *     nearest point, and candidates within rounding of the minimum are
- *     re-evaluated with norm3df, so the result equals the exhaustive minimum.
+ *   FTS_DIST_PRUNED: the points binned on the device along a Morton curve of
+ *     a 64^3 grid over their box, in blocks of 32 with bounding boxes; each
+ *     node scans only the blocks that can hold its nearest point, and
+ *     candidates within rounding of the minimum are re-evaluated with
+ *     norm3df, so the result equals the exhaustive minimum.
  *   FTS_DIST_EXHAUSTIVE: the reference's algorithm (every node against every
  *     point), for comparison.
  * ------------------------------------------------------------------------ */
@@ -352,8 +353,8 @@ typedef struct fts_dist_stats {
     int32_t status;
     int32_t blocks;           /* point blocks */
     int64_t points_scanned;   /* point distances evaluated (all nodes) */
-    double ms_setup;          /* host sort, uploads */
-    double ms_kernel;         /* device time of the distance kernel */
+    double ms_setup;          /* uploads and the device binning of the points */
+    double ms_kernel;         /* device time of the search kernel */
     double ms_total;
 } fts_dist_stats;
 
