@@ -161,8 +161,8 @@ __global__ void k_pts_scatter(int32_t n, const float* __restrict__ raw,
 }
 
 // Block and super-block boxes: one warp per super-block, one lane per point
-// of each of its blocks.
-__global__ void k_block_boxes(int32_t n, const float4* __restrict__ pts, int32_t nb, int32_t ns,
+// of each of its blocks; the last block is padded to 32 points.
+__global__ void k_block_boxes(int32_t n, float4* __restrict__ pts, int32_t nb, int32_t ns,
                               float4* __restrict__ blo, float4* __restrict__ bhi,
                               float4* __restrict__ slo, float4* __restrict__ shi) {
     const int lane = threadIdx.x & 31;
@@ -179,6 +179,8 @@ __global__ void k_block_boxes(int32_t n, const float4* __restrict__ pts, int32_t
                 l = pts[j];
                 h = l;
                 l.w = h.w = 0.f;
+            } else {  // pad the last block to 32 with points at +inf
+                pts[j] = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
             }
             for (int o = 16; o > 0; o >>= 1) {
                 l.x = fminf(l.x, __shfl_xor_sync(0xffffffffu, l.x, o));
@@ -285,14 +287,23 @@ __device__ float pruned_node(float px, float py, float pz, const float4* __restr
     }
 }
 
-// Cooperative pruned search.  Each CTA takes 256 nodes in Morton order (a
-// compact brick), so their candidate points are shared: the CTA bounds its
-// nodes' box, gets an upper bound U of every node's nearest squared distance
-// from the block nearest to the box, keeps the blocks whose box lies within
-// U (1 + margin) of the node box, sorts them by that distance (bitonic, in
-// shared memory) and each thread walks the sorted list until the box
-// distance passes its own best.  Pass 1 and pass 2 are those of the
-// per-node search (same expressions), so the result is the same float.
+// Cooperative pruned search, one pass.  Each CTA takes 256 nodes in Morton
+// order (a compact brick), so their candidate points are shared: the CTA
+// bounds its nodes' box, scans the block nearest to that box, whose values
+// give an upper bound U of every node's threshold (below), keeps the blocks
+// whose box lies within U of the node box, sorts them by that distance
+// (bitonic, in shared memory) and each thread walks the sorted list until the
+// box distance passes its own threshold.
+//
+// Exactness in one pass: a thread keeps thr = min_j fl(sq_j (1 + margin))
+// over the points seen (= fl(best (1 + margin)) by monotone rounding, best =
+// the minimum squared distance so far) and takes norm3df of every point with
+// sq <= thr at the time it is seen.  thr only decreases, so every point within
+// the margin of the final minimum, among them the point with the smallest
+// norm3df (the margin covers the ulps between the two orders), is evaluated;
+// blocks and the walk are cut at thr, never below it.  The minimum of norm3df
+// over a superset of those points that holds only real points is the
+// exhaustive minimum, the same float.
 constexpr int kCtaNodes = 256;
 constexpr int kCandCap = 2048;
 
@@ -301,6 +312,21 @@ __device__ __forceinline__ float boxbox_dist2(float4 alo, float4 ahi, float4 blo
     const float dy = fmaxf(fmaxf(blo.y - ahi.y, alo.y - bhi.y), 0.f);
     const float dz = fmaxf(fmaxf(blo.z - ahi.z, alo.z - bhi.z), 0.f);
     return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
+// One block of 32 points (padded with points at +inf, whose sq is inf and
+// never passes thr <= FLT_MAX (1 + margin) rounded: FLT_MAX at most after the
+// first real point; the start value FLT_MAX keeps inf out).
+__device__ __forceinline__ void scan_block(const float4* __restrict__ q32, float px, float py,
+                                           float pz, float& thr, float& dmin) {
+#pragma unroll 8
+    for (int j = 0; j < kDistBlock; ++j) {
+        const float4 q = __ldg(q32 + j);
+        const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+        const float sq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        thr = fminf(thr, sq * (1.f + kDistMargin));
+        if (sq <= thr) dmin = fminf(dmin, norm3df(dx, dy, dz));
+    }
 }
 
 __global__ void __launch_bounds__(kCtaNodes)
@@ -313,8 +339,9 @@ k_dist_cta(int64_t np, const int32_t* __restrict__ order, const float* __restric
     __shared__ unsigned long long seed;
     __shared__ unsigned int ubits;
     __shared__ int ncand;
-    __shared__ unsigned kmin[3], kmax[3];  // node box as order-preserving keys
+    __shared__ unsigned kmin[3], kmax[3];  // node box as order keys
     __shared__ float bmin[3], bmax[3];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long mine = 0;
     const int64_t nchunks = (np + kCtaNodes - 1) / kCtaNodes;
     for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
@@ -334,12 +361,16 @@ k_dist_cta(int64_t np, const int32_t* __restrict__ order, const float* __restric
             ncand = 0;
         }
         __syncthreads();
-        // node box
-        if (active) {
+        {  // node box
             const float p[3] = {px, py, pz};
             for (int a = 0; a < 3; ++a) {
-                atomicMin(&kmin[a], fkey(p[a]));
-                atomicMax(&kmax[a], fkey(p[a]));
+                unsigned lo = active ? fkey(p[a]) : 0xffffffffu, hi = active ? fkey(p[a]) : 0u;
+                lo = __reduce_min_sync(0xffffffffu, lo);
+                hi = __reduce_max_sync(0xffffffffu, hi);
+                if (lane == 0) {
+                    atomicMin(&kmin[a], lo);
+                    atomicMax(&kmax[a], hi);
+                }
             }
         }
         __syncthreads();
@@ -350,34 +381,46 @@ k_dist_cta(int64_t np, const int32_t* __restrict__ order, const float* __restric
         __syncthreads();
         const float4 clo = make_float4(bmin[0], bmin[1], bmin[2], 0.f);
         const float4 chi = make_float4(bmax[0], bmax[1], bmax[2], 0.f);
-        // seed: the block nearest to the node box
-        for (int32_t b = threadIdx.x; b < nb; b += blockDim.x) {
-            const float d = boxbox_dist2(clo, chi, __ldg(blo + b), __ldg(bhi + b));
-            atomicMin(&seed, ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)b);
-        }
-        __syncthreads();
-        float best = FLT_MAX;
-        if (active) {
-            const int32_t b = (int32_t)(seed & 0xffffffffull);
-            const int32_t j1 = min(n_ifp, (b + 1) * kDistBlock);
-            for (int32_t j = b * kDistBlock; j < j1; ++j) {
-                const float4 q = __ldg(pts + j);
-                const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
-                best = fminf(best, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-            }
-            mine += (unsigned long long)(j1 - b * kDistBlock);
-            atomicMax(&ubits, __float_as_uint(best));  // non-negative: bits order
-        }
-        __syncthreads();
-        const float U = __uint_as_float(ubits) * (1.f + kDistMargin);
-        // candidates: super-blocks, then their blocks, within U of the node box
-        for (int32_t t = threadIdx.x; t < ns; t += blockDim.x) {
-            if (boxbox_dist2(clo, chi, __ldg(slo + t), __ldg(shi + t)) > U) continue;
-            const int32_t b1 = min(nb, (t + 1) * kDistSuper);
-            for (int32_t b = t * kDistSuper; b < b1; ++b) {
+        {  // seed: the block nearest to the node box
+            unsigned long long key = ~0ull;
+            for (int32_t b = threadIdx.x; b < nb; b += blockDim.x) {
                 const float d = boxbox_dist2(clo, chi, __ldg(blo + b), __ldg(bhi + b));
-                if (d > U) continue;
-                const int at = atomicAdd(&ncand, 1);
+                key = min(key, ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)b);
+            }
+            for (int o = 16; o > 0; o >>= 1) key = min(key, __shfl_xor_sync(0xffffffffu, key, o));
+            if (lane == 0) atomicMin(&seed, key);
+        }
+        __syncthreads();
+        const int32_t sb = (int32_t)(seed & 0xffffffffull);
+        float thr = FLT_MAX, dmin = FLT_MAX;
+        if (active) {
+            scan_block(pts + (int64_t)sb * kDistBlock, px, py, pz, thr, dmin);
+            mine += (unsigned long long)(min(n_ifp, (sb + 1) * kDistBlock) - sb * kDistBlock);
+        }
+        {
+            unsigned u = active ? __float_as_uint(thr) : 0u;  // non-negative: bits order
+            u = __reduce_max_sync(0xffffffffu, u);
+            if (lane == 0) atomicMax(&ubits, u);
+        }
+        __syncthreads();
+        const float U = __uint_as_float(ubits);
+        // candidates within U of the node box: a warp per super-block, a lane
+        // per block, appended in ballot order
+        for (int32_t t = warp; t < ns; t += kCtaNodes / 32) {
+            if (boxbox_dist2(clo, chi, __ldg(slo + t), __ldg(shi + t)) > U) continue;
+            const int32_t b = t * kDistSuper + lane;
+            float d = FLT_MAX;
+            bool keep = false;
+            if (b < nb && b != sb) {
+                d = boxbox_dist2(clo, chi, __ldg(blo + b), __ldg(bhi + b));
+                keep = d <= U;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            int base = 0;
+            if (lane == 0 && m) base = atomicAdd(&ncand, __popc(m));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (keep) {
+                const int at = base + __popc(m & ((1u << lane) - 1u));
                 if (at < kCandCap)
                     cand[at] = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)b;
             }
@@ -416,37 +459,13 @@ k_dist_cta(int64_t np, const int32_t* __restrict__ order, const float* __restric
                 __syncthreads();
             }
         if (active) {
-            // pass 1: minimum squared distance over the sorted candidates
-            for (int i = 0; i < nc; ++i) {
-                const unsigned long long key = cand[i];
-                if (__uint_as_float((unsigned)(key >> 32)) > best) break;
-                const int32_t b = (int32_t)(key & 0xffffffffull);
-                if (box_dist2(__ldg(blo + b), __ldg(bhi + b), px, py, pz) > best) continue;
-                const int32_t j1 = min(n_ifp, (b + 1) * kDistBlock);
-                for (int32_t j = b * kDistBlock; j < j1; ++j) {
-                    const float4 q = __ldg(pts + j);
-                    const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
-                    best = fminf(best, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-                }
-                mine += (unsigned long long)(j1 - b * kDistBlock);
-            }
-            // pass 2: norm3df over the points within the margin of the minimum
-            const float thr = best * (1.f + kDistMargin);
-            float dmin = FLT_MAX;
             for (int i = 0; i < nc; ++i) {
                 const unsigned long long key = cand[i];
                 if (__uint_as_float((unsigned)(key >> 32)) > thr) break;
                 const int32_t b = (int32_t)(key & 0xffffffffull);
                 if (box_dist2(__ldg(blo + b), __ldg(bhi + b), px, py, pz) > thr) continue;
-                const int32_t j1 = min(n_ifp, (b + 1) * kDistBlock);
-                for (int32_t j = b * kDistBlock; j < j1; ++j) {
-                    const float4 q = __ldg(pts + j);
-                    const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
-                    if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= thr) {
-                        const float d = norm3df(dx, dy, dz);
-                        if (d < dmin) dmin = d;
-                    }
-                }
+                scan_block(pts + (int64_t)b * kDistBlock, px, py, pz, thr, dmin);
+                mine += (unsigned long long)(min(n_ifp, (b + 1) * kDistBlock) - b * kDistBlock);
             }
             double out = dmin;
             if (phi[k] < 0.0f) out = -out;
@@ -455,7 +474,7 @@ k_dist_cta(int64_t np, const int32_t* __restrict__ order, const float* __restric
         __syncthreads();
     }
     for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
-    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(scanned, mine);
+    if (lane == 0 && mine) atomicAdd(scanned, mine);
 }
 
 }  // namespace fts
@@ -473,7 +492,7 @@ struct fts_dist {
     int64_t cap = 0;            // points the buffers below hold
     float* raw = nullptr;       // [3 cap] points as the caller gave them (host uploads)
     uint32_t* cell = nullptr;   // [cap] binning cell of each point
-    float4* pts = nullptr;      // [cap] points binned by cell
+    float4* pts = nullptr;      // [32 nbc] points binned by cell, padded with +inf points
     float4* boxes = nullptr;    // block boxes lo[nbc], hi[nbc], super-block lo[nsc], hi[nsc]
     uint32_t* counts = nullptr; // [kCells] cell histogram, then cursors
     unsigned* keys = nullptr;   // [6] bounding box of the points as order keys
@@ -527,7 +546,7 @@ void dist_reset_device(fts_dist* D, const float* ifp, bool ifp_on_device, int32_
         const int64_t cap = n_ifp + n_ifp / 4;
         FTS_CUDA(cudaMalloc(&D->raw, 3 * (size_t)cap * sizeof(float)));
         FTS_CUDA(cudaMalloc(&D->cell, (size_t)cap * sizeof(uint32_t)));
-        FTS_CUDA(cudaMalloc(&D->pts, (size_t)cap * sizeof(float4)));
+        FTS_CUDA(cudaMalloc(&D->pts, (size_t)blocks_for(cap) * kDistBlock * sizeof(float4)));
         FTS_CUDA(cudaMalloc(&D->boxes, 2 * (size_t)(blocks_for(cap) + supers_for(cap)) * sizeof(float4)));
         D->cap = cap;
     }
