@@ -6,15 +6,15 @@
 // Here the points are binned on the device into the cells of a 64^3 grid
 // over their bounding box, cells in Morton order (a counting sort: histogram,
 // scan, scatter), and cut into blocks of 32 with bounding boxes, and blocks of
-// 32 blocks with their own boxes; the nodes are taken in Morton order (once per mesh) by CTAs of 256,
-// which share a sorted candidate list of blocks (k_dist_cta), and a thread
-// scans only the candidate blocks whose box is closer than its current best.
-// The first pass finds the minimum squared distance in float; a second pass
-// re-evaluates every point within a relative margin of that minimum with
-// norm3df, the reference's distance, so the result is the same float as the
-// exhaustive minimum of norm3df values (the margin covers the few-ulp
-// difference between the squared-distance order and the norm3df order).  The exhaustive kernel (the reference's algorithm) is kept for
-// comparison and for bit-exact parity tests.
+// 32 blocks with their own boxes.  The nodes are taken in Morton order (once
+// per mesh) by CTAs of 512, which share a sorted candidate list of blocks
+// (k_dist_cta); a thread scans only the candidate blocks whose box is within
+// its running threshold, and takes norm3df, the reference's distance, of every
+// point within a relative margin of the running minimum squared distance, so
+// the result is the same float as the exhaustive minimum of norm3df values
+// (the margin covers the few-ulp difference between the squared-distance
+// order and the norm3df order).  The exhaustive kernel (the reference's
+// algorithm) is kept for comparison and for bit-exact parity tests.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -287,13 +287,13 @@ __device__ float pruned_node(float px, float py, float pz, const float4* __restr
     }
 }
 
-// Cooperative pruned search, one pass.  Each CTA takes 256 nodes in Morton
-// order (a compact brick), so their candidate points are shared: the CTA
-// bounds its nodes' box, scans the block nearest to that box, whose values
-// give an upper bound U of every node's threshold (below), keeps the blocks
-// whose box lies within U of the node box, sorts them by that distance
-// (bitonic, in shared memory) and each thread walks the sorted list until the
-// box distance passes its own threshold.
+// Cooperative pruned search, one pass.  Each CTA takes kCtaNodes nodes in
+// Morton order (a compact brick), so their candidate points are shared: the
+// CTA bounds its nodes' box, scans a block near that box (the nearest block of
+// the nearest super-block), whose values give an upper bound U of every node's
+// threshold (below), keeps the blocks whose box lies within U of the node box,
+// sorts them by that distance (bitonic, in shared memory) and each thread
+// walks the sorted list until the box distance passes its own threshold.
 //
 // Exactness in one pass: a thread keeps thr = min_j fl(sq_j (1 + margin))
 // over the points seen (= fl(best (1 + margin)) by monotone rounding, best =
@@ -304,7 +304,7 @@ __device__ float pruned_node(float px, float py, float pz, const float4* __restr
 // blocks and the walk are cut at thr, never below it.  The minimum of norm3df
 // over a superset of those points that holds only real points is the
 // exhaustive minimum, the same float.
-constexpr int kCtaNodes = 256;
+constexpr int kCtaNodes = 512;
 constexpr int kCandCap = 2048;
 
 __device__ __forceinline__ float boxbox_dist2(float4 alo, float4 ahi, float4 blo, float4 bhi) {
@@ -315,17 +315,27 @@ __device__ __forceinline__ float boxbox_dist2(float4 alo, float4 ahi, float4 blo
 }
 
 // One block of 32 points (padded with points at +inf, whose sq is inf and
-// never passes thr <= FLT_MAX (1 + margin) rounded: FLT_MAX at most after the
-// first real point; the start value FLT_MAX keeps inf out).
-__device__ __forceinline__ void scan_block(const float4* __restrict__ q32, float px, float py,
-                                           float pz, float& thr, float& dmin) {
+// never passes thr <= FLT_MAX).  First the block's minimum squared distance;
+// only if it is within thr, the update thr = min(thr, fl(bmin (1 + margin)))
+// (= the running minimum of fl(sq (1 + margin)) over the block's points) and
+// the norm3df evaluations of the points with sq <= thr.
+__device__ __forceinline__ void scan_block(const float4* q32, float px, float py, float pz,
+                                           float& thr, float& dmin) {
+    float bmin = INFINITY;
 #pragma unroll 8
     for (int j = 0; j < kDistBlock; ++j) {
-        const float4 q = __ldg(q32 + j);
+        const float4 q = q32[j];
         const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
-        const float sq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        thr = fminf(thr, sq * (1.f + kDistMargin));
-        if (sq <= thr) dmin = fminf(dmin, norm3df(dx, dy, dz));
+        bmin = fminf(bmin, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+    }
+    if (bmin <= thr) {
+        thr = fminf(thr, bmin * (1.f + kDistMargin));
+#pragma unroll 4
+        for (int j = 0; j < kDistBlock; ++j) {
+            const float4 q = q32[j];
+            const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+            if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= thr) dmin = fminf(dmin, norm3df(dx, dy, dz));
+        }
     }
 }
 
@@ -336,6 +346,7 @@ k_dist_cta(int64_t np, const int32_t* __restrict__ order, const float* __restric
            const float4* __restrict__ shi, int32_t ns, double* __restrict__ phi,
            unsigned long long* __restrict__ scanned) {
     __shared__ unsigned long long cand[kCandCap];
+    __shared__ float4 stage[kCtaNodes / 32][32];  // one block of points per warp
     __shared__ unsigned long long seed;
     __shared__ unsigned int ubits;
     __shared__ int ncand;
@@ -381,14 +392,21 @@ k_dist_cta(int64_t np, const int32_t* __restrict__ order, const float* __restric
         __syncthreads();
         const float4 clo = make_float4(bmin[0], bmin[1], bmin[2], 0.f);
         const float4 chi = make_float4(bmax[0], bmax[1], bmax[2], 0.f);
-        {  // seed: the block nearest to the node box
+        if (warp == 0) {  // seed: the nearest block of the super-block nearest to the node box
             unsigned long long key = ~0ull;
-            for (int32_t b = threadIdx.x; b < nb; b += blockDim.x) {
-                const float d = boxbox_dist2(clo, chi, __ldg(blo + b), __ldg(bhi + b));
-                key = min(key, ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)b);
+            for (int32_t t = lane; t < ns; t += 32) {
+                const float d = boxbox_dist2(clo, chi, __ldg(slo + t), __ldg(shi + t));
+                key = min(key, ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)t);
             }
             for (int o = 16; o > 0; o >>= 1) key = min(key, __shfl_xor_sync(0xffffffffu, key, o));
-            if (lane == 0) atomicMin(&seed, key);
+            const int32_t b = (int32_t)(key & 0xffffffffull) * kDistSuper + lane;
+            key = ~0ull;
+            if (b < nb) {
+                const float d = boxbox_dist2(clo, chi, __ldg(blo + b), __ldg(bhi + b));
+                key = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)b;
+            }
+            for (int o = 16; o > 0; o >>= 1) key = min(key, __shfl_xor_sync(0xffffffffu, key, o));
+            if (lane == 0) seed = key;
         }
         __syncthreads();
         const int32_t sb = (int32_t)(seed & 0xffffffffull);
@@ -445,28 +463,42 @@ k_dist_cta(int64_t np, const int32_t* __restrict__ order, const float* __restric
         __syncthreads();
         for (int kk = 2; kk <= m; kk <<= 1)
             for (int jj = kk >> 1; jj > 0; jj >>= 1) {
-                for (int i = threadIdx.x; i < m; i += blockDim.x) {
-                    const int l = i ^ jj;
-                    if (l > i) {
-                        const unsigned long long a = cand[i], b = cand[l];
-                        const bool up = (i & kk) == 0;
-                        if ((a > b) == up) {
-                            cand[i] = b;
-                            cand[l] = a;
-                        }
+                for (int q = threadIdx.x; q < (m >> 1); q += blockDim.x) {  // one pair each
+                    const int i = ((q & ~(jj - 1)) << 1) | (q & (jj - 1)), l = i + jj;
+                    const unsigned long long a = cand[i], b = cand[l];
+                    if ((a > b) == ((i & kk) == 0)) {
+                        cand[i] = b;
+                        cand[l] = a;
                     }
                 }
                 __syncthreads();
             }
-        if (active) {
-            for (int i = 0; i < nc; ++i) {
-                const unsigned long long key = cand[i];
-                if (__uint_as_float((unsigned)(key >> 32)) > thr) break;
-                const int32_t b = (int32_t)(key & 0xffffffffull);
-                if (box_dist2(__ldg(blo + b), __ldg(bhi + b), px, py, pz) > thr) continue;
-                scan_block(pts + (int64_t)b * kDistBlock, px, py, pz, thr, dmin);
+        // the walk, warp-uniform: a block that some lane needs is staged once
+        // (one coalesced load) and read back as a broadcast from shared memory
+        // (the next candidate's points are loaded ahead, into a register)
+        int32_t pre_b = -1;
+        float4 pre = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int i = 0; i < nc; ++i) {
+            const unsigned long long key = cand[i];
+            const bool go = active && __uint_as_float((unsigned)(key >> 32)) <= thr;
+            if (__ballot_sync(0xffffffffu, go) == 0u) break;
+            const int32_t b = (int32_t)(key & 0xffffffffull);
+            const bool need = go && box_dist2(__ldg(blo + b), __ldg(bhi + b), px, py, pz) <= thr;
+            if (__ballot_sync(0xffffffffu, need) == 0u) continue;
+            const float4 v = pre_b == b ? pre : __ldg(pts + (int64_t)b * kDistBlock + lane);
+            if (i + 1 < nc) {
+                pre_b = (int32_t)(cand[i + 1] & 0xffffffffull);
+                pre = __ldg(pts + (int64_t)pre_b * kDistBlock + lane);
+            }
+            __syncwarp();
+            stage[warp][lane] = v;
+            __syncwarp();
+            if (need) {
+                scan_block(stage[warp], px, py, pz, thr, dmin);
                 mine += (unsigned long long)(min(n_ifp, (b + 1) * kDistBlock) - b * kDistBlock);
             }
+        }
+        if (active) {
             double out = dmin;
             if (phi[k] < 0.0f) out = -out;
             phi[k] = out;
@@ -627,7 +659,7 @@ int fts_dist_create(const float* xyz, int64_t np, int32_t device, fts_dist** out
         FTS_CUDA(cudaMalloc(&D->counts, kCells * sizeof(uint32_t)));
         FTS_CUDA(cudaMalloc(&D->keys, 6 * sizeof(unsigned)));
         FTS_CUDA(cudaMemcpy(D->xyz, xyz, 3 * np * sizeof(float), cudaMemcpyHostToDevice));
-        // the nodes in Morton order (once per mesh): a CTA's 256 nodes form a brick
+        // the nodes in Morton order (once per mesh): a CTA's nodes form a brick
         {
             float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
             for (int64_t k = 0; k < np; ++k)
