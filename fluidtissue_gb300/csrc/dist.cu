@@ -7,7 +7,7 @@
 // over their bounding box, cells in Morton order (a counting sort: histogram,
 // scan, scatter), and cut into blocks of 32 with bounding boxes, and blocks of
 // 32 blocks with their own boxes.  The nodes are taken in Morton order (once
-// per mesh) by CTAs of 512, which share a sorted candidate list of blocks
+// per mesh) by CTAs of 256, which share a sorted candidate list of blocks
 // (k_dist_cta); a thread scans only the candidate blocks whose box is within
 // its running threshold, and takes norm3df, the reference's distance, of every
 // point within a relative margin of the running minimum squared distance, so
@@ -304,7 +304,7 @@ __device__ float pruned_node(float px, float py, float pz, const float4* __restr
 // blocks and the walk are cut at thr, never below it.  The minimum of norm3df
 // over a superset of those points that holds only real points is the
 // exhaustive minimum, the same float.
-constexpr int kCtaNodes = 512;
+constexpr int kCtaNodes = 256;
 constexpr int kCandCap = 2048;
 
 __device__ __forceinline__ float boxbox_dist2(float4 alo, float4 ahi, float4 blo, float4 bhi) {
@@ -473,29 +473,58 @@ k_dist_cta(int64_t np, const int32_t* __restrict__ order, const float* __restric
                 }
                 __syncthreads();
             }
-        // the walk, warp-uniform: a block that some lane needs is staged once
-        // (one coalesced load) and read back as a broadcast from shared memory
-        // (the next candidate's points are loaded ahead, into a register)
+        // the walk, warp-uniform, in groups of 32 candidates: one lane per
+        // candidate tests its block against the warp's node box and the
+        // largest threshold of the warp; the blocks that pass are taken in
+        // list order, and one that some lane needs is staged once (one
+        // coalesced load) and read back as a broadcast from shared memory (the
+        // next passing block's points are loaded ahead, into a register).
+        float4 wlo, whi;
+        {
+            unsigned kl[3], kh[3];
+            const float p[3] = {px, py, pz};
+            for (int a = 0; a < 3; ++a) {
+                kl[a] = __reduce_min_sync(0xffffffffu, active ? fkey(p[a]) : 0xffffffffu);
+                kh[a] = __reduce_max_sync(0xffffffffu, active ? fkey(p[a]) : 0u);
+            }
+            wlo = make_float4(fkey_inv(kl[0]), fkey_inv(kl[1]), fkey_inv(kl[2]), 0.f);
+            whi = make_float4(fkey_inv(kh[0]), fkey_inv(kh[1]), fkey_inv(kh[2]), 0.f);
+        }
+        const bool warp_live = __any_sync(0xffffffffu, active);
         int32_t pre_b = -1;
         float4 pre = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int i = 0; i < nc; ++i) {
-            const unsigned long long key = cand[i];
-            const bool go = active && __uint_as_float((unsigned)(key >> 32)) <= thr;
-            if (__ballot_sync(0xffffffffu, go) == 0u) break;
-            const int32_t b = (int32_t)(key & 0xffffffffull);
-            const bool need = go && box_dist2(__ldg(blo + b), __ldg(bhi + b), px, py, pz) <= thr;
-            if (__ballot_sync(0xffffffffu, need) == 0u) continue;
-            const float4 v = pre_b == b ? pre : __ldg(pts + (int64_t)b * kDistBlock + lane);
-            if (i + 1 < nc) {
-                pre_b = (int32_t)(cand[i + 1] & 0xffffffffull);
-                pre = __ldg(pts + (int64_t)pre_b * kDistBlock + lane);
+        for (int g = 0; warp_live && g < nc; g += 32) {
+            // thresholds are non-negative: their bits order like the numbers
+            const float tmax =
+                __uint_as_float(__reduce_max_sync(0xffffffffu, active ? __float_as_uint(thr) : 0u));
+            if (__uint_as_float((unsigned)(cand[g] >> 32)) > tmax) break;
+            int32_t bl = -1;
+            bool look = false;
+            if (g + lane < nc) {
+                const unsigned long long key = cand[g + lane];
+                bl = (int32_t)(key & 0xffffffffull);
+                look = __uint_as_float((unsigned)(key >> 32)) <= tmax &&
+                       boxbox_dist2(wlo, whi, __ldg(blo + bl), __ldg(bhi + bl)) <= tmax;
             }
-            __syncwarp();
-            stage[warp][lane] = v;
-            __syncwarp();
-            if (need) {
-                scan_block(stage[warp], px, py, pz, thr, dmin);
-                mine += (unsigned long long)(min(n_ifp, (b + 1) * kDistBlock) - b * kDistBlock);
+            unsigned m = __ballot_sync(0xffffffffu, look);
+            while (m) {
+                const int32_t b = __shfl_sync(0xffffffffu, bl, __ffs(m) - 1);
+                m &= m - 1;
+                const bool need =
+                    active && box_dist2(__ldg(blo + b), __ldg(bhi + b), px, py, pz) <= thr;
+                if (__ballot_sync(0xffffffffu, need) == 0u) continue;
+                const float4 v = pre_b == b ? pre : __ldg(pts + (int64_t)b * kDistBlock + lane);
+                if (m) {
+                    pre_b = __shfl_sync(0xffffffffu, bl, __ffs(m) - 1);
+                    pre = __ldg(pts + (int64_t)pre_b * kDistBlock + lane);
+                }
+                __syncwarp();
+                stage[warp][lane] = v;
+                __syncwarp();
+                if (need) {
+                    scan_block(stage[warp], px, py, pz, thr, dmin);
+                    mine += (unsigned long long)(min(n_ifp, (b + 1) * kDistBlock) - b * kDistBlock);
+                }
             }
         }
         if (active) {
