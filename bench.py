@@ -52,8 +52,8 @@ def _peaks():
 KERNELS = {
     "stencil": ("k_minres_A_lat", "FP32 lattice half-stencil 4x4-block SpMV + MINRES dots"),
     "assembled": ("k_minres_A_ell", "FP32 sliced-ELL 4x4-block SpMV + MINRES dots"),
-    "matfree": ("k_mf_lat_minres_A", "FP32 matrix-free lattice operator, geometry recomputed "
-                "per node, + MINRES dots; compute bound"),
+    "matfree": ("k_mf_cube+k_mf_gather_minres_A", "FP32 matrix-free lattice operator: element "
+                "geometry and rows once per cube, corner sums gathered per node, + MINRES dots"),
 }
 
 

@@ -21,7 +21,7 @@ void free_all(Ctx& c) {
                     c.b, c.x, c.r, c.w64.q, c.w64.R[0], c.w64.R[1], c.w64.Y[0], c.w64.Y[1],
                     c.w64.W[0], c.w64.W[1], c.w64.X, c.w32.q, c.w32.R[0], c.w32.R[1],
                     c.w32.Y[0], c.w32.Y[1], c.w32.W[0], c.w32.W[1], c.w32.X, c.w32.r0, c.ms,
-                    c.os, c.red.partials, c.red.ticket, c.err_flag, c.bicg, c.mf_rec};
+                    c.os, c.red.partials, c.red.ticket, c.err_flag, c.bicg, c.mf_rec, c.mf_cube};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     mg_free(c.mg64);
@@ -715,9 +715,12 @@ static int solve_common(fts_ctx* ctx, const double* phi, const double* source, c
         if (c.matfree)  // tets + node->element map + 64 B record per element; map offsets,
                         // flags, x, r1, q per node
             st.spmv_bytes = (double)c.nt * (16.0 + 16.0 + 64.0) + n * (4.0 + 1.0 + 3.0 * 16.0);
-        if (c.matfree && c.topo.kuhn_elements)  // lattice form: coordinates, flags, x, r1, q
-                                                // per node, FP32 mu per element
-            st.spmv_bytes = (double)c.nt * 4.0 + n * (12.0 + 1.0 + 3.0 * 16.0);
+        if (c.matfree && c.topo.kuhn_elements) {  // lattice form: coordinates, flags, x, r1,
+                                                  // q per node, FP32 mu per element, and the
+                                                  // 32 corner sums per cube written and read
+            const double m = (double)(c.topo.lattice_n - 1);
+            st.spmv_bytes = (double)c.nt * 4.0 + n * (12.0 + 1.0 + 3.0 * 16.0) + m * m * m * 256.0;
+        }
         st.spmv_bytes_fp64 = nb * (16.0 * 8.0 + 4.0) + 4.0 * (n + 1.0) + 3.0 * 4.0 * n * 8.0;
     }
     if (stats) *stats = st;

@@ -187,6 +187,7 @@ struct Ctx {
     // operator representation: false = assembled BSR, true = element gather
     bool matfree = false;
     float* mf_rec = nullptr;   // FP32 element records of the matrix-free operator
+    float* mf_cube = nullptr;  // per-cube corner sums of the lattice matrix-free operator
 
     // preconditioner
     bool use_mg = false;

@@ -14,9 +14,12 @@
 // and Dirichlet velocity values are read as zero.
 //
 // FP32 inner operator: on meshes in the lattice generator's element order the
-// geometry is recomputed per node from the coordinates (k_mf_lat_minres_A);
-// otherwise a 64-byte FP32 record per element (gradients, volume, h^2, mu)
-// built from the FP64 geometry, each read by the element's 4 nodes (L2 reuse).
+// geometry is recomputed from the coordinates, once per element: a thread per
+// cube applies its 6 tetrahedra and writes the sums per cube corner
+// (k_mf_cube), and a thread per node adds the corners it is of in the 8 cubes
+// around it, fused with the MINRES dots (k_mf_gather_minres_A); otherwise a
+// 64-byte FP32 record per element (gradients, volume, h^2, mu) built from the
+// FP64 geometry, each read by the element's 4 nodes (L2 reuse).
 // FP64 outer residual: the stored FP64 ElemGeom.
 #include <cfloat>
 
@@ -164,11 +167,14 @@ k_mf_minres_A(int64_t np, const int32_t* __restrict__ p2t_ptr, const uint32_t* _
 // ---------------------------------------------------------------------------
 // Kuhn-lattice form (elements in the order of the lattice generator: element
 // 6c + t of cube c is the monotone path 0 -> e_p0 -> e_p0 + e_p1 -> (1,1,1) of
-// axis permutation t).  A node's 24 elements follow from its lattice position,
-// and their geometry is recomputed in FP32 from the node coordinates (edge
+// axis permutation t).  A cube's 6 elements follow from its lattice position,
+// and their geometry is recomputed in FP32 from the corner coordinates (edge
 // vectors of nearby float coordinates are exact or nearly so), so one
-// application reads 12 B of coordinates, 24 B of viscosity and the vectors per
-// node — no element records, connectivity or node-element map.
+// application reads 12 B of coordinates per node and 24 B of viscosity per
+// cube, and writes and reads back 128 B of corner sums per cube — no element
+// records, connectivity or node-element map.  Per node and element pair (the
+// first version of this operator) the geometry was formed four times and the
+// kernel took 4.94 ms at 257^3 against 2.04 ms for the two phases.
 // ---------------------------------------------------------------------------
 // First two axes of the path of permutation t: {0,1,2} {0,2,1} {1,0,2}
 // {1,2,0} {2,0,1} {2,1,0} (the lattice generator's order).
@@ -224,16 +230,117 @@ __device__ __forceinline__ void tet_geom_f32(const float p[4][3], float g[4][3],
     hh = h * h;
 }
 
+// The four rows of one element applied to its nodal values u[4][4], each row
+// by the expressions of elem_row (the velocity gradient and the pressure sums
+// formed once for the four).
+__device__ __forceinline__ void elem_apply4(const float g[4][3], float vol, float hh, float mu,
+                                            const float u[4][4], float alpha, float eps,
+                                            const float wq[4], const float mref[4][4],
+                                            float y[4][4]) {
+    float G[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            G[r][c] = u[0][r] * g[0][c] + u[1][r] * g[1][c] + u[2][r] * g[2][c] + u[3][r] * g[3][c];
+    float gp[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) gp[c] = u[0][3] * g[0][c] + u[1][3] * g[1][c] + u[2][3] * g[2][c] + u[3][3] * g[3][c];
+    const float pbar = wq[0] * u[0][3] + wq[1] * u[1][3] + wq[2] * u[2][3] + wq[3] * u[3][3];
+    const float div = G[0][0] + G[1][1] + G[2][2];
+    const float mv = mu * vol;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const float mp = mref[a][0] * u[0][3] + mref[a][1] * u[1][3] + mref[a][2] * u[2][3] + mref[a][3] * u[3][3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+            y[a][r] = mv * (g[a][0] * (G[r][0] + G[0][r]) + g[a][1] * (G[r][1] + G[1][r]) +
+                            g[a][2] * (G[r][2] + G[2][r])) -
+                      vol * g[a][r] * pbar;
+        y[a][3] = -wq[a] * vol * div - alpha * hh * vol * (g[a][0] * gp[0] + g[a][1] * gp[1] + g[a][2] * gp[2]) -
+                  eps * vol * mp;
+    }
+}
+
+// Phase 1 of the lattice matrix-free operator: a thread per cube (ci, cj, ck)
+// of the (n-1)^3 cubes loads its 8 corners (corner q = dx + 2 dy + 4 dz),
+// forms each of its 6 tetrahedra's geometry once (the monotone path
+// 0 -> e_p0 -> e_p0 + e_p1 -> 7 of permutation t) and applies the element's
+// four rows; the sums per corner and component go to
+// out[(4 q + comp) * ncubes + cube] (coalesced for both phases).
 __global__ void __launch_bounds__(kThreads)
-k_mf_lat_minres_A(int n, int64_t np, const float* __restrict__ xyz, const float* __restrict__ muf,
-                  const uint8_t* __restrict__ bnd, const V4<float>* __restrict__ Y, int ybuf,
-                  const V4<float>* __restrict__ R1, V4<float>* __restrict__ q, float alpha,
-                  float eps, MfConst K, Reduction red, MinresScalars* s) {
+k_mf_cube(int n, const float* __restrict__ xyz, const float* __restrict__ muf,
+          const uint8_t* __restrict__ bnd, const V4<float>* __restrict__ Y, int ybuf, float alpha,
+          float eps, MfConst K, const MinresScalars* __restrict__ s, float* __restrict__ out) {
+    if (s->stop) return;
+    const float wadd = (float)s->ycorr[ybuf];
+    const int m = n - 1;
+    const int nn = n * n;
+    const int64_t ncubes = (int64_t)m * m * m;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncubes;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        const int ci = (int)(c % m), cj = (int)((c / m) % m), ck = (int)(c / ((int64_t)m * m));
+        const int o = ci + n * (cj + n * ck);
+        float p[8][3], u[8][4], acc[8][4];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int id = o + (q & 1) + n * ((q >> 1) & 1) + nn * (q >> 2);
+            const float* xp = xyz + 3 * (int64_t)id;
+            p[q][0] = __ldg(xp);
+            p[q][1] = __ldg(xp + 1);
+            p[q][2] = __ldg(xp + 2);
+            const V4<float> xv = Y[id];
+            const bool d = __ldg(bnd + id) != 0;
+            u[q][0] = d ? 0.f : xv.x;
+            u[q][1] = d ? 0.f : xv.y;
+            u[q][2] = d ? 0.f : xv.z;
+            u[q][3] = xv.w + wadd;
+#pragma unroll
+            for (int comp = 0; comp < 4; ++comp) acc[q][comp] = 0.f;
+        }
+#pragma unroll
+        for (int t = 0; t < 6; ++t) {
+            int p0, p1;
+            lat_path(t, p0, p1);
+            const int q1 = 1 << p0, q2 = q1 | (1 << p1);
+            const int cq[4] = {0, q1, q2, 7};
+            float pe[4][3], ue[4][4];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) pe[b][a] = p[cq[b]][a];
+#pragma unroll
+                for (int a = 0; a < 4; ++a) ue[b][a] = u[cq[b]][a];
+            }
+            float g[4][3], vol, hh, ye[4][4];
+            tet_geom_f32(pe, g, vol, hh);
+            elem_apply4(g, vol, hh, __ldg(muf + 6 * c + t), ue, alpha, eps, K.wq, K.mref, ye);
+#pragma unroll
+            for (int b = 0; b < 4; ++b)
+#pragma unroll
+                for (int comp = 0; comp < 4; ++comp) acc[cq[b]][comp] += ye[b][comp];
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+            for (int comp = 0; comp < 4; ++comp) out[(4 * q + comp) * ncubes + c] = acc[q][comp];
+    }
+}
+
+// Phase 2: q = S (y + ycorr e_p) / beta at each node from the corner sums of
+// the cubes around it (Dirichlet velocity rows identity), fused with the
+// MINRES dots v.q and v.r1.
+__global__ void __launch_bounds__(kThreads)
+k_mf_gather_minres_A(int n, int64_t np, const float* __restrict__ cube,
+                     const uint8_t* __restrict__ bnd, const V4<float>* __restrict__ Y, int ybuf,
+                     const V4<float>* __restrict__ R1, V4<float>* __restrict__ q, Reduction red,
+                     MinresScalars* s) {
     if (s->stop) return;
     const float tinv = (float)(1.0 / s->beta);
     const float wadd = (float)s->ycorr[ybuf];
     const int m = n - 1;
     const int nn = n * n;
+    const int64_t ncubes = (int64_t)m * m * m;
     double acc[2] = {0.0, 0.0};
     for (int64_t v64 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v64 < np;
          v64 += (int64_t)gridDim.x * blockDim.x) {
@@ -243,44 +350,18 @@ k_mf_lat_minres_A(int n, int64_t np, const float* __restrict__ xyz, const float*
         const int j = rem / n;
         const int i = rem - j * n;
         float y[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 1
+        // branch-free, so that all 32 loads are in flight at once: a cube
+        // beyond the lattice is read at cube 0 and weighted by zero
+#pragma unroll
         for (int corner = 0; corner < 8; ++corner) {
             const int dx = corner & 1, dy = (corner >> 1) & 1, dz = corner >> 2;
             const int ci = i - dx, cj = j - dy, ck = k - dz;
-            if (ci < 0 || cj < 0 || ck < 0 || ci >= m || cj >= m || ck >= m) continue;
-            const int a = dx + dy + dz;  // the node's place on every path through it
-            const int o = ci + n * (cj + n * ck);
-            const int64_t cube = ci + (int64_t)m * (cj + (int64_t)m * ck);
-            // axis of the single 1 (a == 1) or of the single 0 (a == 2)
-            const int ax = a == 1 ? (dx ? 0 : (dy ? 1 : 2)) : (!dx ? 0 : (!dy ? 1 : 2));
-#pragma unroll 1
-            for (int t = 0; t < 6; ++t) {
-                int p0, p1;
-                lat_path(t, p0, p1);
-                const int p2 = 3 - p0 - p1;
-                if ((a == 1 && p0 != ax) || (a == 2 && p2 != ax)) continue;
-                const int s0 = p0 == 0 ? 1 : (p0 == 1 ? n : nn);
-                const int s1 = p1 == 0 ? 1 : (p1 == 1 ? n : nn);
-                const int ids[4] = {o, o + s0, o + s0 + s1, o + 1 + n + nn};
-                float p[4][3], u[4][4];
+            const bool ok = ci >= 0 && cj >= 0 && ck >= 0 && ci < m && cj < m && ck < m;
+            const int64_t cb = ok ? ci + (int64_t)m * (cj + (int64_t)m * ck) : 0;
+            const float w = ok ? 1.f : 0.f;
 #pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    const float* xp = xyz + 3 * (int64_t)ids[b];
-                    p[b][0] = __ldg(xp);
-                    p[b][1] = __ldg(xp + 1);
-                    p[b][2] = __ldg(xp + 2);
-                    const V4<float> xv = Y[ids[b]];
-                    const bool d = __ldg(bnd + ids[b]) != 0;
-                    u[b][0] = d ? 0.f : xv.x;
-                    u[b][1] = d ? 0.f : xv.y;
-                    u[b][2] = d ? 0.f : xv.z;
-                    u[b][3] = xv.w + wadd;
-                }
-                float g[4][3], vol, hh;
-                tet_geom_f32(p, g, vol, hh);
-                elem_row<float>(g, vol, hh, __ldg(muf + 6 * cube + t), a, u, alpha, eps, K.wq,
-                                K.mref, y);
-            }
+            for (int comp = 0; comp < 4; ++comp)
+                y[comp] = fmaf(w, __ldg(cube + (4 * corner + comp) * ncubes + cb), y[comp]);
         }
         const V4<float> yv = Y[v];
         if (bnd[v]) {
@@ -405,10 +486,15 @@ __global__ void k_mf_pc(int64_t np, const int32_t* __restrict__ p2t_ptr,
 void launch_mf_minres_A(Ctx& c, const V4<float>* Y, int ybuf, const V4<float>* R1, V4<float>* q) {
     static const MfConst K = mf_const();
     if (c.topo.kuhn_elements) {
-        k_mf_lat_minres_A<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
-            c.topo.lattice_n, c.np, c.xyz, c.mf_rec, c.bnd, Y, ybuf, R1, q, (float)c.par.alpha,
-            (float)c.par.eps, K, c.red, c.ms);
-        c.launches += 1;
+        const int n = c.topo.lattice_n;
+        const int64_t ncubes = (int64_t)(n - 1) * (n - 1) * (n - 1);
+        if (!c.mf_cube) c.mf_cube = dev_alloc<float>(c, (size_t)ncubes * 32);
+        k_mf_cube<<<grid_for(c, ncubes), kThreads, 0, c.stream>>>(
+            n, c.xyz, c.mf_rec, c.bnd, Y, ybuf, (float)c.par.alpha, (float)c.par.eps, K, c.ms,
+            c.mf_cube);
+        k_mf_gather_minres_A<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
+            n, c.np, c.mf_cube, c.bnd, Y, ybuf, R1, q, c.red, c.ms);
+        c.launches += 2;
         return;
     }
     k_mf_minres_A<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
