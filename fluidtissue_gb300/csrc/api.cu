@@ -21,7 +21,7 @@ void free_all(Ctx& c) {
                     c.b, c.x, c.r, c.w64.q, c.w64.R[0], c.w64.R[1], c.w64.Y[0], c.w64.Y[1],
                     c.w64.W[0], c.w64.W[1], c.w64.X, c.w32.q, c.w32.R[0], c.w32.R[1],
                     c.w32.Y[0], c.w32.Y[1], c.w32.W[0], c.w32.W[1], c.w32.X, c.w32.r0, c.ms,
-                    c.os, c.red.partials, c.red.ticket, c.err_flag, c.bicg, c.mf_rec, c.mf_cube};
+                    c.os, c.red.partials, c.red.ticket, c.err_flag, c.bicg, c.mf_rec, c.mf_cube, c.mf_rows};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     mg_free(c.mg64);

@@ -188,6 +188,7 @@ struct Ctx {
     bool matfree = false;
     float* mf_rec = nullptr;   // FP32 element records of the matrix-free operator
     float* mf_cube = nullptr;  // per-cube corner sums of the lattice matrix-free operator
+    double* mf_rows = nullptr; // per-element rows of the FP64 matrix-free residual (16 per element)
 
     // preconditioner
     bool use_mg = false;
