@@ -187,7 +187,8 @@ struct Ctx {
     // operator representation: false = assembled BSR, true = element gather
     bool matfree = false;
     float* mf_rec = nullptr;   // FP32 element records of the matrix-free operator
-    float* mf_cube = nullptr;  // per-cube corner sums of the lattice matrix-free operator
+    float* mf_cube = nullptr;  // matrix-free FP32 partial sums: per cube (lattice form) or
+                               // per element row (record form)
     double* mf_rows = nullptr; // per-element rows of the FP64 matrix-free residual (16 per element)
 
     // preconditioner

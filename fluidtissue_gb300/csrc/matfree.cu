@@ -1,7 +1,8 @@
 // Matrix-free element operator for the large single solve (operator_kind =
 // FTS_OP_MATFREE, mixed precision, Kuhn lattices with the multigrid
-// preconditioner).  No block matrix is stored: y = S x is gathered per node
-// over the elements around it (atomic-free, deterministic):
+// preconditioner).  No block matrix is stored: each element's rows are applied
+// once and a thread per node adds the rows of the elements around it
+// (atomic-free, deterministic):
 //
 //   velocity row a, component r:
 //     mu V sum_c g_a[c] (G[r][c] + G[c][r])  -  V g_a[r] sum_b wq[b] p_b
@@ -19,8 +20,10 @@
 // (k_mf_cube), and a thread per node adds the corners it is of in the 8 cubes
 // around it, fused with the MINRES dots (k_mf_gather_minres_A); otherwise a
 // 64-byte FP32 record per element (gradients, volume, h^2, mu) built from the
-// FP64 geometry, each read by the element's 4 nodes (L2 reuse).
-// FP64 outer residual: the stored FP64 ElemGeom.
+// FP64 geometry, its rows applied by a thread per element (k_mf_elem32) and
+// gathered in the node-element map's order (k_mf_gather_map_minres_A).
+// FP64 outer residual: the stored FP64 ElemGeom, rows per element
+// (k_mf_elem64) gathered in the map's order (k_mf_residual64).
 #include <cfloat>
 
 #include "fts_device.cuh"
@@ -50,33 +53,6 @@ static MfConst mf_const() {
     return m;
 }
 
-// Row a of element k applied to the element's nodal values u[4][4] (ux,uy,uz,p).
-template <typename T>
-__device__ __forceinline__ void elem_row(const T g[4][3], T vol, T hh, T mu, int a,
-                                         const T u[4][4], T alpha, T eps, const T wq[4],
-                                         const T mref[4][4], T y[4]) {
-    T G[3][3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-            G[r][c] = u[0][r] * g[0][c] + u[1][r] * g[1][c] + u[2][r] * g[2][c] + u[3][r] * g[3][c];
-    T gp[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) gp[c] = u[0][3] * g[0][c] + u[1][3] * g[1][c] + u[2][3] * g[2][c] + u[3][3] * g[3][c];
-    const T pbar = wq[0] * u[0][3] + wq[1] * u[1][3] + wq[2] * u[2][3] + wq[3] * u[3][3];
-    const T mp = mref[a][0] * u[0][3] + mref[a][1] * u[1][3] + mref[a][2] * u[2][3] + mref[a][3] * u[3][3];
-    const T div = G[0][0] + G[1][1] + G[2][2];
-    const T mv = mu * vol;
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-        y[r] += mv * (g[a][0] * (G[r][0] + G[0][r]) + g[a][1] * (G[r][1] + G[1][r]) +
-                      g[a][2] * (G[r][2] + G[2][r])) -
-                vol * g[a][r] * pbar;
-    y[3] += -wq[a] * vol * div - alpha * hh * vol * (g[a][0] * gp[0] + g[a][1] * gp[1] + g[a][2] * gp[2]) -
-            eps * vol * mp;
-}
-
 // FP32 element records for the inner operator, 64 B per element: gradients
 // g[4][3], volume, h^2, mu (mu refreshed every solve), pad.
 struct alignas(64) ElemF32 {
@@ -99,68 +75,6 @@ __global__ void k_mf_records(int64_t nt, const ElemGeom* __restrict__ geom,
         R.mu = (float)mu[k];
         R.pad = 0.f;
         rec[k] = R;
-    }
-}
-
-// q = S (y + ycorr e_p) / beta over nodes (FP32), fused MINRES dots v.q, v.r1.
-__global__ void __launch_bounds__(kThreads)
-k_mf_minres_A(int64_t np, const int32_t* __restrict__ p2t_ptr, const uint32_t* __restrict__ p2t,
-              const int32_t* __restrict__ tets, const ElemF32* __restrict__ rec,
-              const uint8_t* __restrict__ bnd,
-              const V4<float>* __restrict__ Y, int ybuf, const V4<float>* __restrict__ R1,
-              V4<float>* __restrict__ q, float alpha, float eps, MfConst K, Reduction red,
-              MinresScalars* s) {
-    if (s->stop) return;
-    const float tinv = (float)(1.0 / s->beta);
-    const float wadd = (float)s->ycorr[ybuf];
-    double acc[2] = {0.0, 0.0};
-    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < np;
-         v += (int64_t)gridDim.x * blockDim.x) {
-        float y[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int32_t qq = p2t_ptr[v]; qq < p2t_ptr[v + 1]; ++qq) {
-            const uint32_t e = __ldg(p2t + qq);
-            const int64_t k = e >> 2;
-            const int a = e & 3;
-            const int4 t = __ldg(reinterpret_cast<const int4*>(tets) + k);
-            const int ids[4] = {t.x, t.y, t.z, t.w};
-            const float4* rp = reinterpret_cast<const float4*>(rec + k);
-            const float4 r0 = __ldg(rp), r1v = __ldg(rp + 1), r2 = __ldg(rp + 2), r3 = __ldg(rp + 3);
-            const float g[4][3] = {{r0.x, r0.y, r0.z}, {r0.w, r1v.x, r1v.y},
-                                   {r1v.z, r1v.w, r2.x}, {r2.y, r2.z, r2.w}};
-            const float vol = r3.x, hh = r3.y, mue = r3.z;
-            float u[4][4];
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const V4<float> xv = Y[ids[b]];
-                const bool d = __ldg(bnd + ids[b]) != 0;
-                u[b][0] = d ? 0.f : xv.x;
-                u[b][1] = d ? 0.f : xv.y;
-                u[b][2] = d ? 0.f : xv.z;
-                u[b][3] = xv.w + wadd;
-            }
-            elem_row<float>(g, vol, hh, mue, a, u, alpha, eps, K.wq, K.mref, y);
-        }
-        const V4<float> yv = Y[v];
-        if (bnd[v]) {
-            y[0] = yv.x;
-            y[1] = yv.y;
-            y[2] = yv.z;
-        }
-        V4<float> o;
-        o.x = y[0] * tinv;
-        o.y = y[1] * tinv;
-        o.z = y[2] * tinv;
-        o.w = y[3] * tinv;
-        q[v] = o;
-        const V4<float> r1 = R1[v];
-        const float v0 = yv.x * tinv, v1 = yv.y * tinv, v2 = yv.z * tinv, v3 = (yv.w + wadd) * tinv;
-        acc[0] += (double)(v0 * o.x) + (double)(v1 * o.y) + (double)(v2 * o.z) + (double)(v3 * o.w);
-        acc[1] += (double)(v0 * r1.x) + (double)(v1 * r1.y) + (double)(v2 * r1.z) + (double)(v3 * r1.w);
-    }
-    double tot[2];
-    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
-        const double c1 = s->iters >= 1 ? s->beta / s->oldb : 0.0;
-        s->alfa = tot[0] - c1 * tot[1];
     }
 }
 
@@ -230,9 +144,9 @@ __device__ __forceinline__ void tet_geom_f32(const float p[4][3], float g[4][3],
     hh = h * h;
 }
 
-// The four rows of one element applied to its nodal values u[4][4], each row
-// by the expressions of elem_row (the velocity gradient and the pressure sums
-// formed once for the four).
+// The four rows a of one element applied to its nodal values u[4][4]
+// (ux, uy, uz, p): the velocity gradient G and the pressure sums formed once,
+// then per row the weak forms of the header.
 template <typename T>
 __device__ __forceinline__ void elem_apply4(const T g[4][3], T vol, T hh, T mu, const T u[4][4],
                                             T alpha, T eps, const T wq[4], const T mref[4][4],
@@ -387,6 +301,94 @@ k_mf_gather_minres_A(int n, int64_t np, const float* __restrict__ cube,
     }
 }
 
+// The record form (any element order): a thread per element applies its four
+// rows from its 64-byte record (k_mf_elem32, rows[4 k + a]); a thread per node
+// adds the rows of its elements in the node-element map's order, fused with
+// the MINRES dots (k_mf_gather_map_minres_A).
+__global__ void __launch_bounds__(kThreads)
+k_mf_elem32(int64_t nt, const int32_t* __restrict__ tets, const ElemF32* __restrict__ rec,
+            const uint8_t* __restrict__ bnd, const V4<float>* __restrict__ Y, int ybuf,
+            float alpha, float eps, MfConst K, const MinresScalars* __restrict__ s,
+            V4<float>* __restrict__ rows) {
+    if (s->stop) return;
+    const float wadd = (float)s->ycorr[ybuf];
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nt;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int4 t = __ldg(reinterpret_cast<const int4*>(tets) + k);
+        const int ids[4] = {t.x, t.y, t.z, t.w};
+        const float4* rp = reinterpret_cast<const float4*>(rec + k);
+        const float4 r0 = __ldg(rp), r1v = __ldg(rp + 1), r2 = __ldg(rp + 2), r3 = __ldg(rp + 3);
+        const float g[4][3] = {{r0.x, r0.y, r0.z}, {r0.w, r1v.x, r1v.y},
+                               {r1v.z, r1v.w, r2.x}, {r2.y, r2.z, r2.w}};
+        float u[4][4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const V4<float> xv = Y[ids[b]];
+            const bool d = __ldg(bnd + ids[b]) != 0;
+            u[b][0] = d ? 0.f : xv.x;
+            u[b][1] = d ? 0.f : xv.y;
+            u[b][2] = d ? 0.f : xv.z;
+            u[b][3] = xv.w + wadd;
+        }
+        float y[4][4];
+        elem_apply4<float>(g, r3.x, r3.y, r3.z, u, alpha, eps, K.wq, K.mref, y);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            V4<float> o;
+            o.x = y[a][0];
+            o.y = y[a][1];
+            o.z = y[a][2];
+            o.w = y[a][3];
+            rows[4 * k + a] = o;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_mf_gather_map_minres_A(int64_t np, const int32_t* __restrict__ p2t_ptr,
+                         const uint32_t* __restrict__ p2t, const V4<float>* __restrict__ rows,
+                         const uint8_t* __restrict__ bnd, const V4<float>* __restrict__ Y,
+                         int ybuf, const V4<float>* __restrict__ R1, V4<float>* __restrict__ q,
+                         Reduction red, MinresScalars* s) {
+    if (s->stop) return;
+    const float tinv = (float)(1.0 / s->beta);
+    const float wadd = (float)s->ycorr[ybuf];
+    double acc[2] = {0.0, 0.0};
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < np;
+         v += (int64_t)gridDim.x * blockDim.x) {
+        float y[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int32_t qq = p2t_ptr[v]; qq < p2t_ptr[v + 1]; ++qq) {
+            const uint32_t e = __ldg(p2t + qq);
+            const V4<float> row = rows[4 * (int64_t)(e >> 2) + (e & 3)];
+            y[0] += row.x;
+            y[1] += row.y;
+            y[2] += row.z;
+            y[3] += row.w;
+        }
+        const V4<float> yv = Y[v];
+        if (bnd[v]) {
+            y[0] = yv.x;
+            y[1] = yv.y;
+            y[2] = yv.z;
+        }
+        V4<float> o;
+        o.x = y[0] * tinv;
+        o.y = y[1] * tinv;
+        o.z = y[2] * tinv;
+        o.w = y[3] * tinv;
+        q[v] = o;
+        const V4<float> r1 = R1[v];
+        const float v0 = yv.x * tinv, v1 = yv.y * tinv, v2 = yv.z * tinv, v3 = (yv.w + wadd) * tinv;
+        acc[0] += (double)(v0 * o.x) + (double)(v1 * o.y) + (double)(v2 * o.z) + (double)(v3 * o.w);
+        acc[1] += (double)(v0 * r1.x) + (double)(v1 * r1.y) + (double)(v2 * r1.z) + (double)(v3 * r1.w);
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
+        const double c1 = s->iters >= 1 ? s->beta / s->oldb : 0.0;
+        s->alfa = tot[0] - c1 * tot[1];
+    }
+}
+
 __global__ void k_mu_f32(int64_t nt, const double* __restrict__ mu, float* __restrict__ muf) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nt;
          k += (int64_t)gridDim.x * blockDim.x)
@@ -524,10 +526,14 @@ void launch_mf_minres_A(Ctx& c, const V4<float>* Y, int ybuf, const V4<float>* R
         c.launches += 2;
         return;
     }
-    k_mf_minres_A<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
-        c.np, c.p2t_ptr, c.p2t, c.tets, reinterpret_cast<const ElemF32*>(c.mf_rec), c.bnd, Y,
-        ybuf, R1, q, (float)c.par.alpha, (float)c.par.eps, K, c.red, c.ms);
-    c.launches += 1;
+    if (!c.mf_cube) c.mf_cube = dev_alloc<float>(c, (size_t)c.nt * 16);  // rows[4 nt]
+    V4<float>* rows = reinterpret_cast<V4<float>*>(c.mf_cube);
+    k_mf_elem32<<<grid_for(c, c.nt), kThreads, 0, c.stream>>>(
+        c.nt, c.tets, reinterpret_cast<const ElemF32*>(c.mf_rec), c.bnd, Y, ybuf,
+        (float)c.par.alpha, (float)c.par.eps, K, c.ms, rows);
+    k_mf_gather_map_minres_A<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
+        c.np, c.p2t_ptr, c.p2t, rows, c.bnd, Y, ybuf, R1, q, c.red, c.ms);
+    c.launches += 2;
 }
 
 void launch_mf_residual64(Ctx& c) {
