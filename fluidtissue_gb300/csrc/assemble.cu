@@ -397,6 +397,7 @@ void ensure_bsr64(Ctx& c) {
 // 129^3); here each thread walks one node's elements with no search and no
 // shared-memory staging.
 // ---------------------------------------------------------------------------
+template <bool KUHN>
 __global__ void __launch_bounds__(kThreads)
 k_assemble_lat(int n, const int32_t* __restrict__ p2t_ptr, const uint32_t* __restrict__ p2t,
                const int32_t* __restrict__ tets, const ElemGeom* __restrict__ geom,
@@ -415,14 +416,8 @@ k_assemble_lat(int n, const int32_t* __restrict__ p2t_ptr, const uint32_t* __res
 #pragma unroll
         for (int e = 0; e < 16; ++e) blk[e] = 0.0;
         if (w >= 0) {
-            for (int32_t q = p2t_ptr[v]; q < p2t_ptr[v + 1]; ++q) {
-                const uint32_t pk = p2t[q];
-                const int64_t el = pk >> 2;
-                const int a = pk & 3;
-                const int4 tt = reinterpret_cast<const int4*>(tets)[el];
-                const int b =
-                    tt.x == w ? 0 : (tt.y == w ? 1 : (tt.z == w ? 2 : (tt.w == w ? 3 : -1)));
-                if (b < 0) continue;
+            // the elements holding v and w, in the node-element map's order
+            auto add = [&](int64_t el, int a, int b) {
                 const ElemGeom* G = geom + el;
                 const double ga[3] = {G->g[a][0], G->g[a][1], G->g[a][2]};
                 const double gb[3] = {G->g[b][0], G->g[b][1], G->g[b][2]};
@@ -439,6 +434,18 @@ k_assemble_lat(int n, const int32_t* __restrict__ p2t_ptr, const uint32_t* __res
 #pragma unroll
                 for (int cc = 0; cc < 3; ++cc) blk[12 + cc] += -(gb[cc] * R.wq[a] * vol);
                 blk[15] += -(alpha * (G->hh * vol * gg) + eps * (vol * R.mref[a][b]));
+            };
+            if (KUHN) {  // generator's element order: the elements follow from the lattice
+                kuhn_pair_elements(n, i, j, k, d, add);
+            } else {
+                for (int32_t q = p2t_ptr[v]; q < p2t_ptr[v + 1]; ++q) {
+                    const uint32_t pk = p2t[q];
+                    const int64_t el = pk >> 2;
+                    const int4 tt = reinterpret_cast<const int4*>(tets)[el];
+                    const int b =
+                        tt.x == w ? 0 : (tt.y == w ? 1 : (tt.z == w ? 2 : (tt.w == w ? 3 : -1)));
+                    if (b >= 0) add(el, (int)(pk & 3), b);
+                }
             }
             const bool bi = bnd[v] != 0, bw = bnd[w] != 0;
 #pragma unroll
@@ -471,9 +478,14 @@ void launch_assemble_lat(Ctx& c) {
         FTS_CUDA(cudaMemsetAsync(c.lat64, 0, (size_t)tiles * 64 * 32 * sizeof(double2),
                                  c.stream));
     }
-    k_assemble_lat<<<grid_for(c, c.np * 8), kThreads, 0, c.stream>>>(
-        n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.bnd, c.par.alpha, c.par.eps, ref_args(),
-        c.lat64, reinterpret_cast<float4*>(c.lat_val));
+    if (c.topo.kuhn_elements)
+        k_assemble_lat<true><<<grid_for(c, c.np * 8), kThreads, 0, c.stream>>>(
+            n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.bnd, c.par.alpha, c.par.eps, ref_args(),
+            c.lat64, reinterpret_cast<float4*>(c.lat_val));
+    else
+        k_assemble_lat<false><<<grid_for(c, c.np * 8), kThreads, 0, c.stream>>>(
+            n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.bnd, c.par.alpha, c.par.eps, ref_args(),
+            c.lat64, reinterpret_cast<float4*>(c.lat_val));
     FTS_CUDA(cudaGetLastError());
     c.launches += 1;
     c.a64_valid = false;

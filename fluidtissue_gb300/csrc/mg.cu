@@ -164,7 +164,7 @@ __global__ void k_mg_extract_lat(int n, const double2* __restrict__ L, T* __rest
 // K(v, v + off[d]) = sum over elements holding both nodes of
 // mu vol (delta_rc g_a.g_b + g_a[c] g_b[r]) (Flow.cpp:136-153); Dirichlet rows
 // identity, Dirichlet columns zero.
-template <typename T>
+template <typename T, bool KUHN>
 __global__ void k_mg_from_elements(int n, const int32_t* __restrict__ p2t_ptr,
                                    const uint32_t* __restrict__ p2t,
                                    const int32_t* __restrict__ tets,
@@ -182,17 +182,7 @@ __global__ void k_mg_from_elements(int n, const int32_t* __restrict__ p2t_ptr,
         if (bnd[v]) {
             if (d == 0) blk[0] = blk[4] = blk[8] = 1.0;
         } else if (w >= 0 && !bnd[w]) {
-            for (int32_t q = p2t_ptr[v]; q < p2t_ptr[v + 1]; ++q) {
-                const uint32_t e = p2t[q];
-                const int64_t el = e >> 2;
-                const int a = e & 3;
-                const int4 tt = reinterpret_cast<const int4*>(tets)[el];
-                const int ids[4] = {tt.x, tt.y, tt.z, tt.w};
-                int b = -1;
-#pragma unroll
-                for (int m = 0; m < 4; ++m)
-                    if (ids[m] == w) b = m;
-                if (b < 0) continue;
+            auto add = [&](int64_t el, int a, int b) {
                 const ElemGeom& G = geom[el];
                 const double mv = mu[el] * G.vol;
                 const double gg = G.g[a][0] * G.g[b][0] + G.g[a][1] * G.g[b][1] + G.g[a][2] * G.g[b][2];
@@ -201,6 +191,18 @@ __global__ void k_mg_from_elements(int n, const int32_t* __restrict__ p2t_ptr,
 #pragma unroll
                     for (int cc = 0; cc < 3; ++cc)
                         blk[3 * r + cc] += mv * ((r == cc ? gg : 0.0) + G.g[a][cc] * G.g[b][r]);
+            };
+            if (KUHN) {  // generator's element order: the elements follow from the lattice
+                kuhn_pair_elements(n, i, j, k, d, add);
+            } else {
+                for (int32_t q = p2t_ptr[v]; q < p2t_ptr[v + 1]; ++q) {
+                    const uint32_t e = p2t[q];
+                    const int64_t el = e >> 2;
+                    const int4 tt = reinterpret_cast<const int4*>(tets)[el];
+                    const int b =
+                        tt.x == w ? 0 : (tt.y == w ? 1 : (tt.z == w ? 2 : (tt.w == w ? 3 : -1)));
+                    if (b >= 0) add(el, (int)(e & 3), b);
+                }
             }
         }
 #pragma unroll
@@ -615,8 +617,11 @@ template <typename T>
 void mg_setup(Ctx& c, MG<T>& mg) {
     mg_build<T>(c, mg);
     MGLevel<T>& F = mg.L[0];
-    if (c.matfree)
-        k_mg_from_elements<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
+    if (c.matfree && c.topo.kuhn_elements)
+        k_mg_from_elements<T, true><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
+            F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.bnd, F.K);
+    else if (c.matfree)
+        k_mg_from_elements<T, false><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
             F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.bnd, F.K);
     else if (c.use_lat64)
         k_mg_extract_lat<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(F.n, c.lat64, F.K);

@@ -47,6 +47,43 @@ __device__ __forceinline__ int nbr(int i, int j, int k, int d, int n) {
     return a + n * (b + n * c);
 }
 
+// Kuhn lattice in the generator's element order: element 6c + t of cube c is
+// the monotone path 0 -> e_p0 -> e_p0 + e_p1 -> (1,1,1) of axis permutation t
+// ({0,1,2} {0,2,1} {1,0,2} {1,2,0} {2,0,1} {2,1,0}), its local vertex a the
+// corner at place a on the path.
+__host__ __device__ __forceinline__ constexpr int kuhn_p0(int t) { return t >> 1; }
+__host__ __device__ __forceinline__ constexpr int kuhn_p1(int t) {
+    return (t == 0 || t == 5) ? 1 : ((t == 1 || t == 3) ? 2 : 0);
+}
+
+// The elements holding both v = (i, j, k) and w = v + off(d) (d = 0..7, w
+// inside the lattice), in ascending element index (the order of the
+// node-element map): f(el, a, b) with a, b the local indices of v and w.  The
+// node's corner q in a cube (bits x, y, z) runs from 7 down to 0, which is
+// ascending cube index; w is corner q | off(d) of that cube when the two
+// share no bit; an element holds a corner when the corner lies on its path.
+template <typename F>
+__device__ __forceinline__ void kuhn_pair_elements(int n, int i, int j, int k, int d, F&& f) {
+    const int m = n - 1;
+    const int od = off_x(d) | (off_y(d) << 1) | (off_z(d) << 2);
+#pragma unroll
+    for (int q = 7; q >= 0; --q) {
+        if (q & od) continue;
+        const int ci = i - (q & 1), cj = j - ((q >> 1) & 1), ck = k - (q >> 2);
+        if (ci < 0 || cj < 0 || ck < 0 || ci >= m || cj >= m || ck >= m) continue;
+        const int64_t cube = ci + (int64_t)m * (cj + (int64_t)m * ck);
+        const int qw = q | od;
+        const int a = __popc(q), b = __popc(qw);
+#pragma unroll
+        for (int t = 0; t < 6; ++t) {
+            const int c1 = 1 << kuhn_p0(t), c2 = c1 | (1 << kuhn_p1(t));
+            const bool hv = q == 0 || q == 7 || q == c1 || q == c2;
+            const bool hw = qw == 0 || qw == 7 || qw == c1 || qw == c2;
+            if (hv && hw) f(6 * cube + t, a, b);
+        }
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ T ldk(const T* p) {
     return *p;

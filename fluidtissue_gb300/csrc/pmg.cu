@@ -113,7 +113,7 @@ struct PRef {
 // Fine level from the elements (matrix-free mode): sum over the elements
 // holding v and v + off[d] of alpha h^2 vol g_a.g_b + eps vol Mref[a][b]
 // (the pressure block of Flow.cpp's composition), plus w on the diagonal.
-template <typename T>
+template <typename T, bool KUHN>
 __global__ void k_pmg_from_elements(int n, const int32_t* __restrict__ p2t_ptr,
                                     const uint32_t* __restrict__ p2t,
                                     const int32_t* __restrict__ tets,
@@ -129,21 +129,23 @@ __global__ void k_pmg_from_elements(int n, const int32_t* __restrict__ p2t_ptr,
         const int w = nbr(i, j, k, d, n);
         double val = 0.0;
         if (w >= 0) {
-            for (int32_t q = p2t_ptr[v]; q < p2t_ptr[v + 1]; ++q) {
-                const uint32_t e = p2t[q];
-                const int64_t el = e >> 2;
-                const int a = e & 3;
-                const int4 tt = reinterpret_cast<const int4*>(tets)[el];
-                const int ids[4] = {tt.x, tt.y, tt.z, tt.w};
-                int b = -1;
-#pragma unroll
-                for (int m = 0; m < 4; ++m)
-                    if (ids[m] == w) b = m;
-                if (b < 0) continue;
+            auto add = [&](int64_t el, int a, int b) {
                 const ElemGeom& G = geom[el];
                 const double gg = G.g[a][0] * G.g[b][0] + G.g[a][1] * G.g[b][1] +
                                   G.g[a][2] * G.g[b][2];
                 val += alpha * (G.hh * G.vol * gg) + eps * (G.vol * R.mref[a][b]);
+            };
+            if (KUHN) {  // generator's element order: the elements follow from the lattice
+                kuhn_pair_elements(n, i, j, k, d, add);
+            } else {
+                for (int32_t q = p2t_ptr[v]; q < p2t_ptr[v + 1]; ++q) {
+                    const uint32_t e = p2t[q];
+                    const int64_t el = e >> 2;
+                    const int4 tt = reinterpret_cast<const int4*>(tets)[el];
+                    const int b =
+                        tt.x == w ? 0 : (tt.y == w ? 1 : (tt.z == w ? 2 : (tt.w == w ? 3 : -1)));
+                    if (b >= 0) add(el, (int)(e & 3), b);
+                }
             }
         }
         if (d == 0) val += lumped_inv_mu(v, p2t_ptr, p2t, geom, mu);
@@ -404,8 +406,12 @@ void pmg_setup(Ctx& c, PMG<T>& pm) {
         PRef pr;
         for (int a = 0; a < 4; ++a)
             for (int b = 0; b < 4; ++b) pr.mref[a][b] = R.mref[a][b];
-        k_pmg_from_elements<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
-            F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.par.alpha, c.par.eps, pr, F.K);
+        if (c.topo.kuhn_elements)
+            k_pmg_from_elements<T, true><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
+                F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.par.alpha, c.par.eps, pr, F.K);
+        else
+            k_pmg_from_elements<T, false><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
+                F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.par.alpha, c.par.eps, pr, F.K);
     } else if (c.use_lat64) {
         k_pmg_extract_lat<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
             F.n, c.lat64, c.p2t_ptr, c.p2t, c.geom, c.mu, F.K);

@@ -183,6 +183,7 @@ static bool kuhn_element_order(const fts_mesh& m, int32_t n) {
     static const int perm[6][2] = {{0, 1}, {0, 2}, {1, 0}, {1, 2}, {2, 0}, {2, 1}};
     const int64_t nn = n, cm = n - 1;
     const int64_t step[3] = {1, nn, nn * nn};
+    if (m.nt != 6 * cm * cm * cm) return false;  // exactly the lattice's elements
     bool ok = true;
 #pragma omp parallel for schedule(static) reduction(&& : ok)
     for (int64_t c = 0; c < cm * cm * cm; ++c) {
