@@ -587,64 +587,102 @@ __device__ __forceinline__ void st_point(const float* __restrict__ xyz, const do
 
 __constant__ int c_st_edge[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
 
-// Patch area of each crossing edge (i, j), i < j: the edge's thread walks the
-// elements of i in index order, keeps those holding j, rebuilds their
-// triangles and adds those that contain the edge's point.  nif counts the
-// crossing edges, atot sums the areas (each triangle three times).
-__global__ void k_st_areas(int64_t np, const int32_t* __restrict__ rowptr,
-                           const int32_t* __restrict__ cols, const int32_t* __restrict__ p2t_ptr,
-                           const uint32_t* __restrict__ p2t, const int32_t* __restrict__ tets,
-                           const float* __restrict__ xyz, const double* __restrict__ phi,
-                           float* __restrict__ area, unsigned* __restrict__ nif,
-                           double* __restrict__ atot, int* __restrict__ bad) {
+// The crossing edges (i, j), i < j, whose ends differ in sign bit, as (i, edge
+// slot q) in list[]; nif counts them.
+__global__ void k_st_cross_list(int64_t np, const int32_t* __restrict__ rowptr,
+                                const int32_t* __restrict__ cols, const double* __restrict__ phi,
+                                int2* __restrict__ list, unsigned cap, unsigned* __restrict__ nif) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
          i += (int64_t)gridDim.x * blockDim.x) {
         const bool si = signbit(phi[i]);
         for (int32_t q = rowptr[i]; q < rowptr[i + 1]; ++q) {
             const int32_t j = cols[q];
             if (j <= i || signbit(phi[j]) == si) continue;
-            float A = 0.f;
-            for (int32_t e = p2t_ptr[i]; e < p2t_ptr[i + 1]; ++e) {
+            const unsigned at = atomicAdd(nif, 1u);
+            if (at < cap) list[at] = make_int2((int)i, q);
+        }
+    }
+}
+
+// Patch area of each crossing edge (i, j): a warp per edge, a lane per
+// element of i (in index order, 32 at a time); a lane whose element holds j
+// rebuilds the element's triangles (local edge order 01 02 03 12 13 23) and
+// keeps those that contain the edge's point; lane 0 then adds the kept
+// triangle areas in element order, A = (float)((double)A + 0.5 |cross|), the
+// sequence of the element-by-element walk.  atot sums the areas (each
+// triangle three times).
+__global__ void k_st_areas(const int2* __restrict__ list, const unsigned* __restrict__ nif,
+                           unsigned cap, const int32_t* __restrict__ cols,
+                           const int32_t* __restrict__ p2t_ptr, const uint32_t* __restrict__ p2t,
+                           const int32_t* __restrict__ tets, const float* __restrict__ xyz,
+                           const double* __restrict__ phi, float* __restrict__ area,
+                           double* __restrict__ atot, int* __restrict__ bad) {
+    const int lane = threadIdx.x & 31;
+    const unsigned n = min(*nif, cap);
+    for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < n;
+         w += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        const int2 ed = list[w];
+        const int32_t i = ed.x, q = ed.y, j = cols[q];
+        const int32_t e0 = p2t_ptr[i], e1 = p2t_ptr[i + 1];
+        float A = 0.f;
+        for (int32_t eb = e0; eb < e1; eb += 32) {
+            double t[2] = {0.0, 0.0};
+            int nt = 0;
+            const int32_t e = eb + lane;
+            if (e < e1) {
                 const int64_t k = p2t[e] >> 2;
                 const int4 tt = reinterpret_cast<const int4*>(tets)[k];
                 const int ids[4] = {tt.x, tt.y, tt.z, tt.w};
-                if (ids[0] != j && ids[1] != j && ids[2] != j && ids[3] != j) continue;
-                float pts[4][3];
-                int mine = -1, ne = 0;
-                for (int m = 0; m < 6; ++m) {
-                    const int a = ids[c_st_edge[m][0]], b = ids[c_st_edge[m][1]];
-                    if (signbit(phi[a]) == signbit(phi[b])) continue;
-                    if (ne == 4) {
-                        atomicOr(bad, 1);
-                        break;
+                if (ids[0] == j || ids[1] == j || ids[2] == j || ids[3] == j) {
+                    float pts[4][3];
+                    int mine = -1, ne = 0;
+                    bool over = false;
+                    for (int m = 0; m < 6; ++m) {
+                        const int a = ids[c_st_edge[m][0]], b = ids[c_st_edge[m][1]];
+                        if (signbit(phi[a]) == signbit(phi[b])) continue;
+                        if (ne == 4) {
+                            over = true;
+                            break;
+                        }
+                        const int lo = min(a, b), hi = max(a, b);
+                        if (lo == i && hi == j) mine = ne;
+                        st_point(xyz, phi, lo, hi, pts[ne]);
+                        ++ne;
                     }
-                    const int lo = min(a, b), hi = max(a, b);
-                    if (lo == i && hi == j) mine = ne;
-                    st_point(xyz, phi, lo, hi, pts[ne]);
-                    ++ne;
-                }
-                if (ne != 3 && ne != 4) {
-                    atomicOr(bad, 1);
-                    continue;
-                }
-                const int tri[2][3] = {{0, ne == 3 ? 1 : 2, ne == 3 ? 2 : 3}, {0, 1, 3}};
-                for (int tr = 0; tr < (ne == 3 ? 1 : 2); ++tr) {
-                    if (tri[tr][0] != mine && tri[tr][1] != mine && tri[tr][2] != mine) continue;
-                    const float* p0 = pts[tri[tr][0]];
-                    const float* p1 = pts[tri[tr][1]];
-                    const float* p2 = pts[tri[tr][2]];
-                    const float e1x = __fsub_rn(p1[0], p0[0]), e1y = __fsub_rn(p1[1], p0[1]),
-                                e1z = __fsub_rn(p1[2], p0[2]);
-                    const float e2x = __fsub_rn(p2[0], p0[0]), e2y = __fsub_rn(p2[1], p0[1]),
-                                e2z = __fsub_rn(p2[2], p0[2]);
-                    const float cx = __fsub_rn(__fmul_rn(e1y, e2z), __fmul_rn(e1z, e2y));
-                    const float cy = __fsub_rn(__fmul_rn(e1z, e2x), __fmul_rn(e1x, e2z));
-                    const float cz = __fsub_rn(__fmul_rn(e1x, e2y), __fmul_rn(e1y, e2x));
-                    A = (float)((double)A + 0.5 * (double)st_norm3(cx, cy, cz));
+                    if (over || (ne != 3 && ne != 4)) {
+                        atomicOr(bad, 1);
+                    }
+                    if (ne == 3 || ne == 4) {
+                        const int tri[2][3] = {{0, ne == 3 ? 1 : 2, ne == 3 ? 2 : 3}, {0, 1, 3}};
+                        for (int tr = 0; tr < (ne == 3 ? 1 : 2); ++tr) {
+                            if (tri[tr][0] != mine && tri[tr][1] != mine && tri[tr][2] != mine)
+                                continue;
+                            const float* p0 = pts[tri[tr][0]];
+                            const float* p1 = pts[tri[tr][1]];
+                            const float* p2 = pts[tri[tr][2]];
+                            const float e1x = __fsub_rn(p1[0], p0[0]), e1y = __fsub_rn(p1[1], p0[1]),
+                                        e1z = __fsub_rn(p1[2], p0[2]);
+                            const float e2x = __fsub_rn(p2[0], p0[0]), e2y = __fsub_rn(p2[1], p0[1]),
+                                        e2z = __fsub_rn(p2[2], p0[2]);
+                            const float cx = __fsub_rn(__fmul_rn(e1y, e2z), __fmul_rn(e1z, e2y));
+                            const float cy = __fsub_rn(__fmul_rn(e1z, e2x), __fmul_rn(e1x, e2z));
+                            const float cz = __fsub_rn(__fmul_rn(e1x, e2y), __fmul_rn(e1y, e2x));
+                            t[nt++] = 0.5 * (double)st_norm3(cx, cy, cz);
+                        }
+                    }
                 }
             }
+            // the additions in element order (lane 0 replays them)
+            for (int l = 0; l < 32; ++l) {
+                const int c = __shfl_sync(0xffffffffu, nt, l);
+                const double t0 = __shfl_sync(0xffffffffu, t[0], l);
+                const double t1 = __shfl_sync(0xffffffffu, t[1], l);
+                if (c >= 1) A = (float)((double)A + t0);
+                if (c >= 2) A = (float)((double)A + t1);
+            }
+        }
+        if (lane == 0) {
             area[q] = A;
-            atomicAdd(nif, 1u);
             atomicAdd(atot, (double)A);
         }
     }
@@ -729,6 +767,8 @@ struct fts_ls {
     float* st_gn = nullptr;      // [3][np] normalised components
     float* st_k = nullptr;       // [np] nodal curvature
     float* st_area = nullptr;    // [nnz] patch area per crossing edge slot
+    int2* st_list = nullptr;     // crossing edges (node, edge slot)
+    unsigned st_list_cap = 0;
     double* st_force = nullptr;  // [3 np]
     double* st_acc = nullptr;    // total area (x3)
 };
@@ -747,7 +787,7 @@ void ls_free(fts_ls& S) {
                     S.L,
                     S.flow, S.phi, S.keep, S.ifp, S.count, S.flag, S.norm2, S.S,
                     S.red.partials, S.red.ticket, S.st_phi, S.st_ifn, S.st_ge, S.st_nrm,
-                    S.st_gn, S.st_k, S.st_area, S.st_force, S.st_acc};
+                    S.st_gn, S.st_k, S.st_area, S.st_force, S.st_acc, S.st_list};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (double* p : S.vec)
@@ -1059,6 +1099,9 @@ int fts_ls_surface_tension(fts_ls* S, const double* phi, const double* phi_reset
             S->st_area = ls_alloc<float>(S->nnz);
             S->st_force = ls_alloc<double>(3 * np);
             S->st_acc = ls_alloc<double>(1);
+            // every edge once at most
+            S->st_list_cap = (unsigned)std::min<int64_t>((S->nnz - np) / 2 + 1, 0x7fffffff);
+            S->st_list = ls_alloc<int2>(S->st_list_cap);
         }
         FTS_CUDA(cudaMemcpyAsync(S->st_phi, phi, np * sizeof(double), cudaMemcpyHostToDevice, s));
         const double* ifn = S->vec[11];
@@ -1079,9 +1122,11 @@ int fts_ls_surface_tension(fts_ls* S, const double* phi, const double* phi_reset
         k_st_elem_div<<<ge, kLsThreads, 0, s>>>(nt, S->tets, S->geom, S->st_gn, np, S->st_ge);
         k_st_node_avg<<<gn, kLsThreads, 0, s>>>(np, S->p2t_ptr, S->p2t, S->st_ge, 1, S->st_nrm,
                                                 S->st_gn, S->st_k);
-        k_st_areas<<<gn, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->p2t_ptr, S->p2t, S->tets,
-                                             S->xyz, S->st_phi, S->st_area, S->count, S->st_acc,
-                                             S->flag);
+        k_st_cross_list<<<gn, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->st_phi, S->st_list,
+                                                  S->st_list_cap, S->count);
+        k_st_areas<<<S->num_sms * 8, kLsThreads, 0, s>>>(
+            S->st_list, S->count, S->st_list_cap, S->cols, S->p2t_ptr, S->p2t, S->tets, S->xyz,
+            S->st_phi, S->st_area, S->st_acc, S->flag);
         k_st_force<<<gn, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, S->st_phi, S->st_area,
                                              S->st_k, S->st_nrm, (float)surface_tension,
                                              (int)node_density, S->st_force);
@@ -1101,7 +1146,7 @@ int fts_ls_surface_tension(fts_ls* S, const double* phi, const double* phi_reset
         st.ms_kernels = ms;
         st.interface_points = nif;
         st.area = atot / 3.0;
-        st.kernel_launches = 6;
+        st.kernel_launches = 7;
         if (bad) {
             S->last_error = "an element crosses the interface on other than 3 or 4 edges";
             rc = FTS_ERR_BAD_INPUT;
