@@ -252,11 +252,15 @@ __global__ void k_ls_system(int64_t np, const int32_t* __restrict__ rowptr,
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
          i += (int64_t)gridDim.x * blockDim.x) {
         double acc = 0.0, d = 0.0;
-        for (int32_t q = rowptr[i]; q < rowptr[i + 1]; ++q) {
-            const double l = M[q] + h * A[q];
+        const int32_t q0 = rowptr[i], q1 = rowptr[i + 1];
+#pragma unroll 4
+        for (int32_t q = q0; q < q1; ++q) {  // unrolled: the loads of 4 entries in flight
+            const double m = M[q], a = A[q];
+            const int32_t j = cols[q];
+            const double l = m + h * a;
             L[q] = l;
-            acc += (M[q] - h * A[q]) * phi[cols[q]];
-            if (cols[q] == i) d = l;
+            acc += (m - h * a) * phi[j];
+            if (j == i) d = l;
         }
         b[i] = acc;
         inv[i] = d != 0.0 ? 1.0 / d : 1.0;
@@ -275,7 +279,9 @@ __device__ __forceinline__ double csr_row(const int32_t* __restrict__ rowptr,
                                           const double* __restrict__ L,
                                           const double* __restrict__ v, int64_t i) {
     double acc = 0.0;
-    for (int32_t q = rowptr[i]; q < rowptr[i + 1]; ++q) acc += L[q] * v[cols[q]];
+    const int32_t q0 = rowptr[i], q1 = rowptr[i + 1];
+#pragma unroll 4
+    for (int32_t q = q0; q < q1; ++q) acc += L[q] * v[cols[q]];
     return acc;
 }
 
