@@ -28,6 +28,7 @@
 
 #include "fts_device.cuh"
 #include "mg.cuh"
+#include "mg_device.cuh"
 #include "reduce.cuh"
 
 namespace fts {
@@ -90,19 +91,6 @@ __global__ void k_mf_records(int64_t nt, const ElemGeom* __restrict__ geom,
 // first version of this operator) the geometry was formed four times and the
 // kernel took 4.94 ms at 257^3 against 2.04 ms for the two phases.
 // ---------------------------------------------------------------------------
-// First two axes of the path of permutation t: {0,1,2} {0,2,1} {1,0,2}
-// {1,2,0} {2,0,1} {2,1,0} (the lattice generator's order).
-__device__ __forceinline__ void lat_path(int t, int& p0, int& p1) {
-    switch (t) {
-        case 0: p0 = 0; p1 = 1; break;
-        case 1: p0 = 0; p1 = 2; break;
-        case 2: p0 = 1; p1 = 0; break;
-        case 3: p0 = 1; p1 = 2; break;
-        case 4: p0 = 2; p1 = 0; break;
-        default: p0 = 2; p1 = 1; break;
-    }
-}
-
 // FP32 geometry of a tetrahedron from its 4 vertices (the same formulas as the
 // FP64 element geometry: B = [p1-p0, p2-p0, p3-p0], g = invB^T ghat, V = |det|/6,
 // h = cbrt|det|, h^2 in float).
@@ -214,9 +202,7 @@ k_mf_cube(int n, const float* __restrict__ xyz, const float* __restrict__ muf,
         }
 #pragma unroll
         for (int t = 0; t < 6; ++t) {
-            int p0, p1;
-            lat_path(t, p0, p1);
-            const int q1 = 1 << p0, q2 = q1 | (1 << p1);
+            const int q1 = 1 << kuhn_p0(t), q2 = q1 | (1 << kuhn_p1(t));
             const int cq[4] = {0, q1, q2, 7};
             float pe[4][3], ue[4][4];
 #pragma unroll
