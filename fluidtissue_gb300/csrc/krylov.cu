@@ -790,6 +790,18 @@ template long long minres_inner<float>(Ctx&, double, long long, double*, int*);
 
 template <typename T>
 void setup_preconditioner(Ctx& c) {
+    if (c.use_mg && c.use_pmg && c.aux_stream) {
+        // the pressure hierarchy's set-up on the second stream, under the
+        // velocity hierarchy's (both read the assembled operator only)
+        PMG<T>& pm = pmg_of<T>(c);
+        pmg_build<T>(c, pm);
+        FTS_CUDA(cudaEventRecord(c.ev_fork, c.stream));
+        FTS_CUDA(cudaStreamWaitEvent(c.aux_stream, c.ev_fork, 0));
+        pmg_setup_enqueue<T>(c, pm, c.aux_stream);
+        mg_setup<T>(c, mg_of<T>(c));
+        pmg_setup_finish<T>(c, pm, c.aux_stream);
+        return;
+    }
     if (c.use_mg) mg_setup<T>(c, mg_of<T>(c));
     if (c.use_pmg) pmg_setup<T>(c, pmg_of<T>(c));
 }

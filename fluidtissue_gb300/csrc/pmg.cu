@@ -315,7 +315,7 @@ k_pmg_tail(const __grid_constant__ PTailArgs<T> a, const int* __restrict__ stop)
 // Host side
 // ---------------------------------------------------------------------------
 template <typename T>
-static void pmg_build(Ctx& c, PMG<T>& pm) {
+void pmg_build(Ctx& c, PMG<T>& pm) {
     if (pm.built) return;
     init_ptables(c.device);
     const std::vector<int> chain = mg_chain(c.topo.lattice_n);
@@ -336,6 +336,9 @@ static void pmg_build(Ctx& c, PMG<T>& pm) {
     pm.cinv = dev_alloc<T>(c, (size_t)(Nc * Nc));
     pm.coef = dev_alloc<double>(c, pm.L.size() * kCoefStride);
     pm.gersh = dev_alloc<unsigned long long>(c, pm.L.size());
+    FTS_CUDA(cudaMallocHost(&pm.h_gbits, pm.L.size() * sizeof(unsigned long long)));
+    FTS_CUDA(cudaMallocHost(&pm.h_kc, (size_t)pm.L.back().N * 8 * sizeof(T)));
+    FTS_CUDA(cudaEventCreateWithFlags(&pm.ev_copied, cudaEventDisableTiming));
     pm.tail_level = (int)pm.L.size() - 1;
     for (size_t l = 0; l + 1 < pm.L.size(); ++l)
         if (pm.L[l].N <= kPTailNodes) {
@@ -397,9 +400,11 @@ static bool spd_inverse(std::vector<double>& a, int m) {
 static const int kHostOff[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1},
                                    {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
 
+// Set-up kernels on stream st (after what st waits for), ending with the
+// copies of the Gershgorin bounds and the coarsest stencil into pinned host
+// buffers; pmg_setup_finish waits for them and completes the set-up on the host.
 template <typename T>
-void pmg_setup(Ctx& c, PMG<T>& pm) {
-    pmg_build<T>(c, pm);
+void pmg_setup_enqueue(Ctx& c, PMG<T>& pm, cudaStream_t st) {
     PLevel<T>& F = pm.L[0];
     if (c.matfree) {
         const RefConstants R = ref_constants();
@@ -407,42 +412,48 @@ void pmg_setup(Ctx& c, PMG<T>& pm) {
         for (int a = 0; a < 4; ++a)
             for (int b = 0; b < 4; ++b) pr.mref[a][b] = R.mref[a][b];
         if (c.topo.kuhn_elements)
-            k_pmg_from_elements<T, true><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
+            k_pmg_from_elements<T, true><<<grid_for(c, F.N * 8), kThreads, 0, st>>>(
                 F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.par.alpha, c.par.eps, pr, F.K);
         else
-            k_pmg_from_elements<T, false><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
+            k_pmg_from_elements<T, false><<<grid_for(c, F.N * 8), kThreads, 0, st>>>(
                 F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.par.alpha, c.par.eps, pr, F.K);
     } else if (c.use_lat64) {
-        k_pmg_extract_lat<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
+        k_pmg_extract_lat<T><<<grid_for(c, F.N * 8), kThreads, 0, st>>>(
             F.n, c.lat64, c.p2t_ptr, c.p2t, c.geom, c.mu, F.K);
     } else {
-        k_pmg_extract<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
+        k_pmg_extract<T><<<grid_for(c, F.N * 8), kThreads, 0, st>>>(
             F.n, c.rowptr, c.cols, c.A64, c.p2t_ptr, c.p2t, c.geom, c.mu, F.K);
     }
     c.launches += 1;
-    FTS_CUDA(cudaMemsetAsync(pm.gersh, 0, pm.L.size() * sizeof(unsigned long long), c.stream));
+    FTS_CUDA(cudaMemsetAsync(pm.gersh, 0, pm.L.size() * sizeof(unsigned long long), st));
     for (size_t l = 0; l < pm.L.size(); ++l) {
         PLevel<T>& L = pm.L[l];
         if (l > 0) {
             const PLevel<T>& P = pm.L[l - 1];
-            k_pmg_galerkin<T><<<grid_for(c, L.N * 8), kThreads, 0, c.stream>>>(P.n, P.K, L.n,
+            k_pmg_galerkin<T><<<grid_for(c, L.N * 8), kThreads, 0, st>>>(P.n, P.K, L.n,
                                                                                 L.K);
             c.launches += 1;
         }
-        k_pmg_dinv<T><<<grid_for(c, L.N), kThreads, 0, c.stream>>>(L.n, L.K, L.Di,
+        k_pmg_dinv<T><<<grid_for(c, L.N), kThreads, 0, st>>>(L.n, L.K, L.Di,
                                                                      pm.gersh + l);
         c.launches += 1;
     }
     FTS_CUDA(cudaGetLastError());
     const PLevel<T>& Cl = pm.L.back();
+    FTS_CUDA(cudaMemcpyAsync(pm.h_gbits, pm.gersh, pm.L.size() * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, st));
+    FTS_CUDA(cudaMemcpyAsync(pm.h_kc, Cl.K, (size_t)Cl.N * 8 * sizeof(T), cudaMemcpyDeviceToHost,
+                             st));
+    FTS_CUDA(cudaEventRecord(pm.ev_copied, st));
+}
+
+template <typename T>
+void pmg_setup_finish(Ctx& c, PMG<T>& pm, cudaStream_t st) {
+    FTS_CUDA(cudaEventSynchronize(pm.ev_copied));
+    const PLevel<T>& Cl = pm.L.back();
     const int m = (int)Cl.N;
-    std::vector<unsigned long long> gbits(pm.L.size());
-    std::vector<T> kc((size_t)m * 8);
-    FTS_CUDA(cudaMemcpyAsync(gbits.data(), pm.gersh, gbits.size() * sizeof(unsigned long long),
-                             cudaMemcpyDeviceToHost, c.stream));
-    FTS_CUDA(cudaMemcpyAsync(kc.data(), Cl.K, kc.size() * sizeof(T), cudaMemcpyDeviceToHost,
-                             c.stream));
-    FTS_CUDA(cudaStreamSynchronize(c.stream));
+    const unsigned long long* gbits = pm.h_gbits;
+    const T* kc = pm.h_kc;
     std::vector<double> lam(pm.L.size());
     for (size_t l = 0; l < lam.size(); ++l) {
         double g;
@@ -479,10 +490,17 @@ void pmg_setup(Ctx& c, PMG<T>& pm) {
     }
     std::vector<T> cinv(dense.begin(), dense.end());
     FTS_CUDA(cudaMemcpyAsync(pm.coef, coef.data(), coef.size() * sizeof(double),
-                             cudaMemcpyHostToDevice, c.stream));
+                             cudaMemcpyHostToDevice, st));
     FTS_CUDA(cudaMemcpyAsync(pm.cinv, cinv.data(), cinv.size() * sizeof(T),
-                             cudaMemcpyHostToDevice, c.stream));
-    FTS_CUDA(cudaStreamSynchronize(c.stream));
+                             cudaMemcpyHostToDevice, st));
+    FTS_CUDA(cudaStreamSynchronize(st));
+}
+
+template <typename T>
+void pmg_setup(Ctx& c, PMG<T>& pm) {
+    pmg_build<T>(c, pm);
+    pmg_setup_enqueue<T>(c, pm, c.stream);
+    pmg_setup_finish<T>(c, pm, c.stream);
 }
 
 template <typename T>
@@ -540,16 +558,28 @@ void pmg_free(PMG<T>& pm) {
             if (p) cudaFree(p);
     for (void* p : {(void*)pm.coef, (void*)pm.gersh, (void*)pm.cinv})
         if (p) cudaFree(p);
+    if (pm.h_gbits) cudaFreeHost(pm.h_gbits);
+    if (pm.h_kc) cudaFreeHost(pm.h_kc);
+    if (pm.ev_copied) cudaEventDestroy(pm.ev_copied);
     pm.L.clear();
     pm.coef = nullptr;
     pm.gersh = nullptr;
     pm.cinv = nullptr;
+    pm.h_gbits = nullptr;
+    pm.h_kc = nullptr;
+    pm.ev_copied = nullptr;
     pm.tail_level = -1;
     pm.built = false;
 }
 
 template void pmg_setup<double>(Ctx&, PMG<double>&);
 template void pmg_setup<float>(Ctx&, PMG<float>&);
+template void pmg_build<double>(Ctx&, PMG<double>&);
+template void pmg_build<float>(Ctx&, PMG<float>&);
+template void pmg_setup_enqueue<double>(Ctx&, PMG<double>&, cudaStream_t);
+template void pmg_setup_enqueue<float>(Ctx&, PMG<float>&, cudaStream_t);
+template void pmg_setup_finish<double>(Ctx&, PMG<double>&, cudaStream_t);
+template void pmg_setup_finish<float>(Ctx&, PMG<float>&, cudaStream_t);
 template void pmg_vcycle<double>(Ctx&, PMG<double>&, cudaStream_t, const int*, bool);
 template void pmg_vcycle<float>(Ctx&, PMG<float>&, cudaStream_t, const int*, bool);
 template void pmg_free<double>(PMG<double>&);

@@ -57,6 +57,9 @@ struct PMG {
     std::vector<double> lam_host;
     int tail_level = -1;                 // first level run by the single-CTA tail launch
     bool built = false;
+    unsigned long long* h_gbits = nullptr;  // pinned: Gershgorin bounds per level
+    T* h_kc = nullptr;                      // pinned: coarsest half stencil
+    cudaEvent_t ev_copied = nullptr;        // both copied to the host
 };
 
 // One level as the kernels see it.
@@ -82,6 +85,15 @@ inline PView<T> pview(const PMG<T>& pm, size_t l) {
 
 template <typename T>
 void pmg_setup(Ctx& c, PMG<T>& pm);
+// The same in two halves, so that the kernels can run on another stream while
+// the caller enqueues other work: pmg_build (allocations, on c.stream), then
+// pmg_setup_enqueue on stream st, then pmg_setup_finish (waits for st).
+template <typename T>
+void pmg_build(Ctx& c, PMG<T>& pm);
+template <typename T>
+void pmg_setup_enqueue(Ctx& c, PMG<T>& pm, cudaStream_t st);
+template <typename T>
+void pmg_setup_finish(Ctx& c, PMG<T>& pm, cudaStream_t st);
 // V-cycle on pm.L[0].b on `stream`, whose first Chebyshev direction the
 // caller has written; skip_final as for the velocity V-cycle.
 template <typename T>
