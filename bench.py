@@ -561,9 +561,9 @@ def run_dist(args):
     """Distance reset (EuclideanDistance::resetPhi) on the ellipsoid129 mesh
     against its own interface points (the zero level set's edge crossings,
     LevelSet.cpp:278-300): value = resets/s of the pruned search, through the
-    C ABI with host buffers (host sort, H2D, kernel, D2H).  Beside it the
-    reference's algorithm (every node against every point) on the same GPU, and
-    the oracle's host restatement on a sample of nodes."""
+    C ABI with host buffers (H2D, device binning of the points, search, D2H).
+    Beside it the reference's algorithm (every node against every point) on the
+    same GPU, and the oracle's host restatement on all nodes."""
     import torch
     from fluidtissue_gb300 import workloads as W
     from fluidtissue_gb300.distance import EuclideanDistance, interface_points
