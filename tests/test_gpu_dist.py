@@ -73,3 +73,23 @@ def test_candidate_overflow_falls_back_exactly():
     ex, _ = _reset(inst.xyz, shell, inst.phi, "exhaustive")
     pr, _ = _reset(inst.xyz, shell, inst.phi, "pruned")
     assert np.array_equal(pr, ex), np.abs(pr - ex).max()
+
+
+def test_coincident_points_and_growing_point_sets():
+    """One context, point sets of growing size (the device buffers grow between
+    calls) and a set of coincident points (a bounding box of zero extent): every
+    call equals the reference algorithm bit for bit."""
+    from fluidtissue_gb300.distance import EuclideanDistance
+    inst = workload("sphere65", 21)
+    rng = np.random.default_rng(23)
+    sets = [np.repeat(np.array([[0.4, 0.6, 0.5]], np.float32), 100, axis=0)]
+    sets += [rng.random((m, 3)).astype(np.float32) for m in (500, 20000, 26000, 90000)]
+    d = EuclideanDistance()
+    assert d.init(inst.xyz) == 0, d.last_error()
+    for ifp in sets:
+        pr = np.ascontiguousarray(inst.phi, np.float64).copy()
+        ex = pr.copy()
+        assert d.resetPhi(ifp, pr, "pruned") == 0, d.last_error()
+        assert d.resetPhi(ifp, ex, "exhaustive") == 0, d.last_error()
+        assert np.array_equal(pr, ex), (len(ifp), np.abs(pr - ex).max())
+    d.close()
