@@ -234,57 +234,55 @@ __device__ float pruned_node(float px, float py, float pz, const float4* __restr
                              const float4* __restrict__ bhi, int32_t nb,
                              const float4* __restrict__ slo, const float4* __restrict__ shi,
                              int32_t ns, unsigned long long& mine) {
+    float best = FLT_MAX;
+    // seed: the super-block with the nearest box first
+    int32_t s0 = 0;
     {
-        float best = FLT_MAX;
-        // seed: the super-block with the nearest box first
-        int32_t s0 = 0;
-        {
-            float sb = FLT_MAX;
-            for (int32_t s = 0; s < ns; ++s) {
-                const float d = box_dist2(__ldg(slo + s), __ldg(shi + s), px, py, pz);
-                if (d < sb) {
-                    sb = d;
-                    s0 = s;
-                }
-            }
-        }
-        // pass 1: minimum squared distance (super-block s0, then the others)
-        for (int32_t t = 0; t < ns; ++t) {
-            const int32_t s = t == 0 ? s0 : (t <= s0 ? t - 1 : t);
-            if (box_dist2(__ldg(slo + s), __ldg(shi + s), px, py, pz) > best) continue;
-            const int32_t b1 = min(nb, (s + 1) * kDistSuper);
-            for (int32_t b = s * kDistSuper; b < b1; ++b) {
-                if (box_dist2(__ldg(blo + b), __ldg(bhi + b), px, py, pz) > best) continue;
-                const int32_t j1 = min(n_ifp, (b + 1) * kDistBlock);
-                for (int32_t j = b * kDistBlock; j < j1; ++j) {
-                    const float4 q = __ldg(pts + j);
-                    const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
-                    best = fminf(best, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-                }
-                mine += (unsigned long long)(j1 - b * kDistBlock);
-            }
-        }
-        // pass 2: norm3df over the candidates within the margin of the minimum
-        const float thr = best * (1.f + kDistMargin);
-        float dmin = FLT_MAX;
+        float sb = FLT_MAX;
         for (int32_t s = 0; s < ns; ++s) {
-            if (box_dist2(__ldg(slo + s), __ldg(shi + s), px, py, pz) > thr) continue;
-            const int32_t b1 = min(nb, (s + 1) * kDistSuper);
-            for (int32_t b = s * kDistSuper; b < b1; ++b) {
-                if (box_dist2(__ldg(blo + b), __ldg(bhi + b), px, py, pz) > thr) continue;
-                const int32_t j1 = min(n_ifp, (b + 1) * kDistBlock);
-                for (int32_t j = b * kDistBlock; j < j1; ++j) {
-                    const float4 q = __ldg(pts + j);
-                    const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
-                    if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= thr) {
-                        const float d = norm3df(dx, dy, dz);
-                        if (d < dmin) dmin = d;
-                    }
+            const float d = box_dist2(__ldg(slo + s), __ldg(shi + s), px, py, pz);
+            if (d < sb) {
+                sb = d;
+                s0 = s;
+            }
+        }
+    }
+    // pass 1: minimum squared distance (super-block s0, then the others)
+    for (int32_t t = 0; t < ns; ++t) {
+        const int32_t s = t == 0 ? s0 : (t <= s0 ? t - 1 : t);
+        if (box_dist2(__ldg(slo + s), __ldg(shi + s), px, py, pz) > best) continue;
+        const int32_t b1 = min(nb, (s + 1) * kDistSuper);
+        for (int32_t b = s * kDistSuper; b < b1; ++b) {
+            if (box_dist2(__ldg(blo + b), __ldg(bhi + b), px, py, pz) > best) continue;
+            const int32_t j1 = min(n_ifp, (b + 1) * kDistBlock);
+            for (int32_t j = b * kDistBlock; j < j1; ++j) {
+                const float4 q = __ldg(pts + j);
+                const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+                best = fminf(best, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+            }
+            mine += (unsigned long long)(j1 - b * kDistBlock);
+        }
+    }
+    // pass 2: norm3df over the candidates within the margin of the minimum
+    const float thr = best * (1.f + kDistMargin);
+    float dmin = FLT_MAX;
+    for (int32_t s = 0; s < ns; ++s) {
+        if (box_dist2(__ldg(slo + s), __ldg(shi + s), px, py, pz) > thr) continue;
+        const int32_t b1 = min(nb, (s + 1) * kDistSuper);
+        for (int32_t b = s * kDistSuper; b < b1; ++b) {
+            if (box_dist2(__ldg(blo + b), __ldg(bhi + b), px, py, pz) > thr) continue;
+            const int32_t j1 = min(n_ifp, (b + 1) * kDistBlock);
+            for (int32_t j = b * kDistBlock; j < j1; ++j) {
+                const float4 q = __ldg(pts + j);
+                const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+                if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= thr) {
+                    const float d = norm3df(dx, dy, dz);
+                    if (d < dmin) dmin = d;
                 }
             }
         }
-        return dmin;
     }
+    return dmin;
 }
 
 // Cooperative pruned search, one pass.  Each CTA takes kCtaNodes nodes in
