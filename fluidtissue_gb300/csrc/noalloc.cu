@@ -10,16 +10,18 @@
 // fixed size.  Every GPU that loads libfts.so holds that array until the
 // process exits.
 //
-// Set-up: the first call on a device looks up the array's device address with
-// cudaGetSymbolAddress while that device is current, and caches it; make that
-// first call before any stream capture.  All calls share the one array and it
-// keeps the previous call's contents, so the ticket counter is cleared at the
-// start of every call; two calls whose kernels overlap on the GPU race on the
-// array and give wrong norms.
+// Set-up: every call looks up the array's device address with
+// cudaGetSymbolAddress for the device that is current (a host-side lookup that
+// allocates nothing), so the address stays right after a cudaDeviceReset or a
+// context change.  The first call on a device also loads the library's module
+// into that device's context; make that first call before any stream capture.
+// All calls share the one array and it keeps the previous call's contents, so
+// the ticket counter is cleared at the start of every call; two calls whose
+// kernels overlap on the GPU (calls on different streams, not ordered by an
+// event) race on the array and give wrong norms: serialise them on one stream.
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#include <mutex>
 
 #include "fts.h"
 
@@ -33,9 +35,6 @@ static_assert(FTS_NOALLOC_MAX_NODES % kRowsPerBlock == 0, "node limit is a whole
 // Per-block partial sums (||r||^2, ||b||^2) followed by the arrival ticket.
 constexpr size_t kScratchBytes = (size_t)kMaxBlocksNA * 2 * sizeof(double) + 256;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
-
-std::mutex g_mutex;
-void* g_scratch_ptr[64] = {};
 
 // r = b - S x over one block of rows; partials -> scratch; the last block sums
 // the partials in block order (deterministic) and writes norms[0..1].
@@ -105,17 +104,13 @@ k_residual_noalloc(int64_t np, const int32_t* __restrict__ rowptr,
     }
 }
 
-// Device address of the static scratch array for the current device.
+// Device address of the static scratch array in the current device's context,
+// looked up on every call (never cached: a cudaDeviceReset or another context
+// can place the module at another address).
 int scratch_for_current_device(void** out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return FTS_ERR_CUDA;
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return FTS_ERR_CUDA;
-        g_scratch_ptr[dev] = p;
-    }
-    *out = g_scratch_ptr[dev];
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return FTS_ERR_CUDA;
+    *out = p;
     return FTS_OK;
 }
 
