@@ -178,7 +178,7 @@ OP_AUTO, OP_ASSEMBLED, OP_MATFREE, OP_STENCIL = 0, 1, 2, 3
 STATUS = {
     0: "FTS_OK", 1: "FTS_ERR_BAD_INPUT", 2: "FTS_ERR_DEGENERATE_ELEMENT",
     3: "FTS_ERR_NOT_CONVERGED", 4: "FTS_ERR_CUDA", 5: "FTS_ERR_OOM",
-    6: "FTS_ERR_UNSUPPORTED", 7: "FTS_ERR_NAN",
+    6: "FTS_ERR_UNSUPPORTED", 7: "FTS_ERR_NAN", 8: "FTS_ERR_TIMEOUT",
 }
 
 # Every symbol include/fts.h declares, with (restype, argtypes).
@@ -205,6 +205,7 @@ SIGNATURES = {
     "fts_batch_solve_device": (C.c_int, [_vp, _P(_vp), _P(_vp), _P(_vp), _P(_vp), _P(FtsStats)]),
     "fts_batch_get_config": (C.c_int, [_vp, _P(FtsBatchConfig)]),
     "fts_batch_set_stream": (C.c_int, [_vp, _vp]),
+    "fts_batch_set_barrier_limit": (C.c_int, [_vp, C.c_double, C.c_int32]),
     "fts_batch_last_error": (C.c_char_p, [_vp]),
     "fts_batch_destroy": (None, [_vp]),
     "fts_rd_create": (C.c_int, [_P(FtsMesh), C.c_int32, _P(_vp)]),
@@ -222,6 +223,7 @@ SIGNATURES = {
     "fts_ls_destroy": (None, [_vp]),
     "fts_ls_last_error": (C.c_char_p, [_vp]),
     "fts_ls_reset_values": (C.c_int, [_vp, _dp]),
+    "fts_ls_distance_reset": (C.c_int, [_vp, _dp, _dp]),
     "fts_ls_surface_tension": (C.c_int, [_vp, _dp, _dp, C.c_double, C.c_int32, _dp,
                                          _P(FtsStStats)]),
 }

@@ -1079,6 +1079,47 @@ int fts_ls_reset_values(const fts_ls* S, double* phi_reset) {
     return FTS_OK;
 }
 
+int fts_ls_distance_reset(fts_ls* S, const double* phi, double* phi_reset) {
+    if (!S || !phi || !phi_reset) return FTS_ERR_BAD_INPUT;
+    try {
+        FTS_CUDA(cudaSetDevice(S->device));
+        cudaStream_t s = S->stream;
+        const int64_t np = S->np;
+        const int g = grid_of(*S, np);
+        double* x = S->vec[0];
+        double* ifn = S->vec[11];
+        FTS_CUDA(cudaMemcpyAsync(x, phi, np * sizeof(double), cudaMemcpyHostToDevice, s));
+        const unsigned cap = (unsigned)std::min<int64_t>((S->nnz - np) / 2 + 1, 0x7fffffff);
+        if (cap > S->ifp_cap) {
+            if (S->ifp) cudaFree(S->ifp);
+            S->ifp = nullptr;
+            S->ifp = ls_alloc<float>(3 * (size_t)cap);
+            S->ifp_cap = cap;
+        }
+        FTS_CUDA(cudaMemsetAsync(S->count, 0, sizeof(unsigned), s));
+        FTS_CUDA(cudaMemsetAsync(S->keep, 0, np, s));
+        k_ls_crossings<<<g, kLsThreads, 0, s>>>(np, S->rowptr, S->cols, x, S->xyz, S->ifp,
+                                                S->count, S->keep, S->ifp_cap);
+        FTS_CUDA(cudaGetLastError());
+        unsigned nif = 0;
+        FTS_CUDA(cudaMemcpyAsync(&nif, S->count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+        FTS_CUDA(cudaStreamSynchronize(s));
+        nif = std::min(nif, S->ifp_cap);
+        FTS_CUDA(cudaMemcpyAsync(ifn, x, np * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        dist_reset_device(S->dist, S->ifp, true, (int32_t)nif, ifn, FTS_DIST_PRUNED, s, nullptr);
+        FTS_CUDA(cudaMemcpyAsync(phi_reset, ifn, np * sizeof(double), cudaMemcpyDeviceToHost, s));
+        FTS_CUDA(cudaStreamSynchronize(s));
+        S->have_reset = true;
+    } catch (const CudaError& e) {
+        S->last_error = e.what;
+        return e.code == cudaErrorMemoryAllocation ? FTS_ERR_OOM : FTS_ERR_CUDA;
+    } catch (const std::bad_alloc&) {
+        S->last_error = "host allocation failed";
+        return FTS_ERR_OOM;
+    }
+    return FTS_OK;
+}
+
 int fts_ls_surface_tension(fts_ls* S, const double* phi, const double* phi_reset,
                            double surface_tension, int32_t node_density, double* force,
                            fts_st_stats* stats) {

@@ -71,6 +71,20 @@ class LevelSet:
             raise FtsError(rc, self.last_error())
         return out
 
+    def distance_reset(self, phi: np.ndarray) -> np.ndarray:
+        """LevelSet::resetPhi_'s full reset values (phi_ifn_, LevelSet.cpp:440)
+        of phi: signed distances to its zero level set's edge crossings.  They
+        also become this context's reset values."""
+        if not self._ctx:
+            raise FtsError(1, "LevelSet.init() has not succeeded")
+        phi = np.ascontiguousarray(phi, np.float64)
+        out = np.empty(phi.shape[0])
+        rc = self._lib.fts_ls_distance_reset(self._ctx, N.ptr(phi, C.c_double),
+                                             N.ptr(out, C.c_double))
+        if rc != 0:
+            raise FtsError(rc, self.last_error())
+        return out
+
     def surface_tension(self, phi: np.ndarray, par: dict,
                         phi_reset: np.ndarray | None = None) -> np.ndarray:
         """Flow::surfaceTension_ (Flow.cpp:307-341) with the LevelSet's

@@ -38,7 +38,9 @@ typedef enum fts_status {
     FTS_ERR_OOM = 5,                /* device allocation failed */
     FTS_ERR_UNSUPPORTED = 6,        /* a reference option outside this path (P2; surface tension
                                        without its load) */
-    FTS_ERR_NAN = 7                 /* NaN or Inf in the inputs or in the iteration */
+    FTS_ERR_NAN = 7,                /* NaN or Inf in the inputs or in the iteration */
+    FTS_ERR_TIMEOUT = 8             /* a grid-barrier wait of a persistent launch ran out (a
+                                       block did not arrive); the launch returned */
 } fts_status;
 
 /* Arithmetic of the solve. */
@@ -252,6 +254,14 @@ int fts_batch_solve_device(fts_batch* b, const double* const* phi, const double*
                            const double* const* mu, double* const* flow, fts_stats* stats);
 int fts_batch_get_config(const fts_batch* b, fts_batch_config* cfg);
 int fts_batch_set_stream(fts_batch* b, void* stream);
+/* No counterpart in the reference (its solves are host code).  The longest
+ * wait of any block at a grid barrier of the persistent launch (default 2 s);
+ * when it runs out the launch records the error, every block returns and
+ * fts_batch_solve reports FTS_ERR_TIMEOUT with the context still usable.
+ * absent_block >= 0 is for failure-detection tests: that block of every later
+ * persistent launch leaves at its first barrier without arriving, so the
+ * others' waits run out (-1: none). */
+int fts_batch_set_barrier_limit(fts_batch* b, double seconds, int32_t absent_block);
 const char* fts_batch_last_error(const fts_batch* b);
 void fts_batch_destroy(fts_batch* b);
 
@@ -273,9 +283,12 @@ void fts_batch_destroy(fts_batch* b);
  * holds it until exit).  np must be <= FTS_NOALLOC_MAX_NODES, else
  * FTS_ERR_BAD_INPUT.  Runs on `stream` (a cudaStream_t; NULL = the legacy
  * default stream) of the current device and returns without waiting for it.
- * The first call on a device looks up the scratch array's device address and
- * should come before any stream capture.  Calls share the array: calls whose
- * kernels overlap on the GPU race and their norms are wrong. */
+ * Every call looks up the scratch array's device address in the current
+ * context (nothing is cached, so the address stays right after a
+ * cudaDeviceReset); the first call on a device also loads the library's module
+ * there and should come before any stream capture.  Calls share the array:
+ * calls whose kernels overlap on the GPU (different streams, not ordered)
+ * race and their norms are wrong, so serialise them on one stream. */
 int fts_bsr_residual_noalloc(int64_t np, const int32_t* rowptr, const int32_t* cols,
                              const double* vals, const double* x, const double* b, double* r,
                              double* norms, void* stream);
@@ -413,6 +426,16 @@ const char* fts_ls_last_error(const fts_ls* ls);
  * LevelSet.cpp:440, before the 0.75 / 0.25 mixing), host [np].
  * FTS_ERR_BAD_INPUT before any update with reset = 1. */
 int fts_ls_reset_values(const fts_ls* ls, double* phi_reset);
+
+/* The full distance reset of phi (LevelSet::resetPhi_, LevelSet.cpp:429-441:
+ * phi_ifn_ before the crossing nodes keep their values): every node's signed
+ * distance to the edge crossings of phi's zero level set (LevelSet.cpp:278-300),
+ * sign from phi.  phi[np] in, phi_reset[np] out (host); the values also become
+ * this context's reset values (fts_ls_surface_tension with phi_reset = NULL).
+ * After LevelSet::update the crossing edges and their end values are those
+ * the update's reset used, so this reproduces the level set's phi_ifn_ from
+ * its phi alone. */
+int fts_ls_distance_reset(fts_ls* ls, const double* phi, double* phi_reset);
 
 /* ---------------------------------------------------------------------------
  * Surface tension: Flow::surfaceTension_ (src/growth/Flow.cpp:307-341) with the

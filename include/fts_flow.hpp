@@ -12,6 +12,15 @@
 // the GPU from the growth factor with the reference's profile
 // (ViscosityProfiles.hpp:27-72), exactly as Flow does.
 //
+// "Surface tension" > 0 (Flow.cpp:359-363): Flow::fillF_ adds the interfacial
+// load of Flow::surfaceTension_ (Flow.cpp:307-341), built from the LevelSet's
+// normals, curvature and interface patches.  Those are functions of the level
+// set's full distance reset phi_ifn_, which LevelSet keeps private; after
+// LevelSet::update the crossing edges of getPhi() and their end values are the
+// ones that reset used, so FlowGPU recomputes phi_ifn_ from getPhi() on the GPU
+// (fts_ls_distance_reset), then the load (fts_ls_surface_tension, with
+// "Node density" as rho), and passes it to fts_solve as `force`.
+//
 // The template parameters let the header compile inside the reference's build
 // (Eigen types, Mesh3D) without this header including any of them.
 #pragma once
@@ -31,7 +40,10 @@ public:
     FlowGPU() = default;
     FlowGPU(const FlowGPU&) = delete;
     FlowGPU& operator=(const FlowGPU&) = delete;
-    ~FlowGPU() { fts_destroy(ctx_); }
+    ~FlowGPU() {
+        fts_destroy(ctx_);
+        fts_ls_destroy(ls_);
+    }
 
     // GB300 options not present in the reference's parameter file.
     void setPrecision(int precision) { precision_ = precision; }
@@ -59,6 +71,8 @@ public:
         p.gf_production = p.rd_iterations > 0.0 ? (double)par["GF production"] : 1.0;
         p.advection_dt = par["Advection dt"];
         p.surface_tension = par["Surface tension"];
+        st_ = (float)p.surface_tension;          // Flow.cpp:359
+        rho_ = (int)par["Node density"];         // Flow.cpp:361
         p.precision = precision_;
         p.preconditioner = preconditioner_;
         p.device = device_;
@@ -84,6 +98,16 @@ public:
                          fts_last_error(nullptr));
             return -1;
         }
+        fts_ls_destroy(ls_);
+        ls_ = nullptr;
+        if (st_ > 0.0f) {  // the level-set context that builds the interfacial load
+            rc = fts_ls_create(&m, device_, &ls_);
+            if (rc != FTS_OK) {
+                std::fprintf(stderr, "FlowGPU::init(): %s: %s\n", fts_status_string(rc),
+                             fts_ls_last_error(nullptr));
+                return -1;
+            }
+        }
         return 0;
     }
 
@@ -98,7 +122,22 @@ public:
             src_[i] = (double)source(i);
         }
         for (int64_t i = 0; i < 4 * np_; ++i) out_[i] = (double)flow(i);
-        int rc = fts_solve(ctx_, phi_.data(), src_.data(), nullptr, nullptr, out_.data(), &stats_);
+        const double* force = nullptr;
+        if (st_ > 0.0f) {  // Flow.cpp:359-363
+            reset_.resize((size_t)np_);
+            force_.resize((size_t)(3 * np_));
+            int rs = ls_ ? fts_ls_distance_reset(ls_, phi_.data(), reset_.data()) : FTS_ERR_BAD_INPUT;
+            if (rs == FTS_OK)
+                rs = fts_ls_surface_tension(ls_, phi_.data(), reset_.data(), (double)st_, rho_,
+                                            force_.data(), nullptr);
+            if (rs != FTS_OK) {
+                std::fprintf(stderr, "FlowGPU::solve(): surface tension: %s: %s\n",
+                             fts_status_string(rs), fts_ls_last_error(ls_));
+                return -1;
+            }
+            force = force_.data();
+        }
+        int rc = fts_solve(ctx_, phi_.data(), src_.data(), nullptr, force, out_.data(), &stats_);
         if (rc != FTS_OK) {
             std::fprintf(stderr, "FlowGPU::solve(): %s: %s\n", fts_status_string(rc),
                          fts_last_error(ctx_));
@@ -110,9 +149,16 @@ public:
     }
 
     const fts_stats& stats() const { return stats_; }
+    // The interfacial load of the last solve, [fx(np), fy(np), fz(np)] (empty
+    // when "Surface tension" is 0).
+    const std::vector<double>& surfaceTensionLoad() const { return force_; }
 
 private:
     fts_ctx* ctx_ = nullptr;
+    fts_ls* ls_ = nullptr;
+    float st_ = 0.0f;
+    int rho_ = 0;
+    std::vector<double> reset_, force_;
     int64_t np_ = 0, nt_ = 0;
     int precision_ = FTS_PREC_FP64;
     int preconditioner_ = FTS_PC_AUTO;
