@@ -214,8 +214,9 @@ static void configure_preconditioner(Ctx& c) {
     }
     c.use_lat = !c.matfree && !c.in_batch && n > 0 &&
                 (c.par.operator_kind == FTS_OP_AUTO || c.par.operator_kind == FTS_OP_STENCIL);
-    c.use_lat64 = c.use_lat && c.par.precision == FTS_PREC_MIXED &&
-                  c.par.solver == FTS_SOLVER_MINRES;
+    // both precisions: the FP64 solve runs its operator on the FP64 half
+    // stencil (1 KB/node) as the mixed solve's outer residual does
+    c.use_lat64 = c.use_lat && c.par.solver == FTS_SOLVER_MINRES;
     if (c.matfree && (!c.use_mg || c.par.precision != FTS_PREC_MIXED)) {
         c.last_error = "the matrix-free operator runs in mixed precision with the multigrid "
                        "preconditioner (Kuhn lattice, odd n >= 9)";
@@ -395,13 +396,17 @@ static int solve_device(Ctx& c, bool have_mu, bool have_force, double* flow_out,
             launch_to_f32(c);
         }
     } else if (c.use_lat64) {
-        // Kuhn lattice, mixed precision: FP64 and FP32 half stencils straight
-        // from the elements (no BSR)
-        ensure_fp32(c);
+        // Kuhn lattice: the FP64 half stencil (and for mixed precision the
+        // FP32 one) straight from the elements (no BSR)
+        if (P.precision == FTS_PREC_MIXED) ensure_fp32(c);
         launch_assemble_lat(c);
         launch_preconditioner(c);
-        launch_to_f32(c);
-        setup_preconditioner<float>(c);
+        if (P.precision == FTS_PREC_MIXED) {
+            launch_to_f32(c);
+            setup_preconditioner<float>(c);
+        } else {
+            setup_preconditioner<double>(c);
+        }
     } else {
         launch_assemble(c);
         launch_preconditioner(c);
@@ -580,6 +585,7 @@ const char* fts_status_string(int s) {
         case FTS_ERR_OOM: return "out of device memory";
         case FTS_ERR_UNSUPPORTED: return "unsupported option";
         case FTS_ERR_NAN: return "non-finite value";
+        case FTS_ERR_TIMEOUT: return "grid barrier wait ran out";
         default: return "unknown status";
     }
 }
@@ -712,6 +718,8 @@ static int solve_common(fts_ctx* ctx, const double* phi, const double* source, c
         st.spmv_bytes = nb * (16.0 * V + 4.0) + 4.0 * (n + 1.0) + 3.0 * 4.0 * n * V;
         if (c.use_lat && c.par.precision == FTS_PREC_MIXED)  // 8 blocks per node; x, r1, q
             st.spmv_bytes = n * (8.0 * 16.0 * 4.0) + 3.0 * 4.0 * n * 4.0;
+        if (c.use_lat64 && c.par.precision == FTS_PREC_FP64)  // the same in FP64
+            st.spmv_bytes = n * (8.0 * 16.0 * 8.0) + 3.0 * 4.0 * n * 8.0;
         if (c.matfree)  // tets + node->element map + 64 B record per element; map offsets,
                         // flags, x, r1, q per node
             st.spmv_bytes = (double)c.nt * (16.0 + 16.0 + 64.0) + n * (4.0 + 1.0 + 3.0 * 16.0);

@@ -459,18 +459,21 @@ k_assemble_lat(int n, const int32_t* __restrict__ p2t_ptr, const uint32_t* __res
         for (int r = 0; r < 4; ++r) {
             L64[lat64_idx(d, r, 0, v)] = make_double2(blk[4 * r], blk[4 * r + 1]);
             L64[lat64_idx(d, r, 1, v)] = make_double2(blk[4 * r + 2], blk[4 * r + 3]);
-            L32[((v >> 5) * 32 + d * 4 + r) * 32 + (v & 31)] =
-                make_float4((float)blk[4 * r], (float)blk[4 * r + 1], (float)blk[4 * r + 2],
-                            (float)blk[4 * r + 3]);
+            if (L32)  // NULL: the FP64 solve keeps no FP32 copy
+                L32[((v >> 5) * 32 + d * 4 + r) * 32 + (v & 31)] =
+                    make_float4((float)blk[4 * r], (float)blk[4 * r + 1], (float)blk[4 * r + 2],
+                                (float)blk[4 * r + 3]);
         }
     }
 }
 
 void launch_assemble_lat(Ctx& c) {
     const int n = c.topo.lattice_n;
-    if (n <= 0 || !c.lat_val)
+    const bool mixed = c.par.precision == FTS_PREC_MIXED;
+    if (n <= 0 || (mixed && !c.lat_val))
         throw CudaError(cudaErrorInvalidValue, "lattice assembly without a lattice operator",
                         __FILE__, __LINE__);
+    float4* L32 = mixed ? reinterpret_cast<float4*>(c.lat_val) : nullptr;
     const int64_t tiles = (c.np + 31) / 32;
     if (!c.lat64) {
         c.lat64 = dev_alloc<double2>(c, (size_t)tiles * 64 * 32);
@@ -481,11 +484,11 @@ void launch_assemble_lat(Ctx& c) {
     if (c.topo.kuhn_elements)
         k_assemble_lat<true><<<grid_for(c, c.np * 8), kThreads, 0, c.stream>>>(
             n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.bnd, c.par.alpha, c.par.eps, ref_args(),
-            c.lat64, reinterpret_cast<float4*>(c.lat_val));
+            c.lat64, L32);
     else
         k_assemble_lat<false><<<grid_for(c, c.np * 8), kThreads, 0, c.stream>>>(
             n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.bnd, c.par.alpha, c.par.eps, ref_args(),
-            c.lat64, reinterpret_cast<float4*>(c.lat_val));
+            c.lat64, L32);
     FTS_CUDA(cudaGetLastError());
     c.launches += 1;
     c.a64_valid = false;

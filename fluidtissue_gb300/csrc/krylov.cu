@@ -494,6 +494,68 @@ k_minres_A_lat(int n, int64_t np, const float4* __restrict__ L, const V4<float>*
     }
 }
 
+// Kernel A in FP64 on the FP64 lattice half stencil (lat64_idx), thread per
+// node: the same half-stencil walk as the outer residual.
+__global__ void __launch_bounds__(kThreads)
+k_minres_A_lat64(int n, int64_t np, const double2* __restrict__ L,
+                 const V4<double>* __restrict__ Y, int ybuf, const V4<double>* __restrict__ R1,
+                 V4<double>* __restrict__ q, Reduction red, MinresScalars* s) {
+    pdl_wait();
+    if (s->stop) return;
+    const double tinv = 1.0 / s->beta;
+    const double wadd = s->ycorr[ybuf];
+    double acc[2] = {0.0, 0.0};
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < np;
+         v += (int64_t)gridDim.x * blockDim.x) {
+        const int vi = (int)v;
+        const int k = vi / (n * n), j = (vi / n) % n, i = vi % n;
+        double a[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {  // own blocks: row r . y_w
+            const int w = nbr(i, j, k, d, n);
+            if (w < 0) continue;
+            const V4<double> yw = Y[w];
+            const double y3 = yw.w + wadd;
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) {
+                const double2 u = L[lat64_idx(d, rr, 0, v)], s2 = L[lat64_idx(d, rr, 1, v)];
+                a[rr] = fma(u.x, yw.x, fma(u.y, yw.y, fma(s2.x, yw.z, fma(s2.y, y3, a[rr]))));
+            }
+        }
+#pragma unroll
+        for (int d = 1; d < 8; ++d) {  // the neighbour's block towards v, transposed
+            const int w = nbr(i, j, k, d + 7, n);
+            if (w < 0) continue;
+            const V4<double> yw = Y[w];
+            const double yr[4] = {yw.x, yw.y, yw.z, yw.w + wadd};
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) {
+                const double2 u = L[lat64_idx(d, rr, 0, w)], s2 = L[lat64_idx(d, rr, 1, w)];
+                a[0] = fma(u.x, yr[rr], a[0]);
+                a[1] = fma(u.y, yr[rr], a[1]);
+                a[2] = fma(s2.x, yr[rr], a[2]);
+                a[3] = fma(s2.y, yr[rr], a[3]);
+            }
+        }
+        V4<double> qv;
+        qv.x = a[0] * tinv;
+        qv.y = a[1] * tinv;
+        qv.z = a[2] * tinv;
+        qv.w = a[3] * tinv;
+        q[v] = qv;
+        const V4<double> yv = Y[v], r1 = R1[v];
+        const double e0 = yv.x * tinv, e1 = yv.y * tinv, e2 = yv.z * tinv,
+                     e3 = (yv.w + wadd) * tinv;
+        acc[0] += e0 * qv.x + e1 * qv.y + e2 * qv.z + e3 * qv.w;
+        acc[1] += e0 * r1.x + e1 * r1.y + e2 * r1.z + e3 * r1.w;
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
+        const double c1 = s->iters >= 1 ? s->beta / s->oldb : 0.0;
+        s->alfa = tot[0] - c1 * tot[1];
+    }
+}
+
 // Preconditioner stage 1.
 //   init: n = r0 (written to Rn)      else: n = q - c1 R1 - c2 R2 (written to Rn = R1)
 //   y.w = ip * n.w;  Jacobi: y.xyz = D3^-1 n.xyz;  multigrid: b0 = n.xyz (SoA)
@@ -564,7 +626,10 @@ k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
 
 // Multigrid stage 2, fused with the V-cycle's last post-smoothing step on the
 // finest level: y.xyz = the step's new x (not stored in the level), and with
-// pmg y.w likewise from the pressure V-cycle; beta.
+// pmg y.w likewise from the pressure V-cycle; beta.  (Running the pressure
+// V-cycle's last step on its own stream instead, and reading its x here, made
+// the solve slower: 224.7 -> 226.2 ms on ellipsoid129, the pressure stream
+// then ends after the velocity one.)
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, PView<T> P0,
@@ -745,6 +810,12 @@ long long minres_inner(Ctx& c, double rtol, long long maxit, double* achieved, i
                     c.topo.lattice_n, np, reinterpret_cast<const float4*>(c.lat_val),
                     reinterpret_cast<const V4<float>*>(w.Y[yk]),
                     yk, reinterpret_cast<const V4<float>*>(R1), reinterpret_cast<V4<float>*>(w.q),
+                    c.red, c.ms);
+            else if (sizeof(T) == 8 && c.use_lat64)
+                pdl_launch(k_minres_A_lat64, gn, kThreads, c.stream,
+                    c.topo.lattice_n, np, c.lat64,
+                    reinterpret_cast<const V4<double>*>(w.Y[yk]), yk,
+                    reinterpret_cast<const V4<double>*>(R1), reinterpret_cast<V4<double>*>(w.q),
                     c.red, c.ms);
             else if (sizeof(T) == 4 && c.use_ell)
                 pdl_launch(k_minres_A_ell, grid_for(c, c.nslices * 32), kThreads, c.stream,
