@@ -14,9 +14,10 @@
 // and replayed.  An autotuner picks the block size, the chunk length and the
 // number of threads per block row (the work split of the SpMV).
 //
-// Grid barrier (grid_sync.cuh): the spin has an iteration limit after which the
-// kernel records an error and leaves its loop (no unbounded wait).  With the
-// cooperative launch all blocks are co-resident.
+// Grid barrier (grid_sync.cuh): every wait has a time limit (a runtime field,
+// fts_batch_set_barrier_limit, 2 s by default) after which the kernel records
+// an error and returns (no unbounded wait); the solve then reports
+// FTS_ERR_TIMEOUT.  With the cooperative launch all blocks are co-resident.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -814,7 +815,7 @@ template <typename T>
 static void launch_persistent(fts_batch& B, long long sweeps) {
     BInst<T>* inst = sizeof(T) == 8 ? reinterpret_cast<BInst<T>*>(B.d_inst64)
                                     : reinterpret_cast<BInst<T>*>(B.d_inst32);
-    FTS_CUDA(cudaMemsetAsync(B.d_bar, 0, sizeof(BarrierState), B.stream));
+    FTS_CUDA(cudaMemsetAsync(B.d_bar, 0, kBarrierResetBytes, B.stream));
     const int threads = B.cfg.threads;
     const int nch = B.nch0;
     const BSched S{B.d_sched, B.max_depth, B.d_sched + B.cptr.size(), (int)B.coarse.size()};
@@ -974,6 +975,10 @@ static void batch_build(fts_batch& B) {
     FTS_CUDA(cudaMalloc(&B.d_inst32, B.count * sizeof(BInst<float>)));
     FTS_CUDA(cudaMalloc(&B.d_out, B.count * sizeof(BOuter)));
     FTS_CUDA(cudaMalloc(&B.d_bar, sizeof(BarrierState)));
+    {
+        const BarrierState cfg = barrier_config(kDefaultBarrierLimitNs, -1);
+        FTS_CUDA(cudaMemcpy(B.d_bar, &cfg, sizeof(cfg), cudaMemcpyHostToDevice));
+    }
     batch_chunks(B, B.cfg.chunk_rows);
 }
 
@@ -1136,6 +1141,9 @@ static int batch_solve_common(fts_batch* B, const double* const* phi, const doub
         FTS_CUDA(cudaEventRecord(B->ev[0], B->stream));
         batch_assemble(*B, have_mu);
         batch_levels(*B);
+        // a barrier failure of any launch of this solve stays recorded
+        FTS_CUDA(cudaMemsetAsync(reinterpret_cast<char*>(B->d_bar) + kBarrierErrorOffset, 0,
+                                 sizeof(int), B->stream));
         if (!B->tuned) batch_tune(*B);
         batch_reset_outer(*B);
         const int passes = B->precision == FTS_PREC_MIXED ? 4 : 2;
@@ -1188,7 +1196,7 @@ static int batch_solve_common(fts_batch* B, const double* const* phi, const doub
         FTS_CUDA(cudaStreamSynchronize(B->stream));
         if (bs.error) {
             B->last_error = "batched grid barrier timed out";
-            rc = FTS_ERR_CUDA;
+            rc = FTS_ERR_TIMEOUT;
         }
         float ms = 0.f;
         FTS_CUDA(cudaEventElapsedTime(&ms, B->ev[0], B->ev[1]));
@@ -1224,7 +1232,9 @@ static int batch_solve_common(fts_batch* B, const double* const* phi, const doub
         FTS_CUDA(cudaStreamSynchronize(B->stream));
     } catch (const CudaError& e) {
         B->last_error = e.what;
-        rc = e.code == cudaErrorMemoryAllocation ? FTS_ERR_OOM : FTS_ERR_CUDA;
+        rc = e.code == cudaErrorMemoryAllocation ? FTS_ERR_OOM
+             : e.code == cudaErrorLaunchTimeout  ? FTS_ERR_TIMEOUT
+                                                 : FTS_ERR_CUDA;
     } catch (int code) {
         rc = code;
     }
@@ -1247,6 +1257,24 @@ int fts_batch_get_config(const fts_batch* B, fts_batch_config* cfg) {
     if (!B || !cfg) return FTS_ERR_BAD_INPUT;
     *cfg = B->cfg;
     cfg->graph = B->graph ? 1 : 0;
+    return FTS_OK;
+}
+
+int fts_batch_set_barrier_limit(fts_batch* B, double seconds, int32_t absent_block) {
+    if (!B || !(seconds > 0.0) || seconds > 3600.0 || absent_block < -1)
+        return FTS_ERR_BAD_INPUT;
+    try {
+        FTS_CUDA(cudaSetDevice(B->device));
+        const BarrierState cfg =
+            barrier_config((unsigned long long)(seconds * 1e9), (int)absent_block);
+        // the whole state: no launch is in flight once the stream has drained
+        FTS_CUDA(cudaStreamSynchronize(B->stream));
+        FTS_CUDA(cudaMemcpyAsync(B->d_bar, &cfg, sizeof(cfg), cudaMemcpyHostToDevice, B->stream));
+        FTS_CUDA(cudaStreamSynchronize(B->stream));
+    } catch (const CudaError& e) {
+        B->last_error = e.what;
+        return FTS_ERR_CUDA;
+    }
     return FTS_OK;
 }
 

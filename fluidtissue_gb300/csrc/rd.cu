@@ -301,6 +301,10 @@ int fts_rd_create(const fts_mesh* mesh, int32_t device, fts_rd** out) {
         R->bad = rd_alloc<int>(*R, 1);
         R->nel = rd_alloc<unsigned long long>(*R, 1);
         R->bar = rd_alloc<BarrierState>(*R, 1);
+        {
+            const BarrierState cfg = barrier_config(kDefaultBarrierLimitNs, -1);
+            FTS_CUDA(cudaMemcpy(R->bar, &cfg, sizeof(cfg), cudaMemcpyHostToDevice));
+        }
         FTS_CUDA(cudaMemcpy(R->xyz, mesh->xyz, 3 * R->np * sizeof(float), cudaMemcpyHostToDevice));
         FTS_CUDA(cudaMemcpy(R->tets, mesh->tets, 4 * R->nt * sizeof(int32_t),
                             cudaMemcpyHostToDevice));
@@ -390,7 +394,9 @@ int fts_rd_solve(fts_rd* R, const fts_rd_params* P, const double* phi,
         FTS_CUDA(cudaMemsetAsync(R->bad, 0, sizeof(int), s));
         FTS_CUDA(cudaMemsetAsync(R->nel, 0, sizeof(unsigned long long), s));
         FTS_CUDA(cudaMemsetAsync(R->srcflag, 0, np, s));
-        FTS_CUDA(cudaMemsetAsync(R->bar, 0, sizeof(BarrierState), s));
+        FTS_CUDA(cudaMemsetAsync(R->bar, 0, kBarrierResetBytes, s));
+        FTS_CUDA(cudaMemsetAsync(reinterpret_cast<char*>(R->bar) + kBarrierErrorOffset, 0,
+                                 sizeof(int), s));
         static const RdConst K = rd_const();
         if (nint > 0) {
             k_rd_laplacian<<<grid_of(*R, nint), 256, 0, s>>>(nint, R->list, R->rowptr, R->cols,
@@ -462,7 +468,7 @@ int fts_rd_solve(fts_rd* R, const fts_rd_params* P, const double* phi,
         FTS_CUDA(cudaStreamSynchronize(s));
         if (bs.error) {
             R->last_error = "grid barrier timed out in the Euler steps";
-            rc = FTS_ERR_CUDA;
+            rc = FTS_ERR_TIMEOUT;
         }
         float ms = 0.f;
         FTS_CUDA(cudaEventElapsedTime(&ms, R->ev[0], R->ev[1]));

@@ -272,6 +272,12 @@ class Batch:
     def set_stream(self, stream_handle: int | None) -> int:
         return self._lib.fts_batch_set_stream(self._ctx, stream_handle or None)
 
+    def set_barrier_limit(self, seconds: float, absent_block: int = -1) -> int:
+        """Longest wait at a grid barrier of the persistent launch; a block
+        index >= 0 makes that block leave at its first barrier without
+        arriving (failure-detection tests)."""
+        return self._lib.fts_batch_set_barrier_limit(self._ctx, float(seconds), int(absent_block))
+
     def last_error(self) -> str:
         return self._lib.fts_batch_last_error(self._ctx).decode()
 
