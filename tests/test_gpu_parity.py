@@ -137,25 +137,6 @@ def test_profile_viscosity_matches_oracle():
         f.close()
 
 
-def test_sphere65_fp64_parity():
-    """65^3, jitter +-0.1h, mu = 1: GPU FP64 vs the oracle's own tight solve
-    (the oracle MINRES starts from the GPU solution and must converge to the
-    true solution independently; the difference is the GPU's error)."""
-    import oracle as O
-    inst = workload("sphere65")
-    par = dict(inst.params)
-    f, rc, flow = _solve(inst, par=par, precision="fp64")
-    assert rc == 0, f.last_error()
-    R, _, _, mu = O.system(inst.xyz, inst.tets, inst.boundary, inst.phi, inst.source, inst.mu,
-                           par)
-    x0 = flow[R.sidx]
-    x, tr, _ = O.solve_tight(R, inst.xyz, inst.tets, mu, x0=x0, tol=1e-13)
-    assert tr <= 1e-12
-    ev, ep = _errors(flow, O.scatter(R, x), inst.np)
-    assert ev <= VEL_TOL_FP64 and ep <= P_TOL_FP64, (ev, ep, f.last_stats)
-    f.close()
-
-
 @pytest.mark.parametrize("n", [16, 10])
 def test_even_n_multigrid_parity(n):
     """Even lattice sizes coarsen to n/2 + 1 (the last coarse layer on the
