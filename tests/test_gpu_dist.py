@@ -93,3 +93,29 @@ def test_coincident_points_and_growing_point_sets():
         assert d.resetPhi(ifp, ex, "exhaustive") == 0, d.last_error()
         assert np.array_equal(pr, ex), (len(ifp), np.abs(pr - ex).max())
     d.close()
+
+
+@pytest.mark.parametrize("name,n", [("ellipsoid129", 33), ("sphere65", 21)])
+def test_pruned_equals_reference_kernel(name, n):
+    """The reference's own kernel (distanceToInterface_k, compiled unchanged
+    from src/fem/EuclideanDistance.cu into oracle/_ref and launched as
+    EuclideanDistance::resetPhi launches it) against fts_dist_reset's pruned
+    search: bit for bit on every point set, including a far shell whose
+    blocks overflow the shared candidate list and an empty point set."""
+    import ref_dist
+    if not ref_dist.available():
+        pytest.skip("oracle/_ref/EuclideanDistance.cubin was not built (reference sources "
+                    "absent where the repository was built)")
+    inst = workload(name, n)
+    sets = _point_sets(inst)
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal((70000, 3))
+    sets["far_shell"] = (0.5 + 50.0 * v / np.linalg.norm(v, axis=1, keepdims=True)).astype(
+        np.float32)
+    sets["empty"] = np.zeros((0, 3), np.float32)
+    K = ref_dist.ReferenceDistanceKernel()
+    for label, ifp in sets.items():
+        pr, _ = _reset(inst.xyz, ifp, inst.phi, "pruned")
+        ref = K.reset_phi(inst.xyz, ifp, inst.phi)
+        assert np.array_equal(pr, ref), (label, np.abs(pr - ref).max())
+    K.close()
