@@ -57,3 +57,33 @@ def test_replica_ids_cover_everything():
         seen = sorted(i for r in range(world) for i in bench.replica_ids(96, r, world))
         assert seen == list(range(96))
     pytest.importorskip("torch")
+
+
+def test_bench_gpus_flag_spawns_ranks():
+    """`bench.py --gpus 2` without a launcher starts two local ranks itself:
+    the reference arm (CPU) prints one line from rank 0 with n_gpus 2, and
+    the other rank exits 0 without work."""
+    import json
+    import subprocess
+    import sys
+    env = {k: v for k, v in os.environ.items()
+           if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT")}
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--gpus", "2", "--impl",
+                        "reference", "--workload", "sphere17", "--steps", "1", "--warmup", "3"],
+                       capture_output=True, text=True, env=env, timeout=600, cwd=str(ROOT))
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    line = lines[0]
+    assert line["impl"] == "reference" and line["n_gpus"] == 2
+    assert line["cpu_baseline"]["measured_fraction"] == 1.0 and line["value"] > 0
+
+
+def test_bench_rejects_a_mismatched_launcher():
+    import subprocess
+    import sys
+    env = dict(os.environ, WORLD_SIZE="1", RANK="0", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--gpus", "2", "--impl",
+                        "reference", "--workload", "sphere17"], capture_output=True, text=True,
+                       env=env, timeout=300, cwd=str(ROOT))
+    assert r.returncode != 0 and "does not match WORLD_SIZE" in r.stderr
