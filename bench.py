@@ -618,6 +618,9 @@ def run_reference(args):
     if rank != 0:
         return
     from fluidtissue_gb300 import workloads as W
+    if args.workload == "dist129":
+        run_reference_dist(args, ws)
+        return
     O = _oracle()
     inst = W.WORKLOADS[args.workload]()
     threads = O.num_threads()
@@ -654,6 +657,33 @@ def run_reference(args):
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     out.update(extra)
     print(json.dumps(out), flush=True)
+
+
+def run_reference_dist(args, ws):
+    """Reference arm of the distance workload: the reference's own CUDA kernel
+    (oracle/_ref) through resetPhi's host sequence, on the ellipsoid129 mesh and
+    its interface points."""
+    from fluidtissue_gb300 import workloads as W
+    from fluidtissue_gb300.distance import interface_points
+    inst = W.ellipsoid129()
+    ifp, _ = interface_points(inst.xyz, inst.tets, inst.phi)
+    r = reference_distance_kernel(inst, ifp, args.steps, args.warmup)
+    if r is None:
+        print(json.dumps({"impl": "reference", "unavailable": "oracle/_ref/EuclideanDistance."
+                          "cubin was not built (reference sources absent where the repository "
+                          "was built)"}), flush=True)
+        return
+    r.pop("phi")
+    v = r["resets_per_s"]
+    print(json.dumps({"impl": "reference", "metric": "level-set distance resets/s (ellipsoid129 "
+                      "nodes x its interface points)", "value": v, "unit": "resets/s",
+                      "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": r["ms_per_reset"], "higher_is_better": True,
+                      "config": {"workload": f"dist129: {inst.np} nodes x {len(ifp)} interface "
+                                             f"points"},
+                      "reference_kernel": r,
+                      "e2e": {"value": v, "unit": "resets/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
 
 
 # Fig. 5-6 growth parameters of the reference's parameter summary
@@ -798,6 +828,7 @@ def run_dist(args):
                        "points_scanned": int(res[-1][0]["points_scanned"]),
                        "clocks": clk.stop() if clk else None}
         out[method]["phi"] = res[-1][1]
+    pr_phi = out["pruned"]["phi"]
     same = bool(np.array_equal(out["pruned"].pop("phi"), out["exhaustive"].pop("phi")))
     pr = out["pruned"]
     line = {"metric": "level-set distance resets/s (ellipsoid129 nodes x its interface points)",
@@ -813,6 +844,13 @@ def run_dist(args):
             "pruned_equals_reference_algorithm": same,
             "kernel_speedup": round(out["exhaustive"]["ms_kernel"] / max(pr["ms_kernel"], 1e-9), 1),
             "gpu_launches": 6, "clocks": pr.pop("clocks")}
+    if rank == 0:
+        ref = reference_distance_kernel(inst, ifp, args.steps, args.warmup)
+        if ref is not None:
+            ref["equals_pruned"] = bool(np.array_equal(ref.pop("phi"), pr_phi))
+            ref["kernel_speedup_of_pruned"] = round(ref["ms_kernel"] / max(pr["ms_kernel"], 1e-9),
+                                                   1)
+        line["reference_kernel"] = ref
     if rank == 0 and not args.no_cpu_baseline:
         sys.path.insert(0, str(ROOT / "oracle"))
         import oracle as O
@@ -829,6 +867,48 @@ def run_dist(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     d.close()
+
+
+def reference_distance_kernel(inst, ifp, steps: int, warmup: int):
+    """The reference's own distance kernel (distanceToInterface_k, built
+    unchanged from its source into oracle/_ref) on this GPU with its own launch
+    shape: device time per launch (CUDA events, inputs resident) and time per
+    reset with its host copies (EuclideanDistance::resetPhi's sequence: points
+    and phi up, launch, phi down).  None when the image was not built."""
+    import torch
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import ref_dist
+    if not ref_dist.available():
+        return None
+    K = ref_dist.ReferenceDistanceKernel()
+    dev = torch.device("cuda")
+    xyz = torch.from_numpy(np.ascontiguousarray(inst.xyz, np.float32).reshape(-1)).to(dev)
+    pts = torch.from_numpy(np.ascontiguousarray(ifp, np.float32).reshape(-1)).to(dev)
+    phi = torch.from_numpy(np.ascontiguousarray(inst.phi, np.float64)).to(dev)
+    phi0 = phi.clone()
+    n, m = inst.np, len(ifp)
+    for _ in range(warmup):
+        phi.copy_(phi0)
+        K.launch(xyz.data_ptr(), n, pts.data_ptr(), m, phi.data_ptr())
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        phi.copy_(phi0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        K.launch(xyz.data_ptr(), n, pts.data_ptr(), m, phi.data_ptr())
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        out = K.reset_phi(inst.xyz, ifp, inst.phi)
+    wall = (time.perf_counter() - t0) * 1e3 / steps
+    K.close()
+    return {"ms_kernel": round(statistics.mean(ms), 3), "ms_per_reset": round(wall, 3),
+            "resets_per_s": round(1e3 / wall, 3), "phi": out,
+            "what": "distanceToInterface_k compiled unchanged from src/fem/EuclideanDistance.cu, "
+                    "512 threads per block, ceil(n/512) blocks (EuclideanDistance.cu:90-118)"}
 
 
 def run_p2(args):
