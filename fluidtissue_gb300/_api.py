@@ -78,6 +78,7 @@ class FtsBatchConfig(C.Structure):
         ("blocks", C.c_int32),
         ("ms_per_sweep", C.c_double),
         ("graph", C.c_int32),
+        ("spmv_format", C.c_int32),
     ]
 
     def as_dict(self) -> dict:

@@ -84,7 +84,7 @@ static void build_ell(Ctx& c) {
 // Source block of every lattice half-stencil entry: for node v and direction d
 // (0 = self, 1..7 = the positive Kuhn directions) the BSR block (v, v + d), or
 // -1 where the neighbour is outside the lattice or the block is absent.
-static void build_lattice(Ctx& c) {
+void build_lattice(Ctx& c) {
     const HostTopology& T = c.topo;
     const int64_t n = T.lattice_n;
     const int64_t tiles = (c.np + 31) / 32;

@@ -638,6 +638,17 @@ __global__ void k_to_lat(int64_t tiles, const int32_t* __restrict__ src,
     }
 }
 
+void launch_to_lat(Ctx& c) {
+    if (!c.lat_val || !c.lat_src || !c.A64)
+        throw CudaError(cudaErrorInvalidValue, "lattice copy without its map or the BSR",
+                        __FILE__, __LINE__);
+    const int64_t tiles = (c.np + 31) / 32;
+    k_to_lat<<<grid_for(c, tiles * 256), kThreads, 0, c.stream>>>(
+        tiles, c.lat_src, c.A64, reinterpret_cast<float4*>(c.lat_val));
+    FTS_CUDA(cudaGetLastError());
+    c.launches += 1;
+}
+
 void launch_to_f32(Ctx& c) {
     if ((c.use_lat && !c.lat_val) || (c.use_ell && !c.ell_val) ||
         (!c.use_lat && !c.use_ell && !c.A32) || !c.pc32)

@@ -12,7 +12,10 @@
 // The FP64 outer loop (true residual, solution update) runs per instance
 // between persistent launches; the whole sequence is captured as a CUDA graph
 // and replayed.  An autotuner picks the block size, the chunk length and the
-// number of threads per block row (the work split of the SpMV).
+// number of threads per block row (the work split of the SpMV) and, in mixed
+// precision, the SpMV's operator storage: the FP32 block rows (BSR), or the
+// FP32 lattice half stencil (thread per node, no column indices) on instances
+// whose mesh is a Kuhn lattice.
 //
 // Grid barrier (grid_sync.cuh): every wait has a time limit (a runtime field,
 // fts_batch_set_barrier_limit, 2 s by default) after which the kernel records
@@ -27,6 +30,7 @@
 
 #include "fts_device.cuh"
 #include "grid_sync.cuh"
+#include "lat_device.cuh"
 #include "mg_device.cuh"
 #include "reduce.cuh"
 
@@ -60,6 +64,8 @@ struct BInst {
     double crank;
     int use_mg;          // multigrid velocity preconditioner (else block Jacobi)
     int nlev;            // multigrid levels
+    const float4* lat;   // FP32 lattice half stencil used by the SpMV phase (else BSR)
+    int lat_n;           // its lattice size
     LevelView<T> lv[kMaxLevels];
 };
 
@@ -360,6 +366,28 @@ k_batch_minres(int ninst, BInst<T>* __restrict__ inst, int nchunks,
                 const int sub = threadIdx.x % TPR;
                 const int r = sub & 3, half = sub >> 2;  // half: column split (TPR = 8)
                 const int rows_per_pass = blockDim.x / TPR;
+                if (sizeof(T) == 4 && I.lat) {  // lattice half stencil, thread per node
+                    const V4<float>* Yf = reinterpret_cast<const V4<float>*>(Yv);
+                    const V4<float>* R1f = reinterpret_cast<const V4<float>*>(I.R[p]);
+                    V4<float>* qf = reinterpret_cast<V4<float>*>(I.q);
+                    const float tf = (float)tinv, wf = (float)wadd;
+                    for (int64_t v = C.row0 + threadIdx.x; v < C.row1; v += blockDim.x) {
+                        const float4 a = lat_row(I.lat_n, v, I.lat, Yf, wf);
+                        V4<float> qv;
+                        qv.x = a.x * tf;
+                        qv.y = a.y * tf;
+                        qv.z = a.z * tf;
+                        qv.w = a.w * tf;
+                        qf[v] = qv;
+                        const V4<float> yv = Yf[v], r1v = R1f[v];
+                        const float e0 = yv.x * tf, e1 = yv.y * tf, e2 = yv.z * tf,
+                                    e3 = (yv.w + wf) * tf;
+                        acc[0] += (double)(e0 * qv.x) + (double)(e1 * qv.y) +
+                                  (double)(e2 * qv.z) + (double)(e3 * qv.w);
+                        acc[1] += (double)(e0 * r1v.x) + (double)(e1 * r1v.y) +
+                                  (double)(e2 * r1v.z) + (double)(e3 * r1v.w);
+                    }
+                } else
                 for (int64_t row = C.row0 + threadIdx.x / TPR; row < C.row1; row += rows_per_pass) {
                     T ax = T(0);
                     const int32_t k1 = I.rowptr[row + 1];
@@ -685,7 +713,7 @@ struct fts_batch {
     cudaStream_t stream = nullptr;
     std::string last_error;
     // tuned launch shape of the persistent kernel
-    fts_batch_config cfg{256, 1024, 4, 0, 0.0, 0};
+    fts_batch_config cfg{256, 1024, 4, 0, 0.0, 0, FTS_BATCH_BSR};
     bool tuned = false;
     // device state
     std::vector<BChunk> chunks;   // row chunks (depth 0), then the multigrid levels by depth
@@ -857,6 +885,7 @@ static void batch_assemble(fts_batch& B, const std::vector<int>& have_mu) {
         launch_preconditioner(c);
         if (B.precision == FTS_PREC_MIXED) {
             launch_to_f32(c);
+            if (c.lat_val) launch_to_lat(c);
             if (c.use_mg) setup_preconditioner<float>(c);
         } else if (c.use_mg) {
             setup_preconditioner<double>(c);
@@ -941,6 +970,7 @@ static void batch_build(fts_batch& B) {
         a.rtol = 0.5;
         BInst<float>& f = B.h_inst32[i];
         std::memset(&f, 0, sizeof(f));
+        if (B.precision == FTS_PREC_MIXED && c.topo.lattice_n > 0) build_lattice(c);
         if (B.precision == FTS_PREC_MIXED) {
             f.np = c.np;
             f.rowptr = c.rowptr;
@@ -982,8 +1012,21 @@ static void batch_build(fts_batch& B) {
     batch_chunks(B, B.cfg.chunk_rows);
 }
 
+// The SpMV operator storage of every instance for a batch-wide format choice.
+static void batch_set_format(fts_batch& B, int format) {
+    for (int i = 0; i < B.count; ++i) {
+        const Ctx& c = B.ctx[i]->c;
+        const bool lat = format == FTS_BATCH_LATTICE && c.lat_val != nullptr;
+        B.h_inst32[i].lat = lat ? reinterpret_cast<const float4*>(c.lat_val) : nullptr;
+        B.h_inst32[i].lat_n = lat ? c.topo.lattice_n : 0;
+    }
+    B.cfg.spmv_format = format;
+}
+
 // Autotuner: time a fixed number of sweeps of the persistent kernel for every
-// candidate shape on the assembled batch; keep the fastest.
+// candidate shape (block size, chunk length, threads per block row and, in
+// mixed precision with Kuhn-lattice instances, the SpMV's operator storage) on
+// the assembled batch; keep the fastest.
 static void batch_tune(fts_batch& B) {
     const bool mixed = B.precision == FTS_PREC_MIXED;
     // a residual pass so that every instance has a right-hand side and a tolerance
@@ -1006,9 +1049,14 @@ static void batch_tune(fts_batch& B) {
     const long long sweeps = 24;
     fts_batch_config best = B.cfg;
     best.ms_per_sweep = 1e30;
+    bool any_lattice = false;
+    for (int i = 0; i < B.count; ++i) any_lattice = any_lattice || B.ctx[i]->c.lat_val != nullptr;
+    const int nfmt = mixed && any_lattice ? 2 : 1;
+    for (int fmt = 0; fmt < nfmt; ++fmt)
     for (int tc : threads_c)
         for (int cc : chunk_c)
             for (int tp : tpr_c) {
+                if (fmt == FTS_BATCH_LATTICE && tp != 4) continue;  // BSR instances only
                 B.cfg.threads = tc;
                 B.cfg.chunk_rows = cc;
                 B.cfg.tpr = tp;
@@ -1022,6 +1070,7 @@ static void batch_tune(fts_batch& B) {
                 FTS_CUDA(cudaStreamSynchronize(B.stream));
                 for (auto& a : B.h_inst64) a.rtol = 1e-30, a.maxit = sweeps + 1;
                 for (auto& a : B.h_inst32) a.rtol = 1e-30, a.maxit = sweeps + 1;
+                batch_set_format(B, fmt);
                 batch_chunks(B, cc);
                 if (mixed) launch_persistent<float>(B, 2);  // warm-up of this shape
                 else launch_persistent<double>(B, 2);
@@ -1041,6 +1090,7 @@ static void batch_tune(fts_batch& B) {
                 }
             }
     B.cfg = best;
+    batch_set_format(B, best.spmv_format);
     batch_chunks(B, B.cfg.chunk_rows);
     B.tuned = true;
 }

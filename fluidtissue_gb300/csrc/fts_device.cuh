@@ -230,6 +230,7 @@ void free_all(Ctx& c);
 int validate_params(const fts_params& p, std::string& err);
 void ensure_fp32(Ctx& c);
 void ensure_fp64_work(Ctx& c);
+void build_lattice(Ctx& c);         // lattice half-stencil map and FP32 storage
 
 // ---- assembly (assemble.cu) -----------------------------------------------
 void launch_geometry(Ctx& c, int* bad);
@@ -238,6 +239,7 @@ void launch_mu_minmax(Ctx& c);
 void launch_source(Ctx& c);
 void launch_rhs(Ctx& c, bool have_force);
 void launch_assemble(Ctx& c);       // FP64 BSR (allocated on first use)
+void launch_to_lat(Ctx& c);         // FP32 lattice half stencil from the FP64 BSR
 void launch_assemble_lat(Ctx& c);   // FP64 + FP32 lattice half stencils
 void launch_assemble_p2(Ctx& c);    // P2-P1 FP64 BSR over vertices + edges (p2.cu)
 void launch_rhs_p2(Ctx& c, bool have_force);

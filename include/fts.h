@@ -239,7 +239,12 @@ typedef struct fts_batch_config {
     int32_t blocks;
     double ms_per_sweep;
     int32_t graph;  /* 1 when the outer loop runs as a captured CUDA graph */
+    int32_t spmv_format;  /* operator storage of the Krylov SpMV phase: FTS_BATCH_BSR, or
+                             FTS_BATCH_LATTICE (the FP32 lattice half stencil on Kuhn-lattice
+                             instances, BSR on the others; mixed precision) */
 } fts_batch_config;
+
+enum { FTS_BATCH_BSR = 0, FTS_BATCH_LATTICE = 1 };
 
 /* count instances; meshes[count], params[count] (same precision and device). */
 int fts_batch_create(int32_t count, const fts_mesh* meshes, const fts_params* params,
