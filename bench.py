@@ -4,20 +4,32 @@ Workload (default): ``ellipsoid129`` — 129^3 Kuhn lattice (12.6M tets),
 jitter +-0.1h, ellipsoid level set, 16 Gaussian centres, mu = clip(1/(0.01+c),
 0.01, 100), relative residual 1e-8.  One step = one complete Stokes solve
 (viscosity, source, RHS and matrix assembly, Krylov solve, scatter to flow)
-from a zero initial guess, inputs resident in HBM.
+from a zero initial guess, inputs resident in HBM.  Inputs come from the numpy
+generator (fluidtissue_gb300/workloads.py).
 
 Reported:
-  value     mixed-precision solves/s (device-resident inputs)
+  value     mixed-precision solves/s (device-resident inputs, no per-launch
+            instrumentation in the timed region)
   e2e       the same through fts_solve with pinned host buffers (H2D of
             phi/source/mu and D2H of flow inside the timed region)
-  fp64      the plain FP64 GPU path on the same workload
-  roofline  the Krylov loop's operator kernel (BSR SpMV fused with the MINRES
-            dots), algorithmic bytes / CUDA-event time, vs measured HBM peak
+  fp64      the plain FP64 GPU path on the same workload and operator storage
+            (the FP64 lattice half stencil)
+  roofline  the Krylov loop's operator kernel (the FP32 lattice half-stencil
+            SpMV fused with the MINRES dots), algorithmic bytes / CUDA-event
+            time per launch, vs the measured HBM peak
+  roofline_iteration  algorithmic bytes of one whole MINRES iteration (operator,
+            both V-cycles over every level, updates) / time per iteration
+  batch96, spheres257, components  the batched and the 257^3 matrix-free
+            configurations, and the solve's neighbours (reaction-diffusion,
+            distance reset, level-set update, surface-tension load)
   cpu_baseline  the CPU oracle (restated reference algorithm) on the box's
-            host cores, bounded sample
+            host cores, bounded sample, with the measured fraction stated
 
-``--impl reference`` times the reference's algorithm on the host CPU (the
-oracle port): assembly + un-preconditioned BiCGSTAB, bounded sample.
+``--impl reference`` times the reference's CPU path (the oracle port) on the
+host cores with the same config dict: the reference's own BiCGSTAB to the end
+where it converges, else the restated assembly plus timed chunks of a
+converging CPU method (see run_reference); ``--workload dist129 --impl
+reference`` times the reference's own CUDA distance kernel.
 """
 from __future__ import annotations
 
@@ -322,6 +334,29 @@ def spheres257_subresult(args, local, dist, ws) -> dict:
             "operator_ms": round(m["per"], 4), "steps": 2, "warmup": 3, "clocks": m["clocks"]}
 
 
+def components_subresult(args, local, dist, ws, rank) -> dict:
+    """The solve's neighbours on the ellipsoid129 mesh, device figures only
+    (their own workloads add the CPU baselines): reaction-diffusion (32000
+    Euler steps), distance reset, level-set update and surface-tension load,
+    each with 3 warm-up and 3 timed calls."""
+    import copy
+    a = copy.copy(args)
+    a.steps, a.warmup, a.no_cpu_baseline = 3, 3, True
+    sub = (local, dist, ws, rank)
+    out = {}
+    for name, fn in (("rd129", run_rd), ("dist129", run_dist), ("ls129", run_ls),
+                     ("st129", run_st)):
+        line = fn(a, sub)
+        keep = {k: line[k] for k in ("metric", "value", "unit", "ms_per_step", "config", "e2e",
+                                     "gpu_launches", "clocks") if k in line}
+        for k in ("ms_device_per_call", "device_steps_per_s", "pruned", "iterations",
+                  "ms_assembly", "ms_solve", "ms_reset", "interface_points"):
+            if k in line:
+                keep[k] = line[k]
+        out[name] = keep
+    return out
+
+
 def run_ours(args):
     import torch
     from fluidtissue_gb300 import workloads as W
@@ -393,6 +428,7 @@ def run_ours(args):
     if args.workload == "ellipsoid129" and not args.no_subresults:
         res["batch96"] = batch_measure(args, 2, 3, local, dist, ws)
         res["spheres257"] = spheres257_subresult(args, local, dist, ws)
+        res["components"] = components_subresult(args, local, dist, ws, rank)
     if rank == 0 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(inst, args.cpu_seconds)
     if rank == 0:
@@ -701,7 +737,7 @@ def _rd_sources(inst, count=16):
     return inside[pick].astype(np.int32)
 
 
-def run_rd(args):
+def run_rd(args, sub=None):
     """Reaction-diffusion (RD::solve) on the ellipsoid129 mesh and level set:
     value = RD calls/s, one call = 32000 FP64 explicit Euler steps of the
     activator, inhibitor and growth factor on the interior submesh (all steps
@@ -712,9 +748,12 @@ def run_rd(args):
     from fluidtissue_gb300.flow import Mesh
     from fluidtissue_gb300.rd import RD
 
-    ws, rank, local = _dist()
-    dist = _setup_dist(ws, local)
-    torch.cuda.set_device(local)
+    if sub is None:
+        ws, rank, local = _dist()
+        dist = _setup_dist(ws, local)
+        torch.cuda.set_device(local)
+    else:
+        local, dist, ws, rank = sub
     inst = W.ellipsoid129()
     src = _rd_sources(inst)
     rd = RD()
@@ -756,6 +795,9 @@ def run_rd(args):
            "ms_device_per_call": round(ms_dev, 3), "ms_setup": round(st["ms_setup"], 3),
            "node_steps_per_s": round(nint * n_steps / (ms_dev / 1e3), 1),
            "gpu_launches": int(st["kernel_launches"]), "clocks": clocks}
+    if sub is not None:
+        rd.close()
+        return res
     if rank == 0 and not args.no_cpu_baseline:
         res["cpu_baseline"] = rd_cpu_baseline(inst, src, a0, i0, g0, n_steps)
     if rank == 0:
@@ -788,7 +830,7 @@ def rd_cpu_baseline(inst, src, a0, i0, g0, n_steps, sample_steps=200):
             "t_setup_s": t_setup, "t_step_s": t_step}
 
 
-def run_dist(args):
+def run_dist(args, sub=None):
     """Distance reset (EuclideanDistance::resetPhi) on the ellipsoid129 mesh
     against its own interface points (the zero level set's edge crossings,
     LevelSet.cpp:278-300): value = resets/s of the pruned search, through the
@@ -799,9 +841,12 @@ def run_dist(args):
     from fluidtissue_gb300 import workloads as W
     from fluidtissue_gb300.distance import EuclideanDistance, interface_points
 
-    ws, rank, local = _dist()
-    dist = _setup_dist(ws, local)
-    torch.cuda.set_device(local)
+    if sub is None:
+        ws, rank, local = _dist()
+        dist = _setup_dist(ws, local)
+        torch.cuda.set_device(local)
+    else:
+        local, dist, ws, rank = sub
     inst = W.ellipsoid129()
     ifp, _ = interface_points(inst.xyz, inst.tets, inst.phi)
     d = EuclideanDistance()
@@ -844,6 +889,9 @@ def run_dist(args):
             "pruned_equals_reference_algorithm": same,
             "kernel_speedup": round(out["exhaustive"]["ms_kernel"] / max(pr["ms_kernel"], 1e-9), 1),
             "gpu_launches": 6, "clocks": pr.pop("clocks")}
+    if sub is not None:
+        d.close()
+        return line
     if rank == 0:
         ref = reference_distance_kernel(inst, ifp, args.steps, args.warmup)
         if ref is not None:
@@ -1019,7 +1067,7 @@ def run_p2(args):
         print(json.dumps(line), flush=True)
 
 
-def run_st(args):
+def run_st(args, sub=None):
     """Surface-tension load (Flow::surfaceTension_ with LevelSet's normals,
     curvature and interface patches) on the ellipsoid129 mesh, phi = the
     workload's level set, phi_reset = its distance reset computed once on the
@@ -1030,9 +1078,12 @@ def run_st(args):
     from fluidtissue_gb300.flow import Mesh
     from fluidtissue_gb300.levelset import LevelSet
 
-    ws, rank, local = _dist()
-    dist = _setup_dist(ws, local)
-    torch.cuda.set_device(local)
+    if sub is None:
+        ws, rank, local = _dist()
+        dist = _setup_dist(ws, local)
+        torch.cuda.set_device(local)
+    else:
+        local, dist, ws, rank = sub
     inst = W.ellipsoid129()
     ls = LevelSet()
     if ls.init(Mesh(inst.xyz, inst.tets), device=local) != 0:
@@ -1071,6 +1122,9 @@ def run_st(args):
                     "h2d_bytes_per_step": 2 * 8 * inst.np, "d2h_bytes_per_step": 3 * 8 * inst.np},
             "interface_points": st["interface_points"], "area": st["area"],
             "gpu_launches": int(st["kernel_launches"]), "clocks": clk.stop()}
+    if sub is not None:
+        ls.close()
+        return line
     if rank == 0 and not args.no_cpu_baseline:
         sys.path.insert(0, str(ROOT / "oracle"))
         import oracle as O
@@ -1085,7 +1139,7 @@ def run_st(args):
     ls.close()
 
 
-def run_ls(args):
+def run_ls(args, sub=None):
     """Level-set update (LevelSet::update: Crank-Nicolson advection with
     Jacobi-BiCGSTAB, distance reset, mixing) on the ellipsoid129 mesh, advected
     by the velocity of its own mixed-precision Stokes solve (Advection dt 1/32,
@@ -1096,9 +1150,12 @@ def run_ls(args):
     from fluidtissue_gb300.flow import Flow, Mesh
     from fluidtissue_gb300.levelset import LevelSet
 
-    ws, rank, local = _dist()
-    dist = _setup_dist(ws, local)
-    torch.cuda.set_device(local)
+    if sub is None:
+        ws, rank, local = _dist()
+        dist = _setup_dist(ws, local)
+        torch.cuda.set_device(local)
+    else:
+        local, dist, ws, rank = sub
     inst = W.ellipsoid129()
     f = Flow()
     if f.init(Mesh(inst.xyz, inst.tets), inst.params, precision="mixed", device=local) != 0:
@@ -1140,6 +1197,9 @@ def run_ls(args):
             "ms_assembly": round(st["ms_assembly"], 3), "ms_solve": round(st["ms_solve"], 3),
             "ms_reset": round(st["ms_reset"], 3), "gpu_launches": int(st["kernel_launches"]),
             "clocks": clk.stop()}
+    if sub is not None:
+        ls.close()
+        return line
     if rank == 0 and not args.no_cpu_baseline:
         sys.path.insert(0, str(ROOT / "oracle"))
         import oracle as O
