@@ -577,7 +577,10 @@ k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
 
 // Multigrid stage 2, fused with the V-cycle's last post-smoothing step on the
 // finest level: y.xyz = the step's new x (not stored in the level), and with
-// pmg y.w likewise from the pressure V-cycle; beta.  (Running the pressure
+// pmg y.w likewise from the pressure V-cycle; beta.  With degree-1 smoothing on
+// a finest level (fine1 / pfine1) that step is the pointwise x + d_0.  (Running
+// the pressure V-cycle's last step on its own stream instead, and reading its x
+// here, gave no gain: the pressure stream then ends after the velocity one.)  (Running the pressure
 // V-cycle's last step on its own stream instead, and reading its x here, made
 // the solve slower: 224.7 -> 226.2 ms on ellipsoid129, the pressure stream
 // then ends after the velocity one.)
@@ -585,7 +588,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads)
 k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, PView<T> P0,
              int pmg, int init, const V4<T>* __restrict__ Rn, V4<T>* __restrict__ Ynew,
-             int ybuf, Reduction red, MinresScalars* s) {
+             int ybuf, int fine1, int pfine1, Reduction red, MinresScalars* s) {
     pdl_wait();
     if (s->stop) return;
     double acc[1] = {0.0};
@@ -596,14 +599,20 @@ k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, PVi
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L0.N;
          i += (int64_t)gridDim.x * blockDim.x) {
         T xo[3];
-        mg_step_node<T>(L0, i, step, mode, din, nullptr, xo, false, false);
+        if (fine1) {  // degree-1 finest level: x + d_0
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) xo[cc] = L0.x[cc * L0.N + i] + L0.d0[cc * L0.N + i];
+        } else {
+            mg_step_node<T>(L0, i, step, mode, din, nullptr, xo, false, false);
+        }
         const V4<T> n = Rn[i];
         V4<T> z = Ynew[i];
         z.x = xo[0];
         z.y = xo[1];
         z.z = xo[2];
         if (pmg) {
-            z.w = pmg_step_node<T>(P0, i, ps, pmode, pdin, nullptr, false);
+            z.w = pfine1 ? P0.x[i] + P0.d0[i]
+                         : pmg_step_node<T>(P0, i, ps, pmode, pdin, nullptr, false);
             acc[0] += (double)(n.w * z.w);
         }
         Ynew[i] = z;
@@ -704,7 +713,8 @@ static void launch_pc(Ctx& c, bool use_mg, int init, const V4<T>* q, V4<T>* R1, 
         constexpr int s = kSmooth - 1;
         pdl_launch(k_minres_pc2<T>, gn, kThreads, c.stream,
             L0, s, s == 1 ? kStepAfterFirst : kStepRegular, (s & 1) ? L0.d0 : L0.d1, P0,
-            pmg ? 1 : 0, init, Rn, Ynew, ybuf, c.red, c.ms);
+            pmg ? 1 : 0, init, Rn, Ynew, ybuf, mg_level_degree1(mg, 0) ? 1 : 0,
+            pmg && pmg_level_degree1(pmg_of<T>(c), 0) ? 1 : 0, c.red, c.ms);
         c.launches += 2;
     } else {
         pdl_launch(k_minres_pc1<T, false>, gn, kThreads, c.stream, c.np, init, q, R1, R2, Rn, pc, Ynew,

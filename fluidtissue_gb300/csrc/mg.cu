@@ -424,6 +424,26 @@ k_mg_resid_first(LevelView<T> L, const int* __restrict__ stop) {
 }
 
 template <typename T>
+__global__ void __launch_bounds__(kThreads, 4)
+k_mg_resid_d0(LevelView<T> L, const int* __restrict__ stop) {
+    pdl_wait();
+    if (stop && *stop) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.N;
+         i += (int64_t)gridDim.x * blockDim.x)
+        mg_resid_d0_node<T>(L, i);
+}
+
+// x += d_0 (the degree-1 post-smoothing update).
+template <typename T>
+__global__ void k_mg_add_d0(LevelView<T> L, const int* __restrict__ stop) {
+    pdl_wait();
+    if (stop && *stop) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 3 * L.N;
+         i += (int64_t)gridDim.x * blockDim.x)
+        L.x[i] += L.d0[i];
+}
+
+template <typename T>
 __global__ void k_mg_restrict(LevelView<T> F, LevelView<T> C, const int* __restrict__ stop) {
     pdl_wait();
     if (stop && *stop) return;
@@ -707,6 +727,21 @@ static void vcycle_level(Ctx& c, MG<T>& mg, size_t l, const int* stop, bool skip
         return;
     }
     const LevelView<T> C = level_view(mg, l + 1);
+    if (mg_level_degree1(mg, l)) {
+        // degree 1: x = d_0, r = b - K d_0; after the coarse correction
+        // r = b - K x, d_0 = D^-1 r / theta, x += d_0 (the caller's when skip_final)
+        pdl_launch(k_mg_resid_d0<T>, g, kThreads, c.stream, L, stop);
+        k_mg_restrict<T><<<grid_for(c, C.N), kThreads, 0, c.stream>>>(L, C, stop);
+        vcycle_level<T>(c, mg, l + 1, stop, false);
+        pdl_launch(k_mg_prolong<T>, g, kThreads, c.stream, L, C, stop);
+        pdl_launch(k_mg_resid_first<T>, g, kThreads, c.stream, L, stop);
+        c.launches += 4;
+        if (!skip_final) {
+            pdl_launch(k_mg_add_d0<T>, grid_for(c, 3 * L.N), kThreads, c.stream, L, stop);
+            c.launches += 1;
+        }
+        return;
+    }
     // pre-smoothing from zero (d_0 is already in L.d0)
     T* din = L.d0;
     T* dout = L.d1;

@@ -11,6 +11,11 @@ namespace fts {
 struct Ctx;
 
 constexpr int kSmooth = 2;        // Chebyshev degree of each pre / post smoothing
+// The first kDeg1Levels levels (below the cluster tail) smooth with Chebyshev
+// degree 1 instead of kSmooth: damped Jacobi with the level's 1/theta, one
+// stencil pass before and one after the coarse correction instead of two; on
+// the finest level the caller's final update is then pointwise.
+constexpr int kDeg1Levels = 1;
 constexpr int kCoarse = 20;       // Chebyshev degree of the coarsest-level solve
 constexpr int kPowerIters = 12;   // power iterations for lambda_max(D^-1 K)
 constexpr double kLamSafety = 1.1;
@@ -65,6 +70,14 @@ struct MG {
     int tail_level = -1;
     int tail_blocks = 0;
 };
+
+// Level l smooths with degree 1 (kDeg1Levels) unless it is the coarsest or
+// part of the cluster tail (small levels keep kSmooth).
+template <typename T>
+inline bool mg_level_degree1(const MG<T>& mg, size_t l) {
+    return (int)l < kDeg1Levels && (mg.tail_level < 0 || (int)l < mg.tail_level) &&
+           l + 1 < mg.L.size();
+}
 
 // Nodes per axis of the next coarser lattice.
 inline int mg_coarse_n(int n) { return n % 2 ? (n + 1) / 2 : n / 2 + 1; }

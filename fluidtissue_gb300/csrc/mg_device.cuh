@@ -313,6 +313,21 @@ __device__ __forceinline__ void mg_resid_node(const LevelView<T>& L, int64_t v) 
     for (int c = 0; c < 3; ++c) L.r[c * N + v] = L.b[c * N + v] - ks * y[c];
 }
 
+// Degree-1 pre-smoothing from zero: x = d_0 (= D^-1 b / theta) and
+// r = b - K d_0 at node v.
+template <typename T, bool SPLIT = true>
+__device__ __forceinline__ void mg_resid_d0_node(const LevelView<T>& L, int64_t v) {
+    const int64_t N = L.N;
+    const T ks = (T)*L.ks;
+    T y[3];
+    stencil_apply<T, typename MGStore<T>::type, SPLIT>(L.n, N, v, L.K, L.d0, y);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        L.r[c * N + v] = L.b[c * N + v] - ks * y[c];
+        L.x[c * N + v] = L.d0[c * N + v];
+    }
+}
+
 // r = b - K x and d_0 = D^-1 r / theta at node v (x is left for the next step).
 template <typename T, bool SPLIT = true>
 __device__ __forceinline__ void mg_resid_first_node(const LevelView<T>& L, int64_t v) {

@@ -237,6 +237,25 @@ k_pmg_resid_first(PView<T> L, const int* __restrict__ stop) {
 }
 
 template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_pmg_resid_d0(PView<T> L, const int* __restrict__ stop) {
+    pdl_wait();
+    if (stop && *stop) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.N;
+         i += (int64_t)gridDim.x * blockDim.x)
+        pmg_resid_d0_node<T>(L, i);
+}
+
+template <typename T>
+__global__ void k_pmg_add_d0(PView<T> L, const int* __restrict__ stop) {
+    pdl_wait();
+    if (stop && *stop) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.N;
+         i += (int64_t)gridDim.x * blockDim.x)
+        L.x[i] += L.d0[i];
+}
+
+template <typename T>
 __global__ void k_pmg_restrict(PView<T> F, PView<T> C, const int* __restrict__ stop) {
     pdl_wait();
     if (stop && *stop) return;
@@ -519,6 +538,21 @@ static void pvcycle_level(Ctx& c, PMG<T>& pm, size_t l, cudaStream_t st, const i
     }
     const PView<T> L = pview(pm, l), C = pview(pm, l + 1);
     const int g = grid_for(c, L.N);
+    if (pmg_level_degree1(pm, l)) {
+        // degree 1: x = d_0, r = b - Kp d_0; after the coarse correction
+        // r = b - Kp x, d_0 = D^-1 r / theta, x += d_0 (the caller's when skip_final)
+        pdl_launch(k_pmg_resid_d0<T>, g, kThreads, st, L, stop);
+        k_pmg_restrict<T><<<grid_for(c, C.N), kThreads, 0, st>>>(L, C, stop);
+        pvcycle_level<T>(c, pm, l + 1, st, stop, false);
+        pdl_launch(k_pmg_prolong<T>, g, kThreads, st, L, C, stop);
+        pdl_launch(k_pmg_resid_first<T>, g, kThreads, st, L, stop);
+        c.launches += 4;
+        if (!skip_final) {
+            pdl_launch(k_pmg_add_d0<T>, g, kThreads, st, L, stop);
+            c.launches += 1;
+        }
+        return;
+    }
     T* din = L.d0;
     T* dout = L.d1;
     for (int s = 1; s < kPSmooth; ++s) {

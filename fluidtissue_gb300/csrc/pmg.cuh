@@ -62,6 +62,16 @@ struct PMG {
     cudaEvent_t ev_copied = nullptr;        // both copied to the host
 };
 
+// The first kPDeg1Levels levels of the pressure hierarchy smooth with degree 1
+// (as kDeg1Levels for the velocity hierarchy); level l does unless it is the
+// coarsest or part of the single-CTA tail.
+constexpr int kPDeg1Levels = 1;
+template <typename T>
+inline bool pmg_level_degree1(const PMG<T>& pm, size_t l) {
+    return (int)l < kPDeg1Levels && (pm.tail_level < 0 || (int)l < pm.tail_level) &&
+           l + 1 < pm.L.size();
+}
+
 // One level as the kernels see it.
 template <typename T>
 struct PView {

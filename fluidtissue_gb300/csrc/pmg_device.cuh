@@ -49,6 +49,13 @@ __device__ __forceinline__ T pmg_stencil(int n, int64_t N, int64_t v64, const T*
     return pmg_stencil_body<T, false>(n, N, v, i, j, k, K, x);
 }
 
+// Degree-1 pre-smoothing from zero: x = d_0, r = b - Kp d_0.
+template <typename T>
+__device__ __forceinline__ void pmg_resid_d0_node(const PView<T>& L, int64_t v) {
+    L.r[v] = L.b[v] - pmg_stencil<T>(L.n, L.N, v, L.K, L.d0);
+    L.x[v] = L.d0[v];
+}
+
 // d_0 = D^-1 b / theta.
 template <typename T>
 __device__ __forceinline__ void pmg_first_dir(const PView<T>& L, int64_t v, T bv) {
