@@ -26,6 +26,8 @@ void free_all(Ctx& c) {
         if (p) cudaFree(p);
     mg_free(c.mg64);
     mg_free(c.mg32);
+    p2mg_free(c.p2mg64);
+    p2mg_free(c.p2mg32);
     pmg_free(c.pmg64);
     pmg_free(c.pmg32);
     if (c.ev_fork) cudaEventDestroy(c.ev_fork);
@@ -142,11 +144,6 @@ int validate_params(const fts_params& p, std::string& err) {
         err = "P2-P1 runs on the assembled operator (FTS_OP_AUTO or FTS_OP_ASSEMBLED)";
         return FTS_ERR_UNSUPPORTED;
     }
-    if (p.velocity_degree == 2 && p.preconditioner != FTS_PC_AUTO &&
-        p.preconditioner != FTS_PC_JACOBI) {
-        err = "P2-P1 uses the block-Jacobi preconditioner (FTS_PC_AUTO or FTS_PC_JACOBI)";
-        return FTS_ERR_UNSUPPORTED;
-    }
     if (p.precision != FTS_PREC_FP64 && p.precision != FTS_PREC_MIXED) {
         err = "unknown precision";
         return FTS_ERR_BAD_INPUT;
@@ -180,7 +177,8 @@ int validate_params(const fts_params& p, std::string& err) {
 static int mg_levels(int n) { return (int)mg_chain(n).size(); }
 
 static bool last_layers_dirichlet(const HostTopology& T, int n) {
-    for (int64_t v = 0; v < T.np; ++v) {
+    const int64_t nvert = (int64_t)n * n * n;  // the lattice's nodes (P2: its vertices)
+    for (int64_t v = 0; v < nvert; ++v) {
         const int64_t i = v % n, j = (v / n) % n, k = v / ((int64_t)n * n);
         if ((i == n - 1 || j == n - 1 || k == n - 1) && !T.bnd[v]) return false;
     }
@@ -188,7 +186,8 @@ static bool last_layers_dirichlet(const HostTopology& T, int n) {
 }
 
 static void configure_preconditioner(Ctx& c) {
-    const int n = c.topo.lattice_n;
+    // P2-P1: the velocity V-cycle has the P2 level above the vertex lattice
+    const int n = c.p2 ? c.topo.vertex_lattice_n : c.topo.lattice_n;
     const bool mg_ok = n > 0 && mg_levels(n) >= 3 &&
                        (n % 2 == 1 || last_layers_dirichlet(c.topo, n));
     const bool want_mg = c.par.preconditioner == FTS_PC_MULTIGRID ||
@@ -202,7 +201,8 @@ static void configure_preconditioner(Ctx& c) {
     // batched solves keep the pressure diagonal: on batch96 (jumps of mu up to
     // 1e3 across spheres) a pressure V-cycle inside the persistent kernel cut
     // no iterations and its registers slowed every phase
-    c.use_pmg = c.use_mg && !c.in_batch && c.par.preconditioner != FTS_PC_MULTIGRID_DIAG;
+    c.use_pmg = c.use_mg && !c.in_batch && !c.p2 &&
+                c.par.preconditioner != FTS_PC_MULTIGRID_DIAG;
     if (c.use_pmg && !c.aux_stream) {
         FTS_CUDA(cudaStreamCreateWithFlags(&c.aux_stream, cudaStreamNonBlocking));
         FTS_CUDA(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));
@@ -212,7 +212,7 @@ static void configure_preconditioner(Ctx& c) {
         c.last_error = "the stencil operator needs a Kuhn lattice mesh";
         throw (int)FTS_ERR_UNSUPPORTED;
     }
-    c.use_lat = !c.matfree && !c.in_batch && n > 0 &&
+    c.use_lat = !c.matfree && !c.in_batch && !c.p2 && n > 0 &&
                 (c.par.operator_kind == FTS_OP_AUTO || c.par.operator_kind == FTS_OP_STENCIL);
     // both precisions: the FP64 solve runs its operator on the FP64 half
     // stencil (1 KB/node) as the mixed solve's outer residual does
@@ -394,6 +394,9 @@ static int solve_device(Ctx& c, bool have_mu, bool have_force, double* flow_out,
         if (P.precision == FTS_PREC_MIXED) {
             ensure_fp32(c);
             launch_to_f32(c);
+            setup_preconditioner<float>(c);
+        } else {
+            setup_preconditioner<double>(c);
         }
     } else if (c.use_lat64) {
         // Kuhn lattice: the FP64 half stencil (and for mixed precision the

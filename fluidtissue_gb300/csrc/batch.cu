@@ -257,7 +257,7 @@ __device__ void batch_pc2(const BInst<T>* __restrict__ inst, int nchunks,
             z.y = xo[1];
             z.z = xo[2];
             Yn[i] = z;
-            acc[0] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z);
+            acc[0] += (double)(n.x * z.x + n.y * z.y + n.z * z.z);
         }
         block_sum<1>(acc);
         if (threadIdx.x == 0) part[(int64_t)ch * 3 + 2] = acc[0];
@@ -382,10 +382,9 @@ k_batch_minres(int ninst, BInst<T>* __restrict__ inst, int nchunks,
                         const V4<float> yv = Yf[v], r1v = R1f[v];
                         const float e0 = yv.x * tf, e1 = yv.y * tf, e2 = yv.z * tf,
                                     e3 = (yv.w + wf) * tf;
-                        acc[0] += (double)(e0 * qv.x) + (double)(e1 * qv.y) +
-                                  (double)(e2 * qv.z) + (double)(e3 * qv.w);
-                        acc[1] += (double)(e0 * r1v.x) + (double)(e1 * r1v.y) +
-                                  (double)(e2 * r1v.z) + (double)(e3 * r1v.w);
+                        acc[0] += (double)fmaf(e0, qv.x, fmaf(e1, qv.y, fmaf(e2, qv.z, e3 * qv.w)));
+                        acc[1] += (double)fmaf(e0, r1v.x,
+                                               fmaf(e1, r1v.y, fmaf(e2, r1v.z, e3 * r1v.w)));
                     }
                 } else
                 for (int64_t row = C.row0 + threadIdx.x / TPR; row < C.row1; row += rows_per_pass) {

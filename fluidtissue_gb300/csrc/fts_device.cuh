@@ -9,6 +9,7 @@
 #include "fts.h"
 #include "fts_internal.h"
 #include "mg.cuh"
+#include "p2mg.cuh"
 #include "pmg.cuh"
 
 struct fts_ctx;
@@ -195,6 +196,8 @@ struct Ctx {
     bool use_mg = false;
     MG<double> mg64;
     MG<float> mg32;
+    P2MG<double> p2mg64;  // P2-P1: the P2 velocity level above the vertex hierarchy
+    P2MG<float> p2mg32;
     // pressure-block V-cycle (Kuhn lattices with the velocity multigrid): runs
     // on aux_stream between the events ev_fork and ev_join of each application
     bool use_pmg = false;

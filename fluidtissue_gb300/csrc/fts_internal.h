@@ -37,6 +37,10 @@ struct HostTopology {
                                    // 01 02 03 12 13 23 as nv + edge id (Tetrahedron.hpp:61)
     std::vector<int32_t> xp2t_ptr; // [np'+1] system node -> (tet << 4 | local DOF 0..9)
     std::vector<uint32_t> xp2t;
+    int32_t vertex_lattice_n = 0;  // P2: n if the vertices form the Kuhn lattice of n^3
+    std::vector<int32_t> edge_ends;  // P2: [2 ne] end vertices of edge e (lower first)
+    std::vector<int32_t> vinc_ptr;   // P2: [nv+1] edges incident to each vertex
+    std::vector<int32_t> vinc;       // P2: [2 ne]
 };
 
 // Validates the mesh and builds the topology (OpenMP).  Returns an fts_status.

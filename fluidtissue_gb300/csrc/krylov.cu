@@ -433,10 +433,11 @@ k_minres_A_lat(int n, int64_t np, const float4* __restrict__ L, const V4<float>*
         const V4<float> yv = Y[v], r1 = R1[v];
         const float e0 = yv.x * tinv, e1 = yv.y * tinv, e2 = yv.z * tinv,
                     e3 = (yv.w + wadd) * tinv;
-        acc[0] += (double)(e0 * qv.x) + (double)(e1 * qv.y) + (double)(e2 * qv.z) +
-                  (double)(e3 * qv.w);
-        acc[1] += (double)(e0 * r1.x) + (double)(e1 * r1.y) + (double)(e2 * r1.z) +
-                  (double)(e3 * r1.w);
+        // a node's four products summed in FP32, the node sums in FP64: one
+        // conversion and one FP64 add per dot and node (GB300's FP64 pipe is
+        // narrow; four of each per node kept it a third busy)
+        acc[0] += (double)fmaf(e0, qv.x, fmaf(e1, qv.y, fmaf(e2, qv.z, e3 * qv.w)));
+        acc[1] += (double)fmaf(e0, r1.x, fmaf(e1, r1.y, fmaf(e2, r1.z, e3 * r1.w)));
     }
     double tot[2];
     if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
@@ -556,7 +557,7 @@ k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
             mg_first_dir<T>(L0, i, bv);
         } else {
             pc_jacobi<T>(pc, i, n, z);
-            acc[2] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z);
+            acc[2] += (double)(n.x * z.x + n.y * z.y + n.z * z.z);
         }
         Ynew[i] = z;
         acc[0] += (double)n.w;
@@ -606,17 +607,20 @@ k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, PVi
             mg_step_node<T>(L0, i, step, mode, din, nullptr, xo, false, false);
         }
         const V4<T> n = Rn[i];
-        V4<T> z = Ynew[i];
+        V4<T> z;
         z.x = xo[0];
         z.y = xo[1];
         z.z = xo[2];
+        T dz = n.x * z.x + n.y * z.y + n.z * z.z;  // node sum in T, FP64 across nodes
         if (pmg) {
             z.w = pfine1 ? P0.x[i] + P0.d0[i]
                          : pmg_step_node<T>(P0, i, ps, pmode, pdin, nullptr, false);
-            acc[0] += (double)(n.w * z.w);
+            dz += n.w * z.w;
+        } else {
+            z.w = Ynew[i].w;  // stage 1's pressure diagonal (its dot is in pdot)
         }
         Ynew[i] = z;
-        acc[0] += (double)(n.x * z.x) + (double)(n.y * z.y) + (double)(n.z * z.z);
+        acc[0] += (double)dz;
     }
     double tot[1];
     if (grid_sum<1>(acc, red, tot) && threadIdx.x == 0) {
@@ -654,6 +658,10 @@ k_minres_C(int64_t np, const V4<T>* __restrict__ Yk, int ybuf, V4<T>* Wprev,
     }
     if (last_block(red) && threadIdx.x == 0) s->c_pending = 0;
 }
+
+// The P2 velocity level as a LevelView (p2mg.cu).
+template <typename T>
+LevelView<T> p2_level_view(Ctx& c);
 
 template <typename T>
 static const T* op_of(const Ctx& c);
@@ -695,7 +703,9 @@ static void launch_pc(Ctx& c, bool use_mg, int init, const V4<T>* q, V4<T>* R1, 
     const T* pc = pc_of<T>(c);
     if (use_mg) {
         MG<T>& mg = mg_of<T>(c);
-        const LevelView<T> L0 = level_view(mg, 0);
+        // P2-P1: the finest level is the P2 velocity level (degree-1 smoothing)
+        const LevelView<T> L0 = c.p2 ? p2_level_view<T>(c) : level_view(mg, 0);
+        const bool fine1 = c.p2 || mg_level_degree1(mg, 0);
         const bool pmg = c.use_pmg;
         const PView<T> P0 = pmg ? pview(pmg_of<T>(c), 0) : PView<T>{};
         pdl_launch(k_minres_pc1<T, true>, gn, kThreads, c.stream, c.np, init, q, R1, R2, Rn, pc, Ynew,
@@ -707,13 +717,14 @@ static void launch_pc(Ctx& c, bool use_mg, int init, const V4<T>* q, V4<T>* R1, 
             pmg_vcycle<T>(c, pmg_of<T>(c), c.aux_stream, &c.ms->stop, true);
             FTS_CUDA(cudaEventRecord(c.ev_join, c.aux_stream));
         }
-        mg_vcycle<T>(c, mg, &c.ms->stop, true);
+        if (c.p2) p2mg_vcycle<T>(c, &c.ms->stop);
+        else mg_vcycle<T>(c, mg, &c.ms->stop, true);
         if (pmg) FTS_CUDA(cudaStreamWaitEvent(c.stream, c.ev_join, 0));
         // the last post-smoothing step: step kSmooth - 1 reads d0 when it is odd
         constexpr int s = kSmooth - 1;
         pdl_launch(k_minres_pc2<T>, gn, kThreads, c.stream,
             L0, s, s == 1 ? kStepAfterFirst : kStepRegular, (s & 1) ? L0.d0 : L0.d1, P0,
-            pmg ? 1 : 0, init, Rn, Ynew, ybuf, mg_level_degree1(mg, 0) ? 1 : 0,
+            pmg ? 1 : 0, init, Rn, Ynew, ybuf, fine1 ? 1 : 0,
             pmg && pmg_level_degree1(pmg_of<T>(c), 0) ? 1 : 0, c.red, c.ms);
         c.launches += 2;
     } else {
@@ -834,6 +845,7 @@ void setup_preconditioner(Ctx& c) {
         pmg_setup_finish<T>(c, pm, c.aux_stream);
         return;
     }
+    if (c.use_mg && c.p2) p2mg_setup<T>(c);  // the P2 level first: its K2 feeds the P1 level
     if (c.use_mg) mg_setup<T>(c, mg_of<T>(c));
     if (c.use_pmg) pmg_setup<T>(c, pmg_of<T>(c));
 }

@@ -277,8 +277,8 @@ k_mf_gather_minres_A(int n, int64_t np, const float* __restrict__ cube,
         q[v] = o4;
         const V4<float> r1 = R1[v];
         const float v0 = yv.x * tinv, v1 = yv.y * tinv, v2 = yv.z * tinv, v3 = (yv.w + wadd) * tinv;
-        acc[0] += (double)(v0 * o4.x) + (double)(v1 * o4.y) + (double)(v2 * o4.z) + (double)(v3 * o4.w);
-        acc[1] += (double)(v0 * r1.x) + (double)(v1 * r1.y) + (double)(v2 * r1.z) + (double)(v3 * r1.w);
+        acc[0] += (double)fmaf(v0, o4.x, fmaf(v1, o4.y, fmaf(v2, o4.z, v3 * o4.w)));
+        acc[1] += (double)fmaf(v0, r1.x, fmaf(v1, r1.y, fmaf(v2, r1.z, v3 * r1.w)));
     }
     double tot[2];
     if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {
@@ -365,8 +365,8 @@ k_mf_gather_map_minres_A(int64_t np, const int32_t* __restrict__ p2t_ptr,
         q[v] = o;
         const V4<float> r1 = R1[v];
         const float v0 = yv.x * tinv, v1 = yv.y * tinv, v2 = yv.z * tinv, v3 = (yv.w + wadd) * tinv;
-        acc[0] += (double)(v0 * o.x) + (double)(v1 * o.y) + (double)(v2 * o.z) + (double)(v3 * o.w);
-        acc[1] += (double)(v0 * r1.x) + (double)(v1 * r1.y) + (double)(v2 * r1.z) + (double)(v3 * r1.w);
+        acc[0] += (double)fmaf(v0, o.x, fmaf(v1, o.y, fmaf(v2, o.z, v3 * o.w)));
+        acc[1] += (double)fmaf(v0, r1.x, fmaf(v1, r1.y, fmaf(v2, r1.z, v3 * r1.w)));
     }
     double tot[2];
     if (grid_sum<2>(acc, red, tot) && threadIdx.x == 0) {

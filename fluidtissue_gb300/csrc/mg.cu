@@ -378,7 +378,7 @@ constexpr double kLowFrac = 0.1;
 constexpr int kCoarseThreads = 256;  // one CTA for the coarsest level (<= 9^3 nodes)
 
 // Chebyshev coefficients of one level, computed once per solve on the host.
-static void cheb_table(double lam, double* out) {
+void cheb_table(double lam, double* out) {
     const double lmax = lam, lmin = lam * kLowFrac;
     const double th = 0.5 * (lmax + lmin), de = 0.5 * (lmax - lmin), sg = th / de;
     out[0] = 1.0 / th;
@@ -565,7 +565,9 @@ template <typename T>
 void mg_build(Ctx& c, MG<T>& mg) {
     if (mg.built) return;
     init_tables(c.device);
-    for (const int n : mg_chain(c.topo.lattice_n)) {
+    // P2-P1: the hierarchy lives on the vertex lattice below the P2 level
+    const int lattice_n = c.p2 ? c.topo.vertex_lattice_n : c.topo.lattice_n;
+    for (const int n : mg_chain(lattice_n)) {
         MGLevel<T> L;
         L.n = n;
         L.N = (int64_t)n * n * n;
@@ -643,6 +645,8 @@ void mg_setup(Ctx& c, MG<T>& mg) {
     else if (c.matfree)
         k_mg_from_elements<T, false><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(
             F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.bnd, F.K);
+    else if (c.p2)
+        p2mg_galerkin<T>(c, F.K, F.mask, F.n);
     else if (c.use_lat64)
         k_mg_extract_lat<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(F.n, c.lat64, F.K);
     else

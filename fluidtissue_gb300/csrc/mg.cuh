@@ -79,6 +79,10 @@ inline bool mg_level_degree1(const MG<T>& mg, size_t l) {
            l + 1 < mg.L.size();
 }
 
+// Chebyshev coefficients of one level for lambda_max = lam: 1/theta, then
+// (ca_s, cb_s) for s >= 1 (kCoefStride values).
+void cheb_table(double lam, double* out);
+
 // Nodes per axis of the next coarser lattice.
 inline int mg_coarse_n(int n) { return n % 2 ? (n + 1) / 2 : n / 2 + 1; }
 

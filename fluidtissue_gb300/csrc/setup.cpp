@@ -311,6 +311,28 @@ int extend_p2(const fts_mesh& m, HostTopology& T, std::string& err) {
         err = "mesh: too many P2 nodes for 32-bit indices";
         return FTS_ERR_BAD_INPUT;
     }
+    // edge end vertices and the edges at each vertex (the P2 -> P1 transfer)
+    T.edge_ends.assign((size_t)2 * ne, 0);
+    for (int64_t i = 0; i < nv; ++i)
+        for (int32_t q = T.rowptr[i]; q < T.rowptr[i + 1]; ++q)
+            if (eid[q] >= 0) {
+                T.edge_ends[2 * eid[q]] = (int32_t)i;
+                T.edge_ends[2 * eid[q] + 1] = T.cols[q];
+            }
+    T.vinc_ptr.assign((size_t)nv + 1, 0);
+    for (int64_t e = 0; e < ne; ++e) {
+        T.vinc_ptr[T.edge_ends[2 * e] + 1]++;
+        T.vinc_ptr[T.edge_ends[2 * e + 1] + 1]++;
+    }
+    for (int64_t i = 0; i < nv; ++i) T.vinc_ptr[i + 1] += T.vinc_ptr[i];
+    T.vinc.assign((size_t)2 * ne, 0);
+    {
+        std::vector<int32_t> fill(T.vinc_ptr.begin(), T.vinc_ptr.end() - 1);
+        for (int64_t e = 0; e < ne; ++e) {
+            T.vinc[fill[T.edge_ends[2 * e]]++] = (int32_t)e;
+            T.vinc[fill[T.edge_ends[2 * e + 1]]++] = (int32_t)e;
+        }
+    }
     auto edge_of = [&](int32_t a, int32_t b) -> int64_t {
         if (a > b) std::swap(a, b);
         const int32_t* c0 = T.cols.data() + T.rowptr[a];
@@ -421,6 +443,7 @@ int extend_p2(const fts_mesh& m, HostTopology& T, std::string& err) {
     int64_t nI = 0;
     for (int64_t i = 0; i < nn; ++i) nI += T.bnd[i] ? 0 : 1;
     T.n_interior = nI;
+    T.vertex_lattice_n = T.lattice_n;
     T.nv = nv;
     T.ne = ne;
     T.np = nn;
