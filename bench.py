@@ -171,26 +171,31 @@ def hierarchy_fraction(n: int) -> float:
     return tot
 
 
-# Algorithmic bytes per finest node of one MINRES iteration of the mixed solve
-# (each kernel's stencil and vectors read once, outputs written once; FP32
-# vectors, FP16 velocity stencil of 144 B/node, FP32 pressure stencil of 32 B):
-#   operator (lattice half stencil 512 B + x, r1, q)               560
-#   stage 1 (q, r1, r2 in; r_new, y out; velocity and pressure b, d_0, D^-1)  140
-#   velocity V-cycle per level node: pre-step 228, residual 180, restriction 18,
-#     prolongation 25.5, post residual + d_0 216, post-step / stage 2 240   907.5
-#   pressure V-cycle per level node: 56, 44, 6, 8.5, 52, 60                   226.5
-#   update of w and x (y, w_prev, w_cur, x in; w, x out)                       96
-ITERATION_BYTES = {"operator": 560.0, "stage1": 140.0, "velocity_level": 907.5,
-                   "pressure_level": 226.5, "update": 96.0}
+# Algorithmic bytes per node of one MINRES iteration of the mixed solve (each
+# kernel's stencil and vectors read once, outputs written once; FP32 vectors,
+# FP16 velocity stencil of 144 B/node, FP32 pressure stencil of 32 B/node):
+#   operator (lattice half stencil 512 B + x, r1, q)                         560
+#   stage 1 (q, r1, r2 in; r_new, y out; velocity and pressure b, d_0, D^-1) 140
+#   stage 2 vectors (r_new in, y in and out)                                  48
+#   update of w and x (y, w_prev, w_cur, x in; w, x out)                      96
+#   finest velocity level, degree-1 smoothing: r = b - K d_0 (x = d_0) 192,
+#     restriction 18, prolongation 25.5, post residual + d_0 216, x + d_0 24  475.5
+#   finest pressure level, degree 1: 48, 6, 8.5, 52, 8                       122.5
+#   every coarser velocity level node, degree 2: pre-step 228, residual 180,
+#     restriction 18, prolongation 25.5, post residual + d_0 216, post-step 240  907.5
+#   every coarser pressure level node: 56, 44, 6, 8.5, 52, 60                 226.5
+ITERATION_BYTES = {"operator": 560.0, "stage1": 140.0, "stage2": 48.0, "update": 96.0,
+                   "velocity_finest": 475.5, "pressure_finest": 122.5,
+                   "velocity_level": 907.5, "pressure_level": 226.5}
 
 
 def iteration_bytes(n: int) -> float:
     """Algorithmic bytes of one mixed-precision MINRES iteration on an n^3
     lattice (velocity and pressure V-cycles over every level)."""
-    lv = 1.0 + hierarchy_fraction(n)
     B = ITERATION_BYTES
-    per = (B["operator"] + B["stage1"] + B["update"] +
-           lv * (B["velocity_level"] + B["pressure_level"]))
+    per = (B["operator"] + B["stage1"] + B["stage2"] + B["update"] + B["velocity_finest"] +
+           B["pressure_finest"] + hierarchy_fraction(n) * (B["velocity_level"] +
+                                                           B["pressure_level"]))
     return per * n ** 3
 
 
@@ -966,8 +971,8 @@ def run_p2(args):
     host buffers, beside the FP64 GPU path.  CPU baseline: the oracle's P2-P1
     assembly (the reference's element loop) in full plus its reduced system's
     sparse products, two per iteration of the reference's BiCGSTAB, times the
-    iterations the GPU's FP64 MINRES needs (a lower bound: the reference's
-    un-preconditioned BiCGSTAB needs more)."""
+    iterations block-Jacobi MINRES needs in FP64 (a lower bound: the
+    reference's un-preconditioned BiCGSTAB needs more)."""
     import torch
     from fluidtissue_gb300 import workloads as W
     from fluidtissue_gb300.flow import Flow, Mesh
@@ -1056,13 +1061,25 @@ def run_p2(args):
         for _ in range(reps):
             A @ x
         t_spmv = (time.perf_counter() - t0) / reps
-        its = d["st"]["iterations"]
+        # the iterations of a Krylov method the CPU has without a multigrid:
+        # FP64 MINRES with the block-Jacobi preconditioner (counted on the GPU)
+        from fluidtissue_gb300.flow import Flow, Mesh
+        fj = Flow()
+        if fj.init(Mesh(inst.xyz, inst.tets), par, precision="fp64", warm_start=False,
+                   preconditioner="jacobi", device=local) != 0:
+            raise RuntimeError(fj.last_error())
+        flow_j = np.zeros(4 * inst.np)
+        if fj.solve(inst.phi, inst.source, flow_j, mu=inst.mu) != 0:
+            raise RuntimeError(fj.last_error())
+        its = int(fj.last_stats["iterations"])
+        fj.close()
         t_cpu = t_asm + 2 * its * t_spmv
         line["cpu_baseline"] = {
             "value": 1.0 / t_cpu, "unit": "solves/s", "cores": 1, "kind": "port",
             "sample": (f"oracle P2-P1 assembly in full ({t_asm:.2f} s) + 2 x {its} sparse "
                        f"products of the reduced system ({t_spmv * 1e3:.1f} ms each, scipy, "
-                       f"1 thread): a lower bound for the reference's BiCGSTAB")}
+                       f"1 thread), {its} = the iterations of block-Jacobi MINRES in FP64: "
+                       f"a lower bound for the reference's un-preconditioned BiCGSTAB")}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
