@@ -175,17 +175,18 @@ def hierarchy_fraction(n: int) -> float:
 # kernel's stencil and vectors read once, outputs written once; FP32 vectors,
 # FP16 velocity stencil of 144 B/node, FP32 pressure stencil of 32 B/node):
 #   operator (lattice half stencil 512 B + x, r1, q)                         560
-#   stage 1 (q, r1, r2 in; r_new, y out; velocity and pressure b, d_0, D^-1) 140
-#   stage 2 vectors (r_new in, y in and out)                                  48
+#   stage 1 (q, r1, r2 in; r_new out; velocity and pressure b, d_0, D^-1)    124
+#   stage 2 vectors (r_new in, y out)                                         32
 #   update of w and x (y, w_prev, w_cur, x in; w, x out)                      96
-#   finest velocity level, degree-1 smoothing: r = b - K d_0 (x = d_0) 192,
-#     restriction 18, prolongation 25.5, post residual + d_0 216, x + d_0 24  475.5
-#   finest pressure level, degree 1: 48, 6, 8.5, 52, 8                       122.5
+#   finest velocity level, degree-1 smoothing: r = b - K d_0 180, restriction
+#     18, prolongation x = d_0 + P e 25.5, post d_0 = D^-1 (b - K x) 204,
+#     x + d_0 24                                                             451.5
+#   finest pressure level, degree 1: 44, 6, 8.5, 48, 8                       114.5
 #   every coarser velocity level node, degree 2: pre-step 228, residual 180,
 #     restriction 18, prolongation 25.5, post residual + d_0 216, post-step 240  907.5
 #   every coarser pressure level node: 56, 44, 6, 8.5, 52, 60                 226.5
-ITERATION_BYTES = {"operator": 560.0, "stage1": 140.0, "stage2": 48.0, "update": 96.0,
-                   "velocity_finest": 475.5, "pressure_finest": 122.5,
+ITERATION_BYTES = {"operator": 560.0, "stage1": 124.0, "stage2": 32.0, "update": 96.0,
+                   "velocity_finest": 451.5, "pressure_finest": 114.5,
                    "velocity_level": 907.5, "pressure_level": 226.5}
 
 

@@ -497,8 +497,8 @@ void launch_assemble_lat(Ctx& c) {
 // ---------------------------------------------------------------------------
 // Block-diagonal SPD preconditioner: inverse of the node's 3x3 velocity block
 // (identity on Dirichlet nodes) and, for pressure, the inverse of
-// (alpha D + eps M)_ii + sum_{e ni i} vol_e / (4 mu_e) (lumped 1/mu-weighted
-// mass, a Schur-complement estimate).  pc[8 i + 0..5] = xx xy xz yy yz zz,
+// (alpha D + eps M)_ii + kSchurScale sum_{e ni i} vol_e / (4 mu_e) (lumped
+// 1/mu-weighted mass, a Schur-complement estimate).  pc[8 i + 0..5] = xx xy xz yy yz zz,
 // pc[8 i + 6] = pressure weight.
 // ---------------------------------------------------------------------------
 // Diagonal block (i, i) of the BSR and of the FP64 lattice half stencil.
@@ -557,7 +557,7 @@ __global__ void k_preconditioner(int64_t np, Diag dg, const int32_t* __restrict_
             w += geom[k].vol / (4.0 * mu[k]);
         }
         // a node without pressure (P2 edge node: zero pressure row) gets weight 0
-        const double dp = -D[15] + w;
+        const double dp = -D[15] + kSchurScale * w;
         o[6] = dp != 0.0 ? 1.0 / dp : 0.0;
         o[7] = 0.0;
 #pragma unroll

@@ -181,13 +181,13 @@ __device__ bool batch_vcycle(const BInst<T>* __restrict__ inst, const BChunk* __
             const int mode = s == 1 ? kStepFromZero : kStepRegular;
             level_phase<T>(inst, chunks, S, d, [&](const BInst<T>&, const LevelView<T>& L, int64_t v) {
                 T xo[3];
-                mg_step_node<T, false>(L, v, s, mode, (s & 1) ? L.d0 : L.d1, (s & 1) ? L.d1 : L.d0, xo,
-                                true, true);
+                mg_step_node<T, kSkChecked>(L, v, s, mode, (s & 1) ? L.d0 : L.d1,
+                                            (s & 1) ? L.d1 : L.d0, xo, true, true);
             });
             if (!grid_barrier(bar)) return false;
         }
         level_phase<T>(inst, chunks, S, d, [&](const BInst<T>&, const LevelView<T>& L, int64_t v) {
-            mg_resid_node<T, false>(L, v);
+            mg_resid_node<T, kSkChecked>(L, v);
         });
         if (!grid_barrier(bar)) return false;
         // restriction onto level d + 1 (which may be an instance's coarsest)
@@ -206,7 +206,7 @@ __device__ bool batch_vcycle(const BInst<T>* __restrict__ inst, const BChunk* __
         const BInst<T>& I = inst[S.coarse[k]];
         if (I.s->stop) continue;
         const LevelView<T> L = I.lv[I.nlev - 1];
-        mg_coarse_block<T, false>(L, L.n == 3 ? 1 : kCoarse);
+        mg_coarse_block<T, kSkChecked>(L, L.n == 3 ? 1 : kCoarse);
     }
     if (!grid_barrier(bar)) return false;
     for (int d = D - 1; d >= 0; --d) {
@@ -215,7 +215,7 @@ __device__ bool batch_vcycle(const BInst<T>* __restrict__ inst, const BChunk* __
         });
         if (!grid_barrier(bar)) return false;
         level_phase<T>(inst, chunks, S, d, [&](const BInst<T>&, const LevelView<T>& L, int64_t v) {
-            mg_resid_first_node<T, false>(L, v);
+            mg_resid_first_node<T, kSkChecked>(L, v);
         });
         if (!grid_barrier(bar)) return false;
         const int last = d == 0 ? kSmooth - 2 : kSmooth - 1;
@@ -223,8 +223,8 @@ __device__ bool batch_vcycle(const BInst<T>* __restrict__ inst, const BChunk* __
             const int mode = s == 1 ? kStepAfterFirst : kStepRegular;
             level_phase<T>(inst, chunks, S, d, [&](const BInst<T>&, const LevelView<T>& L, int64_t v) {
                 T xo[3];
-                mg_step_node<T, false>(L, v, s, mode, (s & 1) ? L.d0 : L.d1, (s & 1) ? L.d1 : L.d0, xo,
-                                true, true);
+                mg_step_node<T, kSkChecked>(L, v, s, mode, (s & 1) ? L.d0 : L.d1,
+                                            (s & 1) ? L.d1 : L.d0, xo, true, true);
             });
             if (!grid_barrier(bar)) return false;
         }
@@ -250,7 +250,8 @@ __device__ void batch_pc2(const BInst<T>* __restrict__ inst, int nchunks,
         double acc[1] = {0.0};
         for (int64_t i = C.row0 + threadIdx.x; i < C.row1; i += blockDim.x) {
             T xo[3];
-            mg_step_node<T, false>(L, i, s, mode, (s & 1) ? L.d0 : L.d1, nullptr, xo, false, false);
+            mg_step_node<T, kSkChecked>(L, i, s, mode, (s & 1) ? L.d0 : L.d1, nullptr, xo, false,
+                                        false);
             const V4<T> n = Rn[i];
             V4<T> z = Yn[i];
             z.x = xo[0];

@@ -38,6 +38,15 @@ struct CudaError {
 constexpr int kThreads = 256;
 constexpr int kMaxPartials = 4096;
 
+// Scale of the lumped 1/mu-weighted pressure mass sum_e vol_e / (4 mu_e) in
+// every Schur-complement estimate of the preconditioner (pressure weights and
+// the pressure multigrid's fine operator).  The viscous term is
+// 2 mu eps(u) : eps(v), so B K^-1 B^T is about M / (2 mu): scale 1/2.
+#ifndef FTS_SCHUR_SCALE
+#define FTS_SCHUR_SCALE 0.5
+#endif
+constexpr double kSchurScale = FTS_SCHUR_SCALE;
+
 // Node-interleaved vector element: (ux, uy, uz, p).
 template <typename T>
 struct alignas(4 * sizeof(T)) V4 {

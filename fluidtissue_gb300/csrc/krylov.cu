@@ -559,9 +559,12 @@ k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
             pc_jacobi<T>(pc, i, n, z);
             acc[2] += (double)(n.x * z.x + n.y * z.y + n.z * z.z);
         }
-        Ynew[i] = z;
+        // with both V-cycles stage 2 writes all of y: nothing to store here
+        if (!(MGV && pmg)) {
+            Ynew[i] = z;
+            acc[1] += (double)(n.w * z.w);
+        }
         acc[0] += (double)n.w;
-        acc[1] += (double)(n.w * z.w);
     }
     double tot[3];
     if (grid_sum<3>(acc, red, tot) && threadIdx.x == 0) {
@@ -581,15 +584,22 @@ k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
 // pmg y.w likewise from the pressure V-cycle; beta.  With degree-1 smoothing on
 // a finest level (fine1 / pfine1) that step is the pointwise x + d_0.  (Running
 // the pressure V-cycle's last step on its own stream instead, and reading its x
-// here, gave no gain: the pressure stream then ends after the velocity one.)  (Running the pressure
-// V-cycle's last step on its own stream instead, and reading its x here, made
-// the solve slower: 224.7 -> 226.2 ms on ellipsoid129, the pressure stream
-// then ends after the velocity one.)
-template <typename T>
-__global__ void __launch_bounds__(kThreads)
+// here, made the solve slower: 224.7 -> 226.2 ms on ellipsoid129, the pressure
+// stream then ends after the velocity one.)  FORM: how y.xyz is formed —
+// kPc2Step the fused last Chebyshev step; kPc2Fine1 the pointwise x + d_0;
+// kPc2Post the velocity V-cycle left out its degree-1 finest post-smoothing
+// residual (kSkipPost), which runs here from the prolongated x:
+// y.xyz = x + D^-1 (b - K x) / theta, nothing stored but y.  PFORM: y.w from
+// stage 1's pressure diagonal (kPc2None), the pressure V-cycle's pointwise
+// x + d_0 (kPc2Fine1) or its fused last step (kPc2Step).  Each form is its own
+// kernel so that the pointwise ones keep few registers (one kernel for all
+// held 168 registers and a quarter of the warps).
+enum : int { kPc2Step = 0, kPc2Fine1 = 1, kPc2Post = 2, kPc2None = 3 };
+template <typename T, int FORM, int PFORM>
+__global__ void __launch_bounds__(kThreads, 4)
 k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, PView<T> P0,
-             int pmg, int init, const V4<T>* __restrict__ Rn, V4<T>* __restrict__ Ynew,
-             int ybuf, int fine1, int pfine1, Reduction red, MinresScalars* s) {
+             int init, const V4<T>* __restrict__ Rn, V4<T>* __restrict__ Ynew, int ybuf,
+             Reduction red, MinresScalars* s) {
     pdl_wait();
     if (s->stop) return;
     double acc[1] = {0.0};
@@ -600,7 +610,9 @@ k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, PVi
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L0.N;
          i += (int64_t)gridDim.x * blockDim.x) {
         T xo[3];
-        if (fine1) {  // degree-1 finest level: x + d_0
+        if (FORM == kPc2Post) {
+            mg_post1_node<T>(L0, i, xo);
+        } else if (FORM == kPc2Fine1) {  // degree-1 finest level: x + d_0
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) xo[cc] = L0.x[cc * L0.N + i] + L0.d0[cc * L0.N + i];
         } else {
@@ -612,9 +624,9 @@ k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, PVi
         z.y = xo[1];
         z.z = xo[2];
         T dz = n.x * z.x + n.y * z.y + n.z * z.z;  // node sum in T, FP64 across nodes
-        if (pmg) {
-            z.w = pfine1 ? P0.x[i] + P0.d0[i]
-                         : pmg_step_node<T>(P0, i, ps, pmode, pdin, nullptr, false);
+        if (PFORM != kPc2None) {
+            z.w = PFORM == kPc2Fine1 ? P0.x[i] + P0.d0[i]
+                                     : pmg_step_node<T>(P0, i, ps, pmode, pdin, nullptr, false);
             dz += n.w * z.w;
         } else {
             z.w = Ynew[i].w;  // stage 1's pressure diagonal (its dot is in pdot)
@@ -628,6 +640,23 @@ k_minres_pc2(LevelView<T> L0, int step, int mode, const T* __restrict__ din, PVi
         s->ycorr[ybuf] = cr * s->psum;
         finalize_beta(s, tot[0] + s->pdot + cr * s->psum * s->psum, init != 0);
     }
+}
+
+template <typename T>
+using Pc2Kernel = void (*)(LevelView<T>, int, int, const T*, PView<T>, int, const V4<T>*,
+                           V4<T>*, int, Reduction, MinresScalars*);
+
+// The stage-2 kernel of a velocity form and a pressure form.
+template <typename T>
+static Pc2Kernel<T> pc2_kernel(int form, int pform) {
+    static const Pc2Kernel<T> table[3][4] = {
+        {k_minres_pc2<T, kPc2Step, kPc2Step>, k_minres_pc2<T, kPc2Step, kPc2Fine1>, nullptr,
+         k_minres_pc2<T, kPc2Step, kPc2None>},
+        {k_minres_pc2<T, kPc2Fine1, kPc2Step>, k_minres_pc2<T, kPc2Fine1, kPc2Fine1>, nullptr,
+         k_minres_pc2<T, kPc2Fine1, kPc2None>},
+        {k_minres_pc2<T, kPc2Post, kPc2Step>, k_minres_pc2<T, kPc2Post, kPc2Fine1>, nullptr,
+         k_minres_pc2<T, kPc2Post, kPc2None>}};
+    return table[form][pform];
 }
 
 // C: w_new = (v - oldeps w_prev - delta w_cur) / gamma (into w_prev), x += phi w_new.
@@ -717,15 +746,19 @@ static void launch_pc(Ctx& c, bool use_mg, int init, const V4<T>* q, V4<T>* R1, 
             pmg_vcycle<T>(c, pmg_of<T>(c), c.aux_stream, &c.ms->stop, true);
             FTS_CUDA(cudaEventRecord(c.ev_join, c.aux_stream));
         }
+        // a degree-1 finest velocity level's post-smoothing residual runs in stage 2
+        const bool post = !c.p2 && mg_level_degree1(mg, 0);
         if (c.p2) p2mg_vcycle<T>(c, &c.ms->stop);
-        else mg_vcycle<T>(c, mg, &c.ms->stop, true);
+        else mg_vcycle<T>(c, mg, &c.ms->stop, post ? kSkipPost : kSkipFinal);
         if (pmg) FTS_CUDA(cudaStreamWaitEvent(c.stream, c.ev_join, 0));
         // the last post-smoothing step: step kSmooth - 1 reads d0 when it is odd
         constexpr int s = kSmooth - 1;
-        pdl_launch(k_minres_pc2<T>, gn, kThreads, c.stream,
+        const int form = post ? kPc2Post : (fine1 ? kPc2Fine1 : kPc2Step);
+        const int pform =
+            !pmg ? kPc2None : (pmg_level_degree1(pmg_of<T>(c), 0) ? kPc2Fine1 : kPc2Step);
+        pdl_launch(pc2_kernel<T>(form, pform), gn, kThreads, c.stream,
             L0, s, s == 1 ? kStepAfterFirst : kStepRegular, (s & 1) ? L0.d0 : L0.d1, P0,
-            pmg ? 1 : 0, init, Rn, Ynew, ybuf, fine1 ? 1 : 0,
-            pmg && pmg_level_degree1(pmg_of<T>(c), 0) ? 1 : 0, c.red, c.ms);
+            init, Rn, Ynew, ybuf, c.red, c.ms);
         c.launches += 2;
     } else {
         pdl_launch(k_minres_pc1<T, false>, gn, kThreads, c.stream, c.np, init, q, R1, R2, Rn, pc, Ynew,

@@ -470,7 +470,7 @@ k_mf_residual64(int64_t np, const int32_t* __restrict__ p2t_ptr, const uint32_t*
 }
 
 // Pressure weight of the preconditioner per node (the velocity part is the
-// multigrid V-cycle): 1 / (alpha D_ii + eps M_ii + sum_e vol/(4 mu_e)).
+// multigrid V-cycle): 1 / (alpha D_ii + eps M_ii + kSchurScale sum_e vol/(4 mu_e)).
 __global__ void k_mf_pc(int64_t np, const int32_t* __restrict__ p2t_ptr,
                         const uint32_t* __restrict__ p2t, const ElemGeom* __restrict__ geom,
                         const double* __restrict__ mu, double alpha, double eps, MfConst K,
@@ -484,7 +484,8 @@ __global__ void k_mf_pc(int64_t np, const int32_t* __restrict__ p2t_ptr,
             const int a = e & 3;
             const ElemGeom& G = geom[k];
             const double gg = G.g[a][0] * G.g[a][0] + G.g[a][1] * G.g[a][1] + G.g[a][2] * G.g[a][2];
-            d += alpha * G.hh * G.vol * gg + eps * G.vol * K.mrefd[a][a] + G.vol / (4.0 * mu[k]);
+            d += alpha * G.hh * G.vol * gg + eps * G.vol * K.mrefd[a][a] +
+                 kSchurScale * (G.vol / (4.0 * mu[k]));
         }
         float* o = pc + 8 * v;
         o[0] = 1.f;

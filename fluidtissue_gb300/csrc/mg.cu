@@ -391,7 +391,16 @@ void cheb_table(double lam, double* out) {
     }
 }
 
-template <typename T>
+// Levels of at most kClampNodes nodes (65^3 and below) run the clamped
+// (branch-free) stencil body in their full-GPU kernels, the larger ones the
+// split body: on those latency-bound levels a warp almost always holds a
+// boundary node, and the split body then runs both bodies.
+#ifndef FTS_MG_CLAMP_NODES
+#define FTS_MG_CLAMP_NODES 300000
+#endif
+constexpr int64_t kClampNodes = FTS_MG_CLAMP_NODES;
+
+template <typename T, int SK>
 __global__ void __launch_bounds__(kThreads, 4)
 k_mg_step(LevelView<T> L, int step, int mode, const T* __restrict__ din, T* __restrict__ dout,
           const int* __restrict__ stop) {
@@ -400,27 +409,27 @@ k_mg_step(LevelView<T> L, int step, int mode, const T* __restrict__ din, T* __re
     T xo[3];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.N;
          i += (int64_t)gridDim.x * blockDim.x)
-        mg_step_node<T>(L, i, step, mode, din, dout, xo, true, true);
+        mg_step_node<T, SK>(L, i, step, mode, din, dout, xo, true, true);
 }
 
-template <typename T>
+template <typename T, int SK>
 __global__ void __launch_bounds__(kThreads, 4)
 k_mg_residual(LevelView<T> L, const int* __restrict__ stop) {
     pdl_wait();
     if (stop && *stop) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.N;
          i += (int64_t)gridDim.x * blockDim.x)
-        mg_resid_node<T>(L, i);
+        mg_resid_node<T, SK>(L, i);
 }
 
-template <typename T>
+template <typename T, int SK, bool WR = true>
 __global__ void __launch_bounds__(kThreads, 4)
 k_mg_resid_first(LevelView<T> L, const int* __restrict__ stop) {
     pdl_wait();
     if (stop && *stop) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.N;
          i += (int64_t)gridDim.x * blockDim.x)
-        mg_resid_first_node<T>(L, i);
+        mg_resid_first_node<T, SK, WR>(L, i);
 }
 
 template <typename T>
@@ -452,13 +461,13 @@ __global__ void k_mg_restrict(LevelView<T> F, LevelView<T> C, const int* __restr
         mg_restrict_node<T>(F, C, I);
 }
 
-template <typename T>
+template <typename T, bool FROM_D0 = false>
 __global__ void k_mg_prolong(LevelView<T> F, LevelView<T> C, const int* __restrict__ stop) {
     pdl_wait();
     if (stop && *stop) return;
     for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < F.N;
          f += (int64_t)gridDim.x * blockDim.x)
-        mg_prolong_node<T>(F, C, f);
+        mg_prolong_node<T, FROM_D0>(F, C, f);
 }
 
 template <typename T>
@@ -478,6 +487,12 @@ k_mg_coarse_solve(LevelView<T> L, int steps, const int* __restrict__ stop) {
 // corrected x is the result.  skip_final (l0 == 0) leaves the last
 // post-smoothing step of the finest level to the caller.
 constexpr int kTailThreads = 512;
+// Stencil body of the tail's levels: the clamped one, since nearly every warp
+// of a small lattice holds a boundary node.
+#ifndef FTS_TAIL_SK
+#define FTS_TAIL_SK kSkClamped
+#endif
+constexpr int kTailSk = FTS_TAIL_SK;
 
 template <typename T>
 struct MGTailArgs {
@@ -500,11 +515,11 @@ k_mg_tail(const __grid_constant__ MGTailArgs<T> a, const int* __restrict__ stop)
         for (int s = 1; s < kSmooth; ++s) {
             const int mode = s == 1 ? kStepFromZero : kStepRegular;
             for (int64_t v = tid; v < L.N; v += nth)
-                mg_step_node<T>(L, v, s, mode, (s & 1) ? L.d0 : L.d1, (s & 1) ? L.d1 : L.d0, xo,
-                                true, true);
+                mg_step_node<T, kTailSk>(L, v, s, mode, (s & 1) ? L.d0 : L.d1,
+                                            (s & 1) ? L.d1 : L.d0, xo, true, true);
             cl.sync();
         }
-        for (int64_t v = tid; v < L.N; v += nth) mg_resid_node<T>(L, v);
+        for (int64_t v = tid; v < L.N; v += nth) mg_resid_node<T, kTailSk>(L, v);
         cl.sync();
         const LevelView<T> C = a.lv[l + 1];
         for (int64_t v = tid; v < C.N; v += nth) mg_restrict_node<T>(L, C, v);
@@ -512,21 +527,21 @@ k_mg_tail(const __grid_constant__ MGTailArgs<T> a, const int* __restrict__ stop)
     }
     if (cl.block_rank() == 0) {
         const LevelView<T> L = a.lv[a.nlev - 1];
-        mg_coarse_block<T>(L, L.n == 3 ? 1 : kCoarse);
+        mg_coarse_block<T, kTailSk>(L, L.n == 3 ? 1 : kCoarse);
     }
     cl.sync();
     for (int l = a.nlev - 2; l >= a.l0; --l) {
         const LevelView<T> L = a.lv[l], C = a.lv[l + 1];
         for (int64_t v = tid; v < L.N; v += nth) mg_prolong_node<T>(L, C, v);
         cl.sync();
-        for (int64_t v = tid; v < L.N; v += nth) mg_resid_first_node<T>(L, v);
+        for (int64_t v = tid; v < L.N; v += nth) mg_resid_first_node<T, kTailSk>(L, v);
         cl.sync();
         const int last = (l == 0 && a.skip_final) ? kSmooth - 2 : kSmooth - 1;
         for (int s = 1; s <= last; ++s) {
             const int mode = s == 1 ? kStepAfterFirst : kStepRegular;
             for (int64_t v = tid; v < L.N; v += nth)
-                mg_step_node<T>(L, v, s, mode, (s & 1) ? L.d0 : L.d1, (s & 1) ? L.d1 : L.d0, xo,
-                                true, true);
+                mg_step_node<T, kTailSk>(L, v, s, mode, (s & 1) ? L.d0 : L.d1,
+                                            (s & 1) ? L.d1 : L.d0, xo, true, true);
             cl.sync();
         }
     }
@@ -699,7 +714,7 @@ void mg_setup(Ctx& c, MG<T>& mg) {
 
 // One level of the V-cycle; L.d0 holds the first Chebyshev direction of L.b.
 template <typename T>
-static void vcycle_level(Ctx& c, MG<T>& mg, size_t l, const int* stop, bool skip_final) {
+static void vcycle_level(Ctx& c, MG<T>& mg, size_t l, const int* stop, int skip_final) {
     const LevelView<T> L = level_view(mg, l);
     const int g = grid_for(c, L.N);
     if ((int)l == mg.tail_level) {
@@ -733,48 +748,55 @@ static void vcycle_level(Ctx& c, MG<T>& mg, size_t l, const int* stop, bool skip
     const LevelView<T> C = level_view(mg, l + 1);
     if (mg_level_degree1(mg, l)) {
         // degree 1: x = d_0, r = b - K d_0; after the coarse correction
-        // r = b - K x, d_0 = D^-1 r / theta, x += d_0 (the caller's when skip_final)
+        // x = d_0 + P e, r = b - K x (not stored), d_0 = D^-1 r / theta,
+        // x += d_0 (the caller's when skip_final)
         pdl_launch(k_mg_resid_d0<T>, g, kThreads, c.stream, L, stop);
-        k_mg_restrict<T><<<grid_for(c, C.N), kThreads, 0, c.stream>>>(L, C, stop);
-        vcycle_level<T>(c, mg, l + 1, stop, false);
-        pdl_launch(k_mg_prolong<T>, g, kThreads, c.stream, L, C, stop);
-        pdl_launch(k_mg_resid_first<T>, g, kThreads, c.stream, L, stop);
-        c.launches += 4;
+        pdl_launch(k_mg_restrict<T>, grid_for(c, C.N), kThreads, c.stream, L, C, stop);
+        vcycle_level<T>(c, mg, l + 1, stop, 0);
+        pdl_launch(k_mg_prolong<T, true>, g, kThreads, c.stream, L, C, stop);
+        c.launches += 3;
+        if (skip_final == kSkipPost) return;  // the caller's stage 2 runs the residual
+        pdl_launch(k_mg_resid_first<T, kSkSplit, false>, g, kThreads, c.stream, L, stop);
+        c.launches += 1;
         if (!skip_final) {
             pdl_launch(k_mg_add_d0<T>, grid_for(c, 3 * L.N), kThreads, c.stream, L, stop);
             c.launches += 1;
         }
         return;
     }
+    const bool clamp = L.N <= kClampNodes;
+    auto step_kernel = clamp ? k_mg_step<T, kSkClamped> : k_mg_step<T, kSkSplit>;
     // pre-smoothing from zero (d_0 is already in L.d0)
     T* din = L.d0;
     T* dout = L.d1;
     for (int s = 1; s < kSmooth; ++s) {
-        pdl_launch(k_mg_step<T>, g, kThreads, c.stream, L, s, s == 1 ? kStepFromZero : kStepRegular,
-                                                   din, dout, stop);
+        pdl_launch(step_kernel, g, kThreads, c.stream, L, s, s == 1 ? kStepFromZero : kStepRegular, din,
+                   dout, stop);
         std::swap(din, dout);
     }
-    pdl_launch(k_mg_residual<T>, g, kThreads, c.stream, L, stop);
-    k_mg_restrict<T><<<grid_for(c, C.N), kThreads, 0, c.stream>>>(L, C, stop);
+    pdl_launch(clamp ? k_mg_residual<T, kSkClamped> : k_mg_residual<T, kSkSplit>, g, kThreads,
+               c.stream, L, stop);
+    pdl_launch(k_mg_restrict<T>, grid_for(c, C.N), kThreads, c.stream, L, C, stop);
     c.launches += kSmooth + 1;
-    vcycle_level<T>(c, mg, l + 1, stop, false);
+    vcycle_level<T>(c, mg, l + 1, stop, 0);
     pdl_launch(k_mg_prolong<T>, g, kThreads, c.stream, L, C, stop);
     // post-smoothing from the corrected x
-    pdl_launch(k_mg_resid_first<T>, g, kThreads, c.stream, L, stop);
+    pdl_launch(clamp ? k_mg_resid_first<T, kSkClamped> : k_mg_resid_first<T, kSkSplit>, g,
+               kThreads, c.stream, L, stop);
     c.launches += 2;
     din = L.d0;
     dout = L.d1;
     for (int s = 1; s < kSmooth; ++s) {
         if (skip_final && s == kSmooth - 1) break;
-        pdl_launch(k_mg_step<T>, g, kThreads, c.stream, L, s, s == 1 ? kStepAfterFirst : kStepRegular,
-                                                   din, dout, stop);
+        pdl_launch(step_kernel, g, kThreads, c.stream, L, s, s == 1 ? kStepAfterFirst : kStepRegular, din,
+                   dout, stop);
         std::swap(din, dout);
         c.launches += 1;
     }
 }
 
 template <typename T>
-void mg_vcycle(Ctx& c, MG<T>& mg, const int* stop, bool skip_final) {
+void mg_vcycle(Ctx& c, MG<T>& mg, const int* stop, int skip_final) {
     vcycle_level<T>(c, mg, 0, stop, skip_final);
     FTS_CUDA(cudaGetLastError());
 }
@@ -800,8 +822,8 @@ void mg_free(MG<T>& mg) {
 
 template void mg_setup<double>(Ctx&, MG<double>&);
 template void mg_setup<float>(Ctx&, MG<float>&);
-template void mg_vcycle<double>(Ctx&, MG<double>&, const int*, bool);
-template void mg_vcycle<float>(Ctx&, MG<float>&, const int*, bool);
+template void mg_vcycle<double>(Ctx&, MG<double>&, const int*, int);
+template void mg_vcycle<float>(Ctx&, MG<float>&, const int*, int);
 template void mg_free<double>(MG<double>&);
 template void mg_free<float>(MG<float>&);
 

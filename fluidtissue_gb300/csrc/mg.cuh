@@ -15,7 +15,10 @@ constexpr int kSmooth = 2;        // Chebyshev degree of each pre / post smoothi
 // degree 1 instead of kSmooth: damped Jacobi with the level's 1/theta, one
 // stencil pass before and one after the coarse correction instead of two; on
 // the finest level the caller's final update is then pointwise.
-constexpr int kDeg1Levels = 1;
+#ifndef FTS_DEG1_LEVELS
+#define FTS_DEG1_LEVELS 1
+#endif
+constexpr int kDeg1Levels = FTS_DEG1_LEVELS;
 constexpr int kCoarse = 20;       // Chebyshev degree of the coarsest-level solve
 constexpr int kPowerIters = 12;   // power iterations for lambda_max(D^-1 K)
 constexpr double kLamSafety = 1.1;
@@ -106,10 +109,15 @@ void galerkin_terms(std::vector<int>& start, std::vector<unsigned short>& term,
 template <typename T>
 void mg_setup(Ctx& c, MG<T>& mg);
 // V-cycle on mg.L[0].b, whose first Chebyshev direction L[0].d0 the caller has
-// written.  skip_final leaves out the last post-smoothing step of the finest
-// level, which the caller then runs fused with its own epilogue.
+// written.  skip_final: 0 runs the whole cycle; kSkipFinal leaves out the last
+// post-smoothing step of the finest level (on a degree-1 finest level the
+// update x + d_0), which the caller then runs fused with its own epilogue;
+// kSkipPost on a degree-1 finest level also leaves out the post-smoothing
+// residual (b - K x and its d_0), so the caller's epilogue starts from the
+// prolongated x (elsewhere it acts as kSkipFinal).
+enum : int { kSkipFinal = 1, kSkipPost = 2 };
 template <typename T>
-void mg_vcycle(Ctx& c, MG<T>& mg, const int* stop, bool skip_final);
+void mg_vcycle(Ctx& c, MG<T>& mg, const int* stop, int skip_final);
 template <typename T>
 void mg_free(MG<T>& mg);
 

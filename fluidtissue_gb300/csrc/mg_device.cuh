@@ -140,21 +140,48 @@ __device__ __forceinline__ float half_at(const uint4& u, int k) {
     return __half2float(reinterpret_cast<const __half*>(&u)[k]);
 }
 
+// How a stencil body treats the lattice boundary.
+enum : int {
+    kSkChecked = 0,  // one body: a range check and a branch per neighbour
+    kSkSplit = 1,    // interior nodes take a check-free body, the others the checked one
+    kSkClamped = 2   // one branch-free body: a missing neighbour's loads go to the
+                     // node itself and are weighted 0, so every load of the node
+                     // can issue before the first use (latency-bound levels, where
+                     // nearly every warp holds a boundary node)
+};
+// Per-node stencil bodies: the check-free interior one, the checked one and
+// the clamped one.
+enum : int { kBodyChecked = 0, kBodyInner = 1, kBodyClamped = 2 };
+
+// Neighbour w of node v towards direction d for body B; m = 0 marks a
+// missing neighbour of the clamped body (w is then v itself).
+template <int B>
+__device__ __forceinline__ int stencil_nbr(int n, int v, int i, int j, int k, int d, float& m) {
+    m = 1.f;
+    if (B == kBodyInner) return v + off_x(d) + n * off_y(d) + n * n * off_z(d);
+    const int w = nbr(i, j, k, d, n);
+    if (B == kBodyClamped && w < 0) {
+        m = 0.f;
+        return v;
+    }
+    return w;
+}
+
 // y = K x at node v from the FP16 layout (without the level's scale).
-// INNER: all 14 neighbours exist (no range checks, so the compiler can issue
-// every load of the node before the first use).
-template <bool INNER>
+// Inner body: all 14 neighbours exist (no range checks, so the compiler can
+// issue every load of the node before the first use).
+template <int B>
 __device__ __forceinline__ void stencil_h_body(int n, int64_t N, int v, int i, int j, int k,
                                                const uint4* __restrict__ K,
                                                const float* __restrict__ x, float y[3]) {
-    const int nn = n * n;
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;
     const uint4 e8 = __ldg(K + hidx(8, v));
 #pragma unroll
     for (int d = 0; d < 8; ++d) {  // self and positive directions: own blocks
-        const int w = INNER ? v + off_x(d) + n * off_y(d) + nn * off_z(d) : nbr(i, j, k, d, n);
-        if (!INNER && w < 0) continue;
-        const float x0 = x[w], x1 = x[N + w], x2 = x[2 * N + w];
+        float m;
+        const int w = stencil_nbr<B>(n, v, i, j, k, d, m);
+        if (B == kBodyChecked && w < 0) continue;
+        const float x0 = x[w] * m, x1 = x[N + w] * m, x2 = x[2 * N + w] * m;
         float f[8];
         unpack8(__ldg(K + hidx(d, v)), f);
         const float f8 = half_at(e8, d);
@@ -162,11 +189,15 @@ __device__ __forceinline__ void stencil_h_body(int n, int64_t N, int v, int i, i
         a1 = fmaf(f[3], x0, fmaf(f[4], x1, fmaf(f[5], x2, a1)));
         a2 = fmaf(f[6], x0, fmaf(f[7], x1, fmaf(f8, x2, a2)));
     }
+#ifdef FTS_CLAMP_TWO_ROUNDS
+    if (B == kBodyClamped) asm volatile("" ::: "memory");
+#endif
 #pragma unroll
     for (int d = 1; d < 8; ++d) {  // negative directions: neighbour's block, transposed
-        const int w = INNER ? v - off_x(d) - n * off_y(d) - nn * off_z(d) : nbr(i, j, k, d + 7, n);
-        if (!INNER && w < 0) continue;
-        const float x0 = x[w], x1 = x[N + w], x2 = x[2 * N + w];
+        float m;
+        const int w = stencil_nbr<B>(n, v, i, j, k, d + 7, m);
+        if (B == kBodyChecked && w < 0) continue;
+        const float x0 = x[w] * m, x1 = x[N + w] * m, x2 = x[2 * N + w] * m;
         float f[8];
         unpack8(__ldg(K + hidx(d, (int64_t)w)), f);
         const float f8 = half_at(__ldg(K + hidx(8, (int64_t)w)), d);
@@ -179,10 +210,10 @@ __device__ __forceinline__ void stencil_h_body(int n, int64_t N, int v, int i, i
     y[2] = a2;
 }
 
-// SPLIT: a separate branch-free body for interior nodes (more registers; the
-// persistent batched kernel, which holds every phase in one function, keeps
-// the single checked body).
-template <bool SPLIT>
+// SK (kSk*): the split form has a separate check-free body for interior nodes
+// (more registers; the persistent batched kernel, which holds every phase in
+// one function, keeps the single checked body).
+template <int SK>
 __device__ __forceinline__ void stencil_apply_h(int n, int64_t N, int64_t v64,
                                                 const uint4* __restrict__ K,
                                                 const float* __restrict__ x, float y[3]) {
@@ -192,21 +223,23 @@ __device__ __forceinline__ void stencil_apply_h(int n, int64_t N, int64_t v64,
     const int rem = v - k * nn;
     const int j = rem / n;
     const int i = rem - j * n;
-    if (SPLIT && i > 0 && j > 0 && k > 0 && i < n - 1 && j < n - 1 && k < n - 1)
-        stencil_h_body<true>(n, N, v, i, j, k, K, x, y);
+    if (SK == kSkClamped)
+        stencil_h_body<kBodyClamped>(n, N, v, i, j, k, K, x, y);
+    else if (SK == kSkSplit && i > 0 && j > 0 && k > 0 && i < n - 1 && j < n - 1 && k < n - 1)
+        stencil_h_body<kBodyInner>(n, N, v, i, j, k, K, x, y);
     else
-        stencil_h_body<false>(n, N, v, i, j, k, K, x, y);
+        stencil_h_body<kBodyChecked>(n, N, v, i, j, k, K, x, y);
 }
 
 // y = K x at node v (3 components, without the level's scale); x SoA [3][N].
 // 32-bit lattice coordinates; interior nodes take the neighbour offsets
 // without range checks.
-template <typename T, typename KS, bool SPLIT = true>
+template <typename T, typename KS, int SK = kSkSplit>
 __device__ __forceinline__ void stencil_apply(int n, int64_t N, int64_t v64,
                                               const KS* __restrict__ K,
                                               const T* __restrict__ x, T y[3]) {
     if constexpr (std::is_same<KS, __half>::value) {
-        stencil_apply_h<SPLIT>(n, N, v64, reinterpret_cast<const uint4*>(K), x, y);
+        stencil_apply_h<SK>(n, N, v64, reinterpret_cast<const uint4*>(K), x, y);
         return;
     }
     const int v = (int)v64;
@@ -215,13 +248,19 @@ __device__ __forceinline__ void stencil_apply(int n, int64_t N, int64_t v64,
     const int rem = v - k * nn;
     const int j = rem / n;
     const int i = rem - j * n;
-    const bool inner = i > 0 && j > 0 && k > 0 && i < n - 1 && j < n - 1 && k < n - 1;
+    const bool inner = SK != kSkClamped && i > 0 && j > 0 && k > 0 && i < n - 1 && j < n - 1 &&
+                       k < n - 1;
     T a0 = T(0), a1 = T(0), a2 = T(0);
 #pragma unroll
     for (int d = 0; d < 8; ++d) {  // self and positive directions: own blocks
-        const int w = inner ? v + off_x(d) + n * off_y(d) + nn * off_z(d) : nbr(i, j, k, d, n);
+        int w = inner ? v + off_x(d) + n * off_y(d) + nn * off_z(d) : nbr(i, j, k, d, n);
+        T m = T(1);
+        if (SK == kSkClamped && w < 0) {
+            w = v;
+            m = T(0);
+        }
         if (w < 0) continue;
-        const T x0 = x[w], x1 = x[N + w], x2 = x[2 * N + w];
+        const T x0 = x[w] * m, x1 = x[N + w] * m, x2 = x[2 * N + w] * m;
         const KS* kb = K + kidx(d * 9, v64);
         a0 = fma(ldk<T>(kb), x0, fma(ldk<T>(kb + 32), x1, fma(ldk<T>(kb + 64), x2, a0)));
         a1 = fma(ldk<T>(kb + 96), x0, fma(ldk<T>(kb + 128), x1, fma(ldk<T>(kb + 160), x2, a1)));
@@ -229,9 +268,14 @@ __device__ __forceinline__ void stencil_apply(int n, int64_t N, int64_t v64,
     }
 #pragma unroll
     for (int d = 1; d < 8; ++d) {  // negative directions: neighbour's block, transposed
-        const int w = inner ? v - off_x(d) - n * off_y(d) - nn * off_z(d) : nbr(i, j, k, d + 7, n);
+        int w = inner ? v - off_x(d) - n * off_y(d) - nn * off_z(d) : nbr(i, j, k, d + 7, n);
+        T m = T(1);
+        if (SK == kSkClamped && w < 0) {
+            w = v;
+            m = T(0);
+        }
         if (w < 0) continue;
-        const T x0 = x[w], x1 = x[N + w], x2 = x[2 * N + w];
+        const T x0 = x[w] * m, x1 = x[N + w] * m, x2 = x[2 * N + w] * m;
         const KS* kb = K + kidx(d * 9, (int64_t)w);
         a0 = fma(ldk<T>(kb), x0, fma(ldk<T>(kb + 96), x1, fma(ldk<T>(kb + 192), x2, a0)));
         a1 = fma(ldk<T>(kb + 32), x0, fma(ldk<T>(kb + 128), x1, fma(ldk<T>(kb + 224), x2, a1)));
@@ -241,6 +285,10 @@ __device__ __forceinline__ void stencil_apply(int n, int64_t N, int64_t v64,
     y[1] = a1;
     y[2] = a2;
 }
+
+// A product rounded on its own (never contracted into a following add).
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 
 template <typename T>
 __device__ __forceinline__ void dinv_apply(int64_t N, int64_t v, const T* __restrict__ Di,
@@ -272,7 +320,7 @@ enum : int {
 
 // Chebyshev step s >= 1 at node v.  Returns the new x value (3 components),
 // written to L.x unless `out` is non-null (the fused caller writes it).
-template <typename T, bool SPLIT = true>
+template <typename T, int SK = kSkSplit>
 __device__ __forceinline__ void mg_step_node(const LevelView<T>& L, int64_t v, int step, int mode,
                                              const T* __restrict__ din, T* __restrict__ dout,
                                              T xo[3], bool write_x, bool write_rd) {
@@ -280,7 +328,7 @@ __device__ __forceinline__ void mg_step_node(const LevelView<T>& L, int64_t v, i
     const T A = (T)L.coef[2 * step - 1], B = (T)L.coef[2 * step];
     const T ks = (T)*L.ks;
     T y[3], rr[3], z[3];
-    stencil_apply<T, typename MGStore<T>::type, SPLIT>(L.n, N, v, L.K, din, y);
+    stencil_apply<T, typename MGStore<T>::type, SK>(L.n, N, v, L.K, din, y);
     const T* rin = mode == kStepFromZero ? L.b : L.r;
 #pragma unroll
     for (int c = 0; c < 3; ++c) rr[c] = rin[c * N + v] - ks * y[c];
@@ -303,48 +351,67 @@ __device__ __forceinline__ void mg_step_node(const LevelView<T>& L, int64_t v, i
 }
 
 // r = b - K x at node v.
-template <typename T, bool SPLIT = true>
+template <typename T, int SK = kSkSplit>
 __device__ __forceinline__ void mg_resid_node(const LevelView<T>& L, int64_t v) {
     const int64_t N = L.N;
     const T ks = (T)*L.ks;
     T y[3];
-    stencil_apply<T, typename MGStore<T>::type, SPLIT>(L.n, N, v, L.K, L.x, y);
+    stencil_apply<T, typename MGStore<T>::type, SK>(L.n, N, v, L.K, L.x, y);
 #pragma unroll
     for (int c = 0; c < 3; ++c) L.r[c * N + v] = L.b[c * N + v] - ks * y[c];
 }
 
-// Degree-1 pre-smoothing from zero: x = d_0 (= D^-1 b / theta) and
-// r = b - K d_0 at node v.
-template <typename T, bool SPLIT = true>
+// Degree-1 pre-smoothing from zero: r = b - K d_0 at node v (d_0 = D^-1 b /
+// theta).  The smoothed x is d_0 itself: the prolongation writes
+// x = d_0 + P e, so x is not stored here.
+template <typename T, int SK = kSkSplit>
 __device__ __forceinline__ void mg_resid_d0_node(const LevelView<T>& L, int64_t v) {
     const int64_t N = L.N;
     const T ks = (T)*L.ks;
     T y[3];
-    stencil_apply<T, typename MGStore<T>::type, SPLIT>(L.n, N, v, L.K, L.d0, y);
+    stencil_apply<T, typename MGStore<T>::type, SK>(L.n, N, v, L.K, L.d0, y);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        L.r[c * N + v] = L.b[c * N + v] - ks * y[c];
-        L.x[c * N + v] = L.d0[c * N + v];
-    }
+    for (int c = 0; c < 3; ++c) L.r[c * N + v] = L.b[c * N + v] - ks * y[c];
 }
 
-// r = b - K x and d_0 = D^-1 r / theta at node v (x is left for the next step).
-template <typename T, bool SPLIT = true>
+// r = b - K x and d_0 = D^-1 r / theta at node v (x is left for the next
+// step).  WR = false: r is not stored (degree-1 levels, whose update after
+// this is the pointwise x + d_0).
+template <typename T, int SK = kSkSplit, bool WR = true>
 __device__ __forceinline__ void mg_resid_first_node(const LevelView<T>& L, int64_t v) {
     const int64_t N = L.N;
     const T ks = (T)*L.ks;
     T y[3], rr[3];
-    stencil_apply<T, typename MGStore<T>::type, SPLIT>(L.n, N, v, L.K, L.x, y);
+    stencil_apply<T, typename MGStore<T>::type, SK>(L.n, N, v, L.K, L.x, y);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         rr[c] = L.b[c * N + v] - ks * y[c];
-        L.r[c * N + v] = rr[c];
+        if (WR) L.r[c * N + v] = rr[c];
     }
     mg_first_dir<T>(L, v, rr);
 }
 
+// The degree-1 post-smoothing of a level at node v, nothing stored:
+// xo = x + d_0 with d_0 = D^-1 (b - K x) / theta (the same roundings as
+// mg_resid_first_node followed by x + d_0).
+template <typename T, int SK = kSkSplit>
+__device__ __forceinline__ void mg_post1_node(const LevelView<T>& L, int64_t v, T xo[3]) {
+    const int64_t N = L.N;
+    const T ks = (T)*L.ks;
+    T y[3], rr[3], z[3];
+    stencil_apply<T, typename MGStore<T>::type, SK>(L.n, N, v, L.K, L.x, y);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) rr[c] = L.b[c * N + v] - ks * y[c];
+    dinv_apply<T>(N, v, L.Di, rr, z);
+    const T ith = (T)L.coef[0];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) xo[c] = L.x[c * N + v] + mul_rn(z[c], ith);
+}
+
 // b_c(I) = sum_a w_a r_f(2I + off[a])  (P^T r), zero on Dirichlet nodes; then
-// the coarse level's first direction.
+// the coarse level's first direction.  Branch-free: a fine node outside the
+// lattice reads node 0 and a Dirichlet one its own r, both with weight 0, so
+// every load of the node issues at once.
 template <typename T>
 __device__ __forceinline__ void mg_restrict_node(const LevelView<T>& F, const LevelView<T>& C,
                                                  int64_t I) {
@@ -355,9 +422,13 @@ __device__ __forceinline__ void mg_restrict_node(const LevelView<T>& F, const Le
         const int ci = (int)(I % nc), cj = (int)((I / nc) % nc), ck = (int)(I / ((int64_t)nc * nc));
 #pragma unroll
         for (int d = 0; d < 15; ++d) {
-            const int f = nbr(2 * ci, 2 * cj, 2 * ck, d, nf);
-            if (f < 0 || F.mask[f]) continue;
-            const T w = d == 0 ? T(1) : T(0.5);
+            int f = nbr(2 * ci, 2 * cj, 2 * ck, d, nf);
+            T w = d == 0 ? T(1) : T(0.5);
+            if (f < 0) {
+                f = 0;
+                w = T(0);
+            }
+            if (F.mask[f]) w = T(0);
             a[0] += w * F.r[f];
             a[1] += w * F.r[Nf + f];
             a[2] += w * F.r[2 * Nf + f];
@@ -369,45 +440,40 @@ __device__ __forceinline__ void mg_restrict_node(const LevelView<T>& F, const Le
     mg_first_dir<T>(C, I, a);
 }
 
-// x_f(f) += sum_{parents J} w x_c(J)  (P e).
-template <typename T>
+// x_f(f) += sum_{parents J} w x_c(J)  (P e); FROM_D0: x_f = d_0 + P e (a
+// degree-1 level, whose pre-smoothed x is d_0).
+template <typename T, bool FROM_D0 = false>
 __device__ __forceinline__ void mg_prolong_node(const LevelView<T>& F, const LevelView<T>& C,
                                                 int64_t f) {
-    if (F.mask[f]) return;
+    const T* base = FROM_D0 ? F.d0 : F.x;
+    if (F.mask[f]) {
+        if (FROM_D0)
+            for (int c = 0; c < 3; ++c) F.x[c * F.N + f] = base[c * F.N + f];
+        return;
+    }
     const int nf = F.n, nc = C.n;
     const int64_t Nf = F.N, Nc = C.N;
     const int fi = (int)(f % nf), fj = (int)((f / nf) % nf), fk = (int)(f / ((int64_t)nf * nf));
     const int Ai = fi >> 1, Aj = fj >> 1, Ak = fk >> 1;
     const int oi = fi & 1, oj = fj & 1, ok = fk & 1;
-    T s0 = T(0), s1 = T(0), s2 = T(0);
+    // parents A and Bn (Bn = A for a node on the coarse lattice, then weight 0);
+    // branch-free, so the masks and the values load together
     const int64_t A = Ai + (int64_t)nc * (Aj + (int64_t)nc * Ak);
-    if ((oi | oj | ok) == 0) {
-        if (!C.mask[A]) {
-            s0 = C.x[A];
-            s1 = C.x[Nc + A];
-            s2 = C.x[2 * Nc + A];
-        }
-    } else {
-        const int64_t Bn = (Ai + oi) + (int64_t)nc * ((Aj + oj) + (int64_t)nc * (Ak + ok));
-        if (!C.mask[A]) {
-            s0 += T(0.5) * C.x[A];
-            s1 += T(0.5) * C.x[Nc + A];
-            s2 += T(0.5) * C.x[2 * Nc + A];
-        }
-        if (!C.mask[Bn]) {
-            s0 += T(0.5) * C.x[Bn];
-            s1 += T(0.5) * C.x[Nc + Bn];
-            s2 += T(0.5) * C.x[2 * Nc + Bn];
-        }
-    }
-    F.x[f] += s0;
-    F.x[Nf + f] += s1;
-    F.x[2 * Nf + f] += s2;
+    const int64_t Bn = (Ai + oi) + (int64_t)nc * ((Aj + oj) + (int64_t)nc * (Ak + ok));
+    const bool on = (oi | oj | ok) == 0;
+    const T wa = C.mask[A] ? T(0) : (on ? T(1) : T(0.5));
+    const T wb = (on || C.mask[Bn]) ? T(0) : T(0.5);
+    const T s0 = wa * C.x[A] + wb * C.x[Bn];
+    const T s1 = wa * C.x[Nc + A] + wb * C.x[Nc + Bn];
+    const T s2 = wa * C.x[2 * Nc + A] + wb * C.x[2 * Nc + Bn];
+    F.x[f] = base[f] + s0;
+    F.x[Nf + f] = base[Nf + f] + s1;
+    F.x[2 * Nf + f] = base[2 * Nf + f] + s2;
 }
 
 // Coarsest level: `steps` Chebyshev steps from zero on L.b by the calling CTA
 // alone (every thread of the block must call it).
-template <typename T, bool SPLIT = true>
+template <typename T, int SK = kSkSplit>
 __device__ __forceinline__ void mg_coarse_block(const LevelView<T>& L, int steps) {
     const int64_t N = L.N;
     for (int64_t v = threadIdx.x; v < N; v += blockDim.x) {
@@ -427,7 +493,7 @@ __device__ __forceinline__ void mg_coarse_block(const LevelView<T>& L, int steps
         T* dout = (s & 1) ? L.d1 : L.d0;
         const int mode = s == 1 ? kStepFromZero : kStepRegular;
         for (int64_t v = threadIdx.x; v < N; v += blockDim.x)
-            mg_step_node<T, SPLIT>(L, v, s, mode, din, dout, xo, true, true);
+            mg_step_node<T, SK>(L, v, s, mode, din, dout, xo, true, true);
         __syncthreads();
     }
 }

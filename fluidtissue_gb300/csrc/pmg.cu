@@ -44,7 +44,8 @@ __device__ __forceinline__ T pentry(const T* __restrict__ K, int64_t N, int e, i
 // Set-up kernels
 // ---------------------------------------------------------------------------
 
-// Lumped 1/mu mass of node v: sum over its elements of vol / (4 mu).
+// Scaled lumped 1/mu mass of node v: kSchurScale times the sum over its
+// elements of vol / (4 mu).
 __device__ __forceinline__ double lumped_inv_mu(int64_t v, const int32_t* __restrict__ p2t_ptr,
                                                 const uint32_t* __restrict__ p2t,
                                                 const ElemGeom* __restrict__ geom,
@@ -54,7 +55,7 @@ __device__ __forceinline__ double lumped_inv_mu(int64_t v, const int32_t* __rest
         const int64_t k = p2t[q] >> 2;
         w += geom[k].vol / (4.0 * mu[k]);
     }
-    return w;
+    return kSchurScale * w;
 }
 
 // Fine level from the assembled system: the pressure entry (3,3) of the 4x4
@@ -226,14 +227,14 @@ k_pmg_residual(PView<T> L, const int* __restrict__ stop) {
         pmg_resid_node<T>(L, v);
 }
 
-template <typename T>
+template <typename T, bool WR = true>
 __global__ void __launch_bounds__(kThreads)
 k_pmg_resid_first(PView<T> L, const int* __restrict__ stop) {
     pdl_wait();
     if (stop && *stop) return;
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < L.N;
          v += (int64_t)gridDim.x * blockDim.x)
-        pmg_resid_first_node<T>(L, v);
+        pmg_resid_first_node<T, WR>(L, v);
 }
 
 template <typename T>
@@ -264,13 +265,13 @@ __global__ void k_pmg_restrict(PView<T> F, PView<T> C, const int* __restrict__ s
         pmg_restrict_node<T>(F, C, I);
 }
 
-template <typename T>
+template <typename T, bool FROM_D0 = false>
 __global__ void k_pmg_prolong(PView<T> F, PView<T> C, const int* __restrict__ stop) {
     pdl_wait();
     if (stop && *stop) return;
     for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < F.N;
          f += (int64_t)gridDim.x * blockDim.x)
-        pmg_prolong_node<T>(F, C, f);
+        pmg_prolong_node<T, FROM_D0>(F, C, f);
 }
 
 // Levels l0.. of one V-cycle in one CTA (__syncthreads between phases); the
@@ -540,12 +541,13 @@ static void pvcycle_level(Ctx& c, PMG<T>& pm, size_t l, cudaStream_t st, const i
     const int g = grid_for(c, L.N);
     if (pmg_level_degree1(pm, l)) {
         // degree 1: x = d_0, r = b - Kp d_0; after the coarse correction
-        // r = b - Kp x, d_0 = D^-1 r / theta, x += d_0 (the caller's when skip_final)
+        // x = d_0 + P e, r = b - Kp x (not stored), d_0 = D^-1 r / theta,
+        // x += d_0 (the caller's when skip_final)
         pdl_launch(k_pmg_resid_d0<T>, g, kThreads, st, L, stop);
-        k_pmg_restrict<T><<<grid_for(c, C.N), kThreads, 0, st>>>(L, C, stop);
+        pdl_launch(k_pmg_restrict<T>, grid_for(c, C.N), kThreads, st, L, C, stop);
         pvcycle_level<T>(c, pm, l + 1, st, stop, false);
-        pdl_launch(k_pmg_prolong<T>, g, kThreads, st, L, C, stop);
-        pdl_launch(k_pmg_resid_first<T>, g, kThreads, st, L, stop);
+        pdl_launch(k_pmg_prolong<T, true>, g, kThreads, st, L, C, stop);
+        pdl_launch(k_pmg_resid_first<T, false>, g, kThreads, st, L, stop);
         c.launches += 4;
         if (!skip_final) {
             pdl_launch(k_pmg_add_d0<T>, g, kThreads, st, L, stop);
@@ -561,7 +563,7 @@ static void pvcycle_level(Ctx& c, PMG<T>& pm, size_t l, cudaStream_t st, const i
         std::swap(din, dout);
     }
     pdl_launch(k_pmg_residual<T>, g, kThreads, st, L, stop);
-    k_pmg_restrict<T><<<grid_for(c, C.N), kThreads, 0, st>>>(L, C, stop);
+    pdl_launch(k_pmg_restrict<T>, grid_for(c, C.N), kThreads, st, L, C, stop);
     c.launches += kPSmooth + 1;
     pvcycle_level<T>(c, pm, l + 1, st, stop, false);
     pdl_launch(k_pmg_prolong<T>, g, kThreads, st, L, C, stop);

@@ -65,7 +65,10 @@ struct PMG {
 // The first kPDeg1Levels levels of the pressure hierarchy smooth with degree 1
 // (as kDeg1Levels for the velocity hierarchy); level l does unless it is the
 // coarsest or part of the single-CTA tail.
-constexpr int kPDeg1Levels = 1;
+#ifndef FTS_PDEG1_LEVELS
+#define FTS_PDEG1_LEVELS 1
+#endif
+constexpr int kPDeg1Levels = FTS_PDEG1_LEVELS;
 template <typename T>
 inline bool pmg_level_degree1(const PMG<T>& pm, size_t l) {
     return (int)l < kPDeg1Levels && (pm.tail_level < 0 || (int)l < pm.tail_level) &&

@@ -49,11 +49,11 @@ __device__ __forceinline__ T pmg_stencil(int n, int64_t N, int64_t v64, const T*
     return pmg_stencil_body<T, false>(n, N, v, i, j, k, K, x);
 }
 
-// Degree-1 pre-smoothing from zero: x = d_0, r = b - Kp d_0.
+// Degree-1 pre-smoothing from zero: r = b - Kp d_0 (the smoothed x is d_0,
+// written by the prolongation as x = d_0 + P e).
 template <typename T>
 __device__ __forceinline__ void pmg_resid_d0_node(const PView<T>& L, int64_t v) {
     L.r[v] = L.b[v] - pmg_stencil<T>(L.n, L.N, v, L.K, L.d0);
-    L.x[v] = L.d0[v];
 }
 
 // d_0 = D^-1 b / theta.
@@ -91,11 +91,12 @@ __device__ __forceinline__ void pmg_resid_node(const PView<T>& L, int64_t v) {
     L.r[v] = L.b[v] - pmg_stencil<T>(L.n, L.N, v, L.K, L.x);
 }
 
-// r = b - Kp x and d_0 = D^-1 r / theta (x is updated by the next step).
-template <typename T>
+// r = b - Kp x and d_0 = D^-1 r / theta (x is updated by the next step);
+// WR = false: r is not stored (degree-1 levels).
+template <typename T, bool WR = true>
 __device__ __forceinline__ void pmg_resid_first_node(const PView<T>& L, int64_t v) {
     const T rr = L.b[v] - pmg_stencil<T>(L.n, L.N, v, L.K, L.x);
-    L.r[v] = rr;
+    if (WR) L.r[v] = rr;
     pmg_first_dir<T>(L, v, rr);
 }
 
@@ -118,8 +119,9 @@ __device__ __forceinline__ void pmg_restrict_node(const PView<T>& F, const PView
 }
 
 // x_f += (P x_c)(f): the coarse value at even positions, the mean of the two
-// ends of the coarse Kuhn edge through f elsewhere.
-template <typename T>
+// ends of the coarse Kuhn edge through f elsewhere; FROM_D0: x_f = d_0 + P x_c
+// (a degree-1 level).
+template <typename T, bool FROM_D0 = false>
 __device__ __forceinline__ void pmg_prolong_node(const PView<T>& F, const PView<T>& C,
                                                  int64_t f) {
     const int nf = F.n, nc = C.n;
@@ -134,7 +136,7 @@ __device__ __forceinline__ void pmg_prolong_node(const PView<T>& F, const PView<
         const int64_t Bn = (Ai + oi) + (int64_t)nc * ((Aj + oj) + (int64_t)nc * (Ak + ok));
         s = T(0.5) * (C.x[A] + C.x[Bn]);
     }
-    F.x[f] += s;
+    F.x[f] = (FROM_D0 ? F.d0[f] : F.x[f]) + s;
 }
 
 }  // namespace fts
