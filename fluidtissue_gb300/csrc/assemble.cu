@@ -143,44 +143,50 @@ void launch_viscosity_profile(Ctx& c) {
 __global__ void k_mu_minmax(int64_t nt, const int32_t* __restrict__ tets,
                             const double* __restrict__ phi, const double* __restrict__ mu,
                             Reduction red, OuterScalars* os) {
-    double mn = DBL_MAX, mx = -DBL_MAX;
+    // [0] interior min, [1] interior max, [2] min, [3] max
+    double m[4] = {DBL_MAX, -DBL_MAX, DBL_MAX, -DBL_MAX};
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nt;
          k += (int64_t)gridDim.x * blockDim.x) {
         int4 t = reinterpret_cast<const int4*>(tets)[k];
+        const double u = mu[k];
         if (phi[t.x] < 0.0 && phi[t.y] < 0.0 && phi[t.z] < 0.0 && phi[t.w] < 0.0) {
-            mn = fmin(mn, mu[k]);
-            mx = fmax(mx, mu[k]);
+            m[0] = fmin(m[0], u);
+            m[1] = fmax(m[1], u);
         }
+        m[2] = fmin(m[2], u);
+        m[3] = fmax(m[3], u);
     }
-    // max-reduce (-mn, mx) through shuffles; partials via the ticket
+    // reduce through shuffles; partials via the ticket
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const double other = __shfl_xor_sync(0xffffffffu, m[q], o);
+            m[q] = (q & 1) ? fmax(m[q], other) : fmin(m[q], other);
+        }
     }
-    __shared__ double smn[32], smx[32];
+    __shared__ double sm[4][32];
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) {
-        smn[wid] = mn;
-        smx[wid] = mx;
-    }
+    if (lane == 0)
+        for (int q = 0; q < 4; ++q) sm[q][wid] = m[q];
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-            mn = fmin(mn, smn[w]);
-            mx = fmax(mx, smx[w]);
-        }
-        red.partials[blockIdx.x] = mn;
-        red.partials[kMaxPartials + blockIdx.x] = mx;
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+            for (int q = 0; q < 4; ++q)
+                m[q] = (q & 1) ? fmax(m[q], sm[q][w]) : fmin(m[q], sm[q][w]);
+        for (int q = 0; q < 4; ++q) red.partials[q * kMaxPartials + blockIdx.x] = m[q];
     }
     if (last_block(red) && threadIdx.x == 0) {
-        double a = DBL_MAX, b = -DBL_MAX;
-        for (unsigned i = 0; i < gridDim.x; ++i) {
-            a = fmin(a, __ldcg(&red.partials[i]));
-            b = fmax(b, __ldcg(&red.partials[kMaxPartials + i]));
-        }
-        os->mu_min = a;
-        os->mu_max = b;
+        double a[4] = {DBL_MAX, -DBL_MAX, DBL_MAX, -DBL_MAX};
+        for (unsigned i = 0; i < gridDim.x; ++i)
+            for (int q = 0; q < 4; ++q) {
+                const double p = __ldcg(&red.partials[q * kMaxPartials + i]);
+                a[q] = (q & 1) ? fmax(a[q], p) : fmin(a[q], p);
+            }
+        os->mu_min = a[0];
+        os->mu_max = a[1];
+        os->mu_all_min = a[2];
+        os->mu_all_max = a[3];
     }
 }
 
@@ -497,8 +503,8 @@ void launch_assemble_lat(Ctx& c) {
 // ---------------------------------------------------------------------------
 // Block-diagonal SPD preconditioner: inverse of the node's 3x3 velocity block
 // (identity on Dirichlet nodes) and, for pressure, the inverse of
-// (alpha D + eps M)_ii + kSchurScale sum_{e ni i} vol_e / (4 mu_e) (lumped
-// 1/mu-weighted mass, a Schur-complement estimate).  pc[8 i + 0..5] = xx xy xz yy yz zz,
+// (alpha D + eps M)_ii + s sum_{e ni i} vol_e / (4 mu_e) (lumped 1/mu-weighted
+// mass, a Schur-complement estimate; s = schur_scale).  pc[8 i + 0..5] = xx xy xz yy yz zz,
 // pc[8 i + 6] = pressure weight.
 // ---------------------------------------------------------------------------
 // Diagonal block (i, i) of the BSR and of the FP64 lattice half stencil.
@@ -529,7 +535,9 @@ template <typename Diag>
 __global__ void k_preconditioner(int64_t np, Diag dg, const int32_t* __restrict__ p2t_ptr,
                                  const uint32_t* __restrict__ p2t,
                                  const ElemGeom* __restrict__ geom, const double* __restrict__ mu,
+                                 const OuterScalars* __restrict__ os,
                                  const uint8_t* __restrict__ bnd, double* __restrict__ pc) {
+    const double ws = schur_scale(os);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < np;
          i += (int64_t)gridDim.x * blockDim.x) {
         double D[16];
@@ -551,13 +559,9 @@ __global__ void k_preconditioner(int64_t np, Diag dg, const int32_t* __restrict_
             o[0] = c00 * id; o[1] = c01 * id; o[2] = c02 * id;
             o[3] = c11 * id; o[4] = c12 * id; o[5] = c22 * id;
         }
-        double w = 0.0;
-        for (int32_t q = p2t_ptr[i]; q < p2t_ptr[i + 1]; ++q) {
-            int64_t k = p2t[q] >> 2;
-            w += geom[k].vol / (4.0 * mu[k]);
-        }
+        const double w = ws * lumped_inv_mu(i, p2t_ptr, p2t, geom, mu);
         // a node without pressure (P2 edge node: zero pressure row) gets weight 0
-        const double dp = -D[15] + kSchurScale * w;
+        const double dp = -D[15] + w;
         o[6] = dp != 0.0 ? 1.0 / dp : 0.0;
         o[7] = 0.0;
 #pragma unroll
@@ -568,10 +572,10 @@ __global__ void k_preconditioner(int64_t np, Diag dg, const int32_t* __restrict_
 void launch_preconditioner(Ctx& c) {
     if (c.use_lat64)
         k_preconditioner<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
-            c.np, LatDiag{c.lat64}, c.p2t_ptr, c.p2t, c.geom, c.mu, c.bnd, c.pc64);
+            c.np, LatDiag{c.lat64}, c.p2t_ptr, c.p2t, c.geom, c.mu, c.os, c.bnd, c.pc64);
     else
         k_preconditioner<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
-            c.np, BsrDiag{c.A64, c.diag}, c.p2t_ptr, c.p2t, c.geom, c.mu, c.bnd, c.pc64);
+            c.np, BsrDiag{c.A64, c.diag}, c.p2t_ptr, c.p2t, c.geom, c.mu, c.os, c.bnd, c.pc64);
     FTS_CUDA(cudaGetLastError());
     c.launches += 1;
 }

@@ -879,6 +879,7 @@ static void batch_assemble(fts_batch& B, const std::vector<int>& have_mu) {
         launch_check_finite(c, c.src, c.np);
         if (have_mu[i]) launch_check_finite(c, c.mu, c.nt);
         if (!have_mu[i]) launch_viscosity_profile(c);
+        launch_mu_minmax(c);  // the Schur weight's scale reads the range
         launch_source(c);
         launch_rhs(c, false);
         launch_assemble(c);

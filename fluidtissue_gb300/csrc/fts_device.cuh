@@ -38,15 +38,6 @@ struct CudaError {
 constexpr int kThreads = 256;
 constexpr int kMaxPartials = 4096;
 
-// Scale of the lumped 1/mu-weighted pressure mass sum_e vol_e / (4 mu_e) in
-// every Schur-complement estimate of the preconditioner (pressure weights and
-// the pressure multigrid's fine operator).  The viscous term is
-// 2 mu eps(u) : eps(v), so B K^-1 B^T is about M / (2 mu): scale 1/2.
-#ifndef FTS_SCHUR_SCALE
-#define FTS_SCHUR_SCALE 0.5
-#endif
-constexpr double kSchurScale = FTS_SCHUR_SCALE;
-
 // Node-interleaved vector element: (ux, uy, uz, p).
 template <typename T>
 struct alignas(4 * sizeof(T)) V4 {
@@ -63,6 +54,21 @@ struct alignas(128) ElemGeom {
     double hh;
     double pad[2];
 };
+
+// Unscaled Schur-complement weight of node v: the lumped 1/mu-weighted mass,
+// sum over the node's elements of vol_e / (4 mu_e) (the caller multiplies by
+// schur_scale).
+__device__ __forceinline__ double lumped_inv_mu(int64_t v, const int32_t* __restrict__ p2t_ptr,
+                                                const uint32_t* __restrict__ p2t,
+                                                const ElemGeom* __restrict__ geom,
+                                                const double* __restrict__ mu) {
+    double w = 0.0;
+    for (int32_t q = p2t_ptr[v]; q < p2t_ptr[v + 1]; ++q) {
+        const int64_t k = p2t[q] >> 2;
+        w += geom[k].vol / (4.0 * mu[k]);
+    }
+    return w;
+}
 
 // FP64 lattice half stencil (Kuhn lattices, mixed precision): entries
 // (r, 2h) and (r, 2h + 1) of node v's 4x4 block towards direction d (0 = self,
@@ -96,10 +102,32 @@ struct OuterScalars {
     double bb;     // ||b||^2
     double scale;  // 1 / ||r|| used to normalise the FP32 inner right-hand side
     double sum;    // scratch reduction (source mean)
-    double mu_min, mu_max;
+    double mu_min, mu_max;          // over the interior elements (Flow.cpp:241)
+    double mu_all_min, mu_all_max;  // over every element (the Schur weight's scale)
     int nonfinite;
     int pad;
 };
+
+// Scale s of every Schur-complement estimate of the preconditioner (pressure
+// weights, the pressure multigrid's fine operator): Kp = alpha D + eps M +
+// s * lumped 1/mu mass.  The viscous term is 2 mu eps(u) : eps(v), so with
+// constant viscosity B K^-1 B^T is about M / (2 mu): s = 1/2.  With viscosity
+// contrast the weighted mass overestimates the Schur complement (the stiff
+// side of an interface carries its nodes), and s falls with the contrast C =
+// max mu / min mu over the elements: s = 1/2 / (1 + 1.5 log10 C), which
+// matches the measured optimum of a uniform s on constant viscosity (1/2) and
+// on contrast 200 (about 1/8).
+#ifndef FTS_SCHUR_SCALE
+#define FTS_SCHUR_SCALE 0.5
+#endif
+#ifndef FTS_SCHUR_CONTRAST
+#define FTS_SCHUR_CONTRAST 1.5
+#endif
+__device__ __forceinline__ double schur_scale(const OuterScalars* os) {
+    const double lo = os->mu_all_min, hi = os->mu_all_max;
+    const double lc = (lo > 0.0 && hi > lo) ? log10(hi / lo) : 0.0;
+    return FTS_SCHUR_SCALE / (1.0 + FTS_SCHUR_CONTRAST * lc);
+}
 
 struct Reduction {
     double* partials;   // [kMaxPartials * 4]

@@ -470,11 +470,13 @@ k_mf_residual64(int64_t np, const int32_t* __restrict__ p2t_ptr, const uint32_t*
 }
 
 // Pressure weight of the preconditioner per node (the velocity part is the
-// multigrid V-cycle): 1 / (alpha D_ii + eps M_ii + kSchurScale sum_e vol/(4 mu_e)).
+// multigrid V-cycle): 1 / (alpha D_ii + eps M_ii + s sum_e vol/(4 mu_e)), s =
+// schur_scale.
 __global__ void k_mf_pc(int64_t np, const int32_t* __restrict__ p2t_ptr,
                         const uint32_t* __restrict__ p2t, const ElemGeom* __restrict__ geom,
                         const double* __restrict__ mu, double alpha, double eps, MfConst K,
-                        float* __restrict__ pc) {
+                        const OuterScalars* __restrict__ os, float* __restrict__ pc) {
+    const double ws = schur_scale(os);
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < np;
          v += (int64_t)gridDim.x * blockDim.x) {
         double d = 0.0;
@@ -484,9 +486,9 @@ __global__ void k_mf_pc(int64_t np, const int32_t* __restrict__ p2t_ptr,
             const int a = e & 3;
             const ElemGeom& G = geom[k];
             const double gg = G.g[a][0] * G.g[a][0] + G.g[a][1] * G.g[a][1] + G.g[a][2] * G.g[a][2];
-            d += alpha * G.hh * G.vol * gg + eps * G.vol * K.mrefd[a][a] +
-                 kSchurScale * (G.vol / (4.0 * mu[k]));
+            d += alpha * G.hh * G.vol * gg + eps * G.vol * K.mrefd[a][a];
         }
+        d += ws * lumped_inv_mu(v, p2t_ptr, p2t, geom, mu);
         float* o = pc + 8 * v;
         o[0] = 1.f;
         o[1] = 0.f;
@@ -548,7 +550,8 @@ void launch_mf_pc(Ctx& c) {
     }
     c.launches += 1;
     k_mf_pc<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(c.np, c.p2t_ptr, c.p2t, c.geom, c.mu,
-                                                         c.par.alpha, c.par.eps, K, c.pc32);
+                                                         c.par.alpha, c.par.eps, K, c.os,
+                                                         c.pc32);
     FTS_CUDA(cudaGetLastError());
     c.launches += 1;
 }

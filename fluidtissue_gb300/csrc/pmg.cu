@@ -44,20 +44,6 @@ __device__ __forceinline__ T pentry(const T* __restrict__ K, int64_t N, int e, i
 // Set-up kernels
 // ---------------------------------------------------------------------------
 
-// Scaled lumped 1/mu mass of node v: kSchurScale times the sum over its
-// elements of vol / (4 mu).
-__device__ __forceinline__ double lumped_inv_mu(int64_t v, const int32_t* __restrict__ p2t_ptr,
-                                                const uint32_t* __restrict__ p2t,
-                                                const ElemGeom* __restrict__ geom,
-                                                const double* __restrict__ mu) {
-    double w = 0.0;
-    for (int32_t q = p2t_ptr[v]; q < p2t_ptr[v + 1]; ++q) {
-        const int64_t k = p2t[q] >> 2;
-        w += geom[k].vol / (4.0 * mu[k]);
-    }
-    return kSchurScale * w;
-}
-
 // Fine level from the assembled system: the pressure entry (3,3) of the 4x4
 // blocks, negated back to +(alpha D + eps M), plus w on the diagonal.  One
 // thread per (node, stored direction).
@@ -66,8 +52,10 @@ __global__ void k_pmg_extract(int n, const int32_t* __restrict__ rowptr,
                               const int32_t* __restrict__ cols, const double* __restrict__ A,
                               const int32_t* __restrict__ p2t_ptr,
                               const uint32_t* __restrict__ p2t, const ElemGeom* __restrict__ geom,
-                              const double* __restrict__ mu, T* __restrict__ K) {
+                              const double* __restrict__ mu, const OuterScalars* __restrict__ os,
+                              T* __restrict__ K) {
     const int64_t N = (int64_t)n * n * n;
+    const double ws = schur_scale(os);
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * 8;
          t += (int64_t)gridDim.x * blockDim.x) {
         const int d = (int)(t / N);
@@ -84,7 +72,7 @@ __global__ void k_pmg_extract(int n, const int32_t* __restrict__ rowptr,
             }
             if (cols[lo] == w) val = -A[(int64_t)lo * 16 + 15];
         }
-        if (d == 0) val += lumped_inv_mu(v, p2t_ptr, p2t, geom, mu);
+        if (d == 0) val += ws * lumped_inv_mu(v, p2t_ptr, p2t, geom, mu);
         K[d * N + v] = (T)val;
     }
 }
@@ -95,14 +83,16 @@ __global__ void k_pmg_extract_lat(int n, const double2* __restrict__ L,
                                   const int32_t* __restrict__ p2t_ptr,
                                   const uint32_t* __restrict__ p2t,
                                   const ElemGeom* __restrict__ geom,
-                                  const double* __restrict__ mu, T* __restrict__ K) {
+                                  const double* __restrict__ mu,
+                                  const OuterScalars* __restrict__ os, T* __restrict__ K) {
     const int64_t N = (int64_t)n * n * n;
+    const double ws = schur_scale(os);
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * 8;
          t += (int64_t)gridDim.x * blockDim.x) {
         const int d = (int)(t / N);
         const int64_t v = t - d * N;
         double val = -L[lat64_idx(d, 3, 1, v)].y;
-        if (d == 0) val += lumped_inv_mu(v, p2t_ptr, p2t, geom, mu);
+        if (d == 0) val += ws * lumped_inv_mu(v, p2t_ptr, p2t, geom, mu);
         K[d * N + v] = (T)val;
     }
 }
@@ -120,8 +110,10 @@ __global__ void k_pmg_from_elements(int n, const int32_t* __restrict__ p2t_ptr,
                                     const int32_t* __restrict__ tets,
                                     const ElemGeom* __restrict__ geom,
                                     const double* __restrict__ mu, double alpha, double eps,
-                                    PRef R, T* __restrict__ K) {
+                                    PRef R, const OuterScalars* __restrict__ os,
+                                    T* __restrict__ K) {
     const int64_t N = (int64_t)n * n * n;
+    const double ws = schur_scale(os);
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * 8;
          t += (int64_t)gridDim.x * blockDim.x) {
         const int d = (int)(t / N);
@@ -149,7 +141,7 @@ __global__ void k_pmg_from_elements(int n, const int32_t* __restrict__ p2t_ptr,
                 }
             }
         }
-        if (d == 0) val += lumped_inv_mu(v, p2t_ptr, p2t, geom, mu);
+        if (d == 0) val += ws * lumped_inv_mu(v, p2t_ptr, p2t, geom, mu);
         K[d * N + v] = (T)val;
     }
 }
@@ -433,16 +425,18 @@ void pmg_setup_enqueue(Ctx& c, PMG<T>& pm, cudaStream_t st) {
             for (int b = 0; b < 4; ++b) pr.mref[a][b] = R.mref[a][b];
         if (c.topo.kuhn_elements)
             k_pmg_from_elements<T, true><<<grid_for(c, F.N * 8), kThreads, 0, st>>>(
-                F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.par.alpha, c.par.eps, pr, F.K);
+                F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.par.alpha, c.par.eps, pr, c.os,
+                F.K);
         else
             k_pmg_from_elements<T, false><<<grid_for(c, F.N * 8), kThreads, 0, st>>>(
-                F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.par.alpha, c.par.eps, pr, F.K);
+                F.n, c.p2t_ptr, c.p2t, c.tets, c.geom, c.mu, c.par.alpha, c.par.eps, pr, c.os,
+                F.K);
     } else if (c.use_lat64) {
         k_pmg_extract_lat<T><<<grid_for(c, F.N * 8), kThreads, 0, st>>>(
-            F.n, c.lat64, c.p2t_ptr, c.p2t, c.geom, c.mu, F.K);
+            F.n, c.lat64, c.p2t_ptr, c.p2t, c.geom, c.mu, c.os, F.K);
     } else {
         k_pmg_extract<T><<<grid_for(c, F.N * 8), kThreads, 0, st>>>(
-            F.n, c.rowptr, c.cols, c.A64, c.p2t_ptr, c.p2t, c.geom, c.mu, F.K);
+            F.n, c.rowptr, c.cols, c.A64, c.p2t_ptr, c.p2t, c.geom, c.mu, c.os, F.K);
     }
     c.launches += 1;
     FTS_CUDA(cudaMemsetAsync(pm.gersh, 0, pm.L.size() * sizeof(unsigned long long), st));
