@@ -477,7 +477,9 @@ static int solve_device(Ctx& c, bool have_mu, bool have_force, double* flow_out,
     int outer = 0;
     int status = FTS_OK;
     double est = rel;
-    const double floor32 = P.inner_tol > 0.0 ? P.inner_tol : 1e-4;
+    const double floor32 = P.inner_tol > 0.0 ? P.inner_tol
+                           : (!c.p2 && c.np >= kInnerTolLargeNodes) ? kInnerTolFloorLarge
+                                                                    : kInnerTolFloorSmall;
     while (rel > tol) {
         if (outer >= 40 || iters >= maxit) {
             status = FTS_ERR_NOT_CONVERGED;

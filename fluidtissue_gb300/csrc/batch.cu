@@ -936,7 +936,7 @@ static void batch_reset_outer(fts_batch& B) {
         O.rel = 1.0;
         O.pc_ratio = B.precision == FTS_PREC_MIXED ? c.pc_ratio32 : c.pc_ratio64;
         O.tol = c.par.tol > 0.0 ? c.par.tol : DBL_EPSILON;
-        O.floor32 = c.par.inner_tol > 0.0 ? c.par.inner_tol : 1e-4;
+        O.floor32 = c.par.inner_tol > 0.0 ? c.par.inner_tol : kInnerTolFloorLarge;
         const long long N = 3 * c.topo.n_interior + c.np;
         O.maxit = c.par.max_iter > 0 ? c.par.max_iter : 2 * N;
     }

@@ -38,6 +38,17 @@ struct CudaError {
 constexpr int kThreads = 256;
 constexpr int kMaxPartials = 4096;
 
+// Mixed precision: the smallest relative reduction asked of one FP32 inner
+// MINRES run (the parameter inner_tol overrides it).  Deeper inner runs mean
+// fewer outer passes and restarts: 1e-5 for P1 systems of at least 100,000
+// nodes and for batches (measured: 129^3 122 -> 116 iterations, 257^3 141 ->
+// 139, 65^3 99 -> 99 with the set-up of one pass less, batch96 358 -> 325
+// mean), 1e-4 for smaller systems and P2-P1 (17^3: 365 at 1e-4 against 436
+// at 1e-5; P2-P1 33^3: 211 against 231).
+constexpr double kInnerTolFloorLarge = 1e-5;
+constexpr double kInnerTolFloorSmall = 1e-4;
+constexpr int64_t kInnerTolLargeNodes = 100000;
+
 // Node-interleaved vector element: (ux, uy, uz, p).
 template <typename T>
 struct alignas(4 * sizeof(T)) V4 {

@@ -374,7 +374,10 @@ __global__ void k_mg_unit_scale(int levels, double* __restrict__ scale) {
 //   rho_0 = 1/sigma, rho_i = 1/(2 sigma - rho_{i-1});
 //   d_0 = D^-1 r / theta;  d_i = rho_i rho_{i-1} d_{i-1} + (2 rho_i/delta) D^-1 r_i.
 // ---------------------------------------------------------------------------
-constexpr double kLowFrac = 0.1;
+#ifndef FTS_MG_LOW_FRAC
+#define FTS_MG_LOW_FRAC 0.1
+#endif
+constexpr double kLowFrac = FTS_MG_LOW_FRAC;
 constexpr int kCoarseThreads = 256;  // one CTA for the coarsest level (<= 9^3 nodes)
 
 // Chebyshev coefficients of one level, computed once per solve on the host.
@@ -668,6 +671,12 @@ void mg_setup(Ctx& c, MG<T>& mg) {
         k_mg_extract<T><<<grid_for(c, F.N * 8), kThreads, 0, c.stream>>>(F.n, c.rowptr, c.cols,
                                                                            c.A64, F.K);
     c.launches += 1;
+    // Each level's power iterations need only its own stencil and D^-1: with a
+    // second stream (and the pressure set-up on it, whose kernels reduce
+    // nothing through c.red) they run there, under the next levels' Galerkin
+    // products on this stream.
+    const bool side = c.aux_stream != nullptr && c.use_pmg;
+    cudaStream_t ps = side ? c.aux_stream : c.stream;
     for (size_t l = 0; l < mg.L.size(); ++l) {
         MGLevel<T>& L = mg.L[l];
         if (l > 0) {
@@ -680,17 +689,25 @@ void mg_setup(Ctx& c, MG<T>& mg) {
         mg_store(c, mg, l);
         k_mg_power_init<T><<<grid_for(c, L.N), kThreads, 0, c.stream>>>(L.N, L.mask, L.d0);
         c.launches += 2;
+        if (side) {
+            FTS_CUDA(cudaEventRecord(c.ev_fork, c.stream));
+            FTS_CUDA(cudaStreamWaitEvent(ps, c.ev_fork, 0));
+        }
         const LevelView<T> V = level_view(mg, l);
         T* v = L.d0;
         T* w = L.d1;
         for (int it = 0; it < kPowerIters; ++it) {
-            k_mg_power<T><<<grid_for(c, L.N), kThreads, 0, c.stream>>>(V, v, w, mg.lam + l,
-                                                                        it == 0, c.red);
+            k_mg_power<T><<<grid_for(c, L.N), kThreads, 0, ps>>>(V, v, w, mg.lam + l, it == 0,
+                                                                  c.red);
             c.launches += 1;
             T* t = v;
             v = w;
             w = t;
         }
+    }
+    if (side) {
+        FTS_CUDA(cudaEventRecord(c.ev_join, ps));
+        FTS_CUDA(cudaStreamWaitEvent(c.stream, c.ev_join, 0));
     }
     FTS_CUDA(cudaGetLastError());
     // lambda_max ~ ||D^-1 K v|| for the normalised v of the last step; scale by

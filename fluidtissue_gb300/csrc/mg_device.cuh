@@ -189,9 +189,6 @@ __device__ __forceinline__ void stencil_h_body(int n, int64_t N, int v, int i, i
         a1 = fmaf(f[3], x0, fmaf(f[4], x1, fmaf(f[5], x2, a1)));
         a2 = fmaf(f[6], x0, fmaf(f[7], x1, fmaf(f8, x2, a2)));
     }
-#ifdef FTS_CLAMP_TWO_ROUNDS
-    if (B == kBodyClamped) asm volatile("" ::: "memory");
-#endif
 #pragma unroll
     for (int d = 1; d < 8; ++d) {  // negative directions: neighbour's block, transposed
         float m;

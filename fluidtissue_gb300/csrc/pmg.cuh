@@ -29,7 +29,10 @@
 namespace fts {
 
 constexpr int kPSmooth = 2;          // Chebyshev degree of each pressure pre / post smoothing
-constexpr double kPLowFrac = 0.1;    // lower end of the smoothing interval / lambda
+#ifndef FTS_PMG_LOW_FRAC
+#define FTS_PMG_LOW_FRAC 0.1
+#endif
+constexpr double kPLowFrac = FTS_PMG_LOW_FRAC;  // lower end of the smoothing interval / lambda
 
 // Levels with at most this many nodes run in one launch of a single CTA.
 constexpr int64_t kPTailNodes = 1000;

@@ -121,8 +121,10 @@ typedef struct fts_params {
     int32_t warm_start;         /* 1: start from the previous solution (USE_INITIAL_GUESS,
                                    Flow.cpp:15); 0: start from zero */
     int32_t device;             /* CUDA device ordinal */
-    double inner_tol;           /* mixed precision: relative reduction asked of each FP32
-                                   inner solve (<= 0: default 1e-4) */
+    double inner_tol;           /* mixed precision: smallest relative reduction asked of
+                                   each FP32 inner solve (<= 0: default 1e-5 for P1
+                                   systems of >= 100,000 nodes and for batches, else
+                                   1e-4) */
     int32_t verbose;            /* 1: print the reference's progress lines to stdout */
     int32_t time_kernels;       /* 1: bracket every operator application of the Krylov
                                    loop with CUDA events (fills fts_stats.ms_spmv) */
