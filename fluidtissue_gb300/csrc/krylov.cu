@@ -593,7 +593,7 @@ k_minres_pc1(int64_t np, int init, const V4<T>* __restrict__ q, V4<T>* R1,
 // stage 1's pressure diagonal (kPc2None), the pressure V-cycle's pointwise
 // x + d_0 (kPc2Fine1) or its fused last step (kPc2Step).  Each form is its own
 // kernel so that the pointwise ones keep few registers (one kernel for all
-// held 168 registers and a quarter of the warps).
+// held 168 registers and an eighth of the warps).
 enum : int { kPc2Step = 0, kPc2Fine1 = 1, kPc2Post = 2, kPc2None = 3 };
 template <typename T, int FORM, int PFORM>
 __global__ void __launch_bounds__(kThreads, 4)
