@@ -569,7 +569,12 @@ __global__ void k_preconditioner(int64_t np, Diag dg, const int32_t* __restrict_
     }
 }
 
+// With both V-cycles (velocity and pressure multigrid) the node weights are
+// never read, so they are not formed.
+static bool pc_unused(const Ctx& c) { return c.use_mg && c.use_pmg; }
+
 void launch_preconditioner(Ctx& c) {
+    if (pc_unused(c)) return;
     if (c.use_lat64)
         k_preconditioner<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(
             c.np, LatDiag{c.lat64}, c.p2t_ptr, c.p2t, c.geom, c.mu, c.os, c.bnd, c.pc64);
@@ -660,6 +665,7 @@ void launch_to_f32(Ctx& c) {
                         __FILE__, __LINE__);
     if (c.use_lat64) {
         // lat_val was written by the lattice assembly
+        if (pc_unused(c)) return;
         k_to_f32<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(c.np * 8, c.pc64, c.pc32);
         FTS_CUDA(cudaGetLastError());
         c.launches += 1;
@@ -674,9 +680,12 @@ void launch_to_f32(Ctx& c) {
             c.np, c.nslices, c.rowptr, c.A64, c.ell_ptr, c.ell_val);
     else
         k_to_f32<<<grid_for(c, c.nnzb * 8), kThreads, 0, c.stream>>>(c.nnzb * 16, c.A64, c.A32);
-    k_to_f32<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(c.np * 8, c.pc64, c.pc32);
+    c.launches += 1;
+    if (!pc_unused(c)) {
+        k_to_f32<<<grid_for(c, c.np * 4), kThreads, 0, c.stream>>>(c.np * 8, c.pc64, c.pc32);
+        c.launches += 1;
+    }
     FTS_CUDA(cudaGetLastError());
-    c.launches += 2;
 }
 
 // flow = [ux(np), uy(np), uz(np), p(np)], zero velocity on boundary nodes

@@ -549,6 +549,9 @@ void launch_mf_pc(Ctx& c) {
             c.nt, c.geom, c.mu, reinterpret_cast<ElemF32*>(c.mf_rec));
     }
     c.launches += 1;
+    // with both V-cycles no node weight is read (velocity and pressure come
+    // from the hierarchies)
+    if (c.use_mg && c.use_pmg) return;
     k_mf_pc<<<grid_for(c, c.np), kThreads, 0, c.stream>>>(c.np, c.p2t_ptr, c.p2t, c.geom, c.mu,
                                                          c.par.alpha, c.par.eps, K, c.os,
                                                          c.pc32);
