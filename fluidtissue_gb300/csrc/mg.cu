@@ -224,24 +224,35 @@ __global__ void k_mg_coarse_mask(int nf, const uint8_t* __restrict__ mf, int nc,
     }
 }
 
-// Galerkin coarse operator, one thread per (coarse node, coarse direction).
+// Galerkin coarse operator, one thread per (coarse node, coarse direction);
+// the self block (115 terms against 15..27 for the others) is split over
+// kGalSelfSplit threads whose partial sums k_mg_galerkin_self adds, so no
+// thread walks far more terms than the rest.
+constexpr int kGalSelfSplit = 4;
+
 template <typename T>
 __global__ void k_mg_galerkin(int nf, const T* __restrict__ Kf, const uint8_t* __restrict__ mf,
-                              int nc, T* __restrict__ Kc, const uint8_t* __restrict__ mc) {
+                              int nc, T* __restrict__ Kc, const uint8_t* __restrict__ mc,
+                              T* __restrict__ self_part) {
     const int64_t Nf = (int64_t)nf * nf * nf, Nc = (int64_t)nc * nc * nc;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Nc * 8;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Nc * (7 + kGalSelfSplit);
          t += (int64_t)gridDim.x * blockDim.x) {
-        const int dJ = (int)(t / Nc);
-        const int64_t I = t - dJ * Nc;
+        const int vd = (int)(t / Nc);
+        const int64_t I = t - vd * Nc;
+        const int dJ = vd < kGalSelfSplit ? 0 : vd - kGalSelfSplit + 1;
+        int q0 = c_gal_start[dJ], q1 = c_gal_start[dJ + 1];
+        if (dJ == 0) {
+            const int len = q1 - q0;
+            q1 = q0 + (vd + 1) * len / kGalSelfSplit;
+            q0 = q0 + vd * len / kGalSelfSplit;
+        }
         const int ci = (int)(I % nc), cj = (int)((I / nc) % nc), ck = (int)(I / ((int64_t)nc * nc));
         T acc[9];
 #pragma unroll
         for (int e = 0; e < 9; ++e) acc[e] = T(0);
         const int J = nbr(ci, cj, ck, dJ, nc);
-        if (mc[I]) {
-            if (dJ == 0) acc[0] = acc[4] = acc[8] = T(1);
-        } else if (J >= 0 && !mc[J]) {
-            for (int q = c_gal_start[dJ]; q < c_gal_start[dJ + 1]; ++q) {
+        if (!mc[I] && J >= 0 && !mc[J]) {
+            for (int q = q0; q < q1; ++q) {
                 const int a = c_gal_term[q] & 15, e = (c_gal_term[q] >> 4) & 15;
                 const int fi = 2 * ci + off_x(a), fj = 2 * cj + off_y(a), fk = 2 * ck + off_z(a);
                 if (fi < 0 || fj < 0 || fk < 0 || fi >= nf || fj >= nf || fk >= nf) continue;
@@ -254,15 +265,43 @@ __global__ void k_mg_galerkin(int nf, const T* __restrict__ Kf, const uint8_t* _
                 for (int x = 0; x < 9; ++x) acc[x] += w * kblock<T>(Kf, e, x, f, nf);
             }
         }
-        if (dJ == 0) {  // the self block of a symmetric operator: symmetrise rounding
-            T s01 = T(0.5) * (acc[1] + acc[3]), s02 = T(0.5) * (acc[2] + acc[6]),
-              s12 = T(0.5) * (acc[5] + acc[7]);
+        if (dJ == 0) {
+#pragma unroll
+            for (int x = 0; x < 9; ++x) self_part[((int64_t)vd * 9 + x) * Nc + I] = acc[x];
+        } else {
+#pragma unroll
+            for (int x = 0; x < 9; ++x) Kc[kidx(dJ * 9 + x, I)] = acc[x];
+        }
+    }
+}
+
+// The self blocks of a Galerkin product: the partial sums in a fixed order,
+// identity on Dirichlet nodes, the symmetric part (symmetrising rounding).
+template <typename T>
+__global__ void k_mg_galerkin_self(int nc, const T* __restrict__ self_part, T* __restrict__ Kc,
+                                   const uint8_t* __restrict__ mc) {
+    const int64_t Nc = (int64_t)nc * nc * nc;
+    for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < Nc;
+         I += (int64_t)gridDim.x * blockDim.x) {
+        T acc[9];
+#pragma unroll
+        for (int x = 0; x < 9; ++x) {
+            T s = T(0);
+            for (int p = 0; p < kGalSelfSplit; ++p) s += self_part[((int64_t)p * 9 + x) * Nc + I];
+            acc[x] = s;
+        }
+        if (mc[I]) {
+#pragma unroll
+            for (int x = 0; x < 9; ++x) acc[x] = (x % 4 == 0) ? T(1) : T(0);
+        } else {
+            const T s01 = T(0.5) * (acc[1] + acc[3]), s02 = T(0.5) * (acc[2] + acc[6]),
+                    s12 = T(0.5) * (acc[5] + acc[7]);
             acc[1] = acc[3] = s01;
             acc[2] = acc[6] = s02;
             acc[5] = acc[7] = s12;
         }
 #pragma unroll
-        for (int x = 0; x < 9; ++x) Kc[kidx(dJ * 9 + x, I)] = acc[x];
+        for (int x = 0; x < 9; ++x) Kc[kidx(x, I)] = acc[x];
     }
 }
 
@@ -606,6 +645,8 @@ void mg_build(Ctx& c, MG<T>& mg) {
     mg.coef = dev_alloc<double>(c, mg.L.size() * kCoefStride);
     mg.scale = dev_alloc<double>(c, mg.L.size());
     mg.maxbits = dev_alloc<unsigned>(c, mg.L.size());
+    if (mg.L.size() > 1)  // the largest coarse level's partial self blocks
+        mg.gal_self = dev_alloc<T>(c, (size_t)kGalSelfSplit * 9 * (size_t)mg.L[1].N);
     if (mg.L.size() > (size_t)kMaxMGLevels) {
         c.last_error = "lattice too large for the multigrid hierarchy";
         throw (int)FTS_ERR_UNSUPPORTED;
@@ -681,9 +722,11 @@ void mg_setup(Ctx& c, MG<T>& mg) {
         MGLevel<T>& L = mg.L[l];
         if (l > 0) {
             MGLevel<T>& P = mg.L[l - 1];
-            k_mg_galerkin<T><<<grid_for(c, L.N * 8), kThreads, 0, c.stream>>>(P.n, P.K, P.mask,
-                                                                               L.n, L.K, L.mask);
-            c.launches += 1;
+            k_mg_galerkin<T><<<grid_for(c, L.N * (7 + kGalSelfSplit)), kThreads, 0, c.stream>>>(
+                P.n, P.K, P.mask, L.n, L.K, L.mask, mg.gal_self);
+            k_mg_galerkin_self<T><<<grid_for(c, L.N), kThreads, 0, c.stream>>>(L.n, mg.gal_self,
+                                                                                L.K, L.mask);
+            c.launches += 2;
         }
         k_mg_dinv<T><<<grid_for(c, L.N), kThreads, 0, c.stream>>>(L.N, L.K, L.Di);
         mg_store(c, mg, l);
@@ -826,13 +869,15 @@ void mg_free(MG<T>& mg) {
                         (void*)L.d1, (void*)L.mask})
             if (p) cudaFree(p);
     }
-    for (void* p : {(void*)mg.lam, (void*)mg.coef, (void*)mg.scale, (void*)mg.maxbits})
+    for (void* p : {(void*)mg.lam, (void*)mg.coef, (void*)mg.scale, (void*)mg.maxbits,
+                    (void*)mg.gal_self})
         if (p) cudaFree(p);
     mg.tail_level = -1;
     mg.lam = nullptr;
     mg.coef = nullptr;
     mg.scale = nullptr;
     mg.maxbits = nullptr;
+    mg.gal_self = nullptr;
     mg.L.clear();
     mg.built = false;
 }

@@ -66,6 +66,7 @@ struct MG {
     double* coef = nullptr;          // device: Chebyshev coefficients per level
     double* scale = nullptr;         // device: stencil scale per level (Kh * scale = K)
     unsigned* maxbits = nullptr;     // device: max |K| per level (float bits)
+    T* gal_self = nullptr;           // device: partial self blocks of a Galerkin product
     std::vector<double> lam_host;
     bool built = false;
     // levels tail_level.. of every V-cycle run in one launch of a single
